@@ -1,0 +1,206 @@
+/*
+ * wemgpu.h — C ABI of the GB300 one-way wave-equation library.
+ *
+ * Drop-in boundary for the one-way downward-continuation hot path of
+ * arustam92/wem-fwi (split-step Fourier / PSPI depth step and the Born
+ * operators built on it).  Every entry point replaces one binding of the
+ * reference's pybind11 modules; the replaced interface is cited beside it.
+ *
+ * Conventions
+ *   - complex values are interleaved float pairs (re, im), C99-compatible
+ *     with `float _Complex` and `std::complex<float>`;
+ *   - 2D fields are row-major [nz][nx] with x fastest, the layout of the
+ *     reference's complex2DReg::_mat (complex/include/complex2DReg.h:41-46);
+ *   - frequency-extended fields are [nw][nz][nx];
+ *   - data are [ns][nr][nt] (real, time) or [ns][nr][nbin] (complex bins),
+ *     time/bin fastest, as in the reference's float3DReg / complex3DReg;
+ *   - pointers may be host or device memory; the library detects which and
+ *     moves host buffers itself (host calls are synchronous);
+ *   - `add` follows the reference: 0 zeroes the output before accumulating;
+ *   - no C++ exception crosses this boundary: every call returns a status
+ *     code; wem_last_error() gives the message of the last failure on the
+ *     calling thread.
+ *
+ * Threading: a handle is not thread-safe; use one handle per host thread /
+ * CUDA stream.  The reference drives one operator object per Python process
+ * and holds the GIL around every call (propagator/src/python/pyWEM.cpp).
+ */
+#ifndef WEMGPU_H
+#define WEMGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  WEM_OK       = 0,
+  WEM_EINVAL   = 1,  /* bad argument: shape, geometry, parameter, slowness <= 0 */
+  WEM_ENOMEM   = 2,  /* device or host allocation failed */
+  WEM_EDEVICE  = 3,  /* CUDA error reported by the runtime */
+  WEM_ETIMEOUT = 4,  /* a bounded device wait ran out (error word set by a kernel) */
+  WEM_ENOTIMPL = 5   /* valid request this build does not support */
+};
+
+/* propagator choice: par "prop" (propagator/src/OneWay.cpp:22-27) */
+enum { WEM_PROP_SSF = 0, WEM_PROP_PSPI = 1 };
+
+/* adjoint flavour of the Born operators.
+ * COMPAT reproduces the reference's adjoint exactly as coded: Scatter's
+ *   k-filter applied before the slowness scaling (propagator/src/Scatter.cpp:52-66)
+ *   and LinDown::adjoint clearing the last depth row of the gradient
+ *   (propagator/src/LinOneWay.cpp:64-65), with the frequencies of one shot
+ *   processed in order by one task.
+ * EXACT is the true transpose of the forward operator (dot test to 1e-5). */
+enum { WEM_ADJ_COMPAT = 0, WEM_ADJ_EXACT = 1 };
+
+/* reference-slowness partition (propagator/src/RefSampler.cpp:41-84).
+ * ASCODED replays the reference's sort of the nx-long history buffer;
+ * NEAREST is the textbook nearest-reference partition. */
+enum { WEM_REFS_ASCODED = 0, WEM_REFS_NEAREST = 1 };
+
+/* data representation of a call */
+enum { WEM_DATA_TIME = 0,    /* float  [ns][nr][nt]                         */
+       WEM_DATA_FREQ = 1 };  /* complex [ns][nr][nbin] (nbin >= nt + tpad) */
+
+/* Parameters.  Names and defaults follow the reference's paramObj keys
+ * (PropParam.h:45-85, OneStep.h:19-38, Device.h:39-85, wem_prop.cpp:43-44,
+ * LinOneWay.cpp:17, Scatter.cpp:12).  wem_params_default() fills defaults. */
+typedef struct wem_params {
+  /* model grid: axis 1 = x (fast), axis 2 = z */
+  int   nx, nz;
+  float ox, oz, dx, dz;
+  /* wavelet / data time axis */
+  int   nt;
+  float ot, dt;
+  /* regular acquisition (Device.h:39-63) */
+  int   ns;  float osx, osz, dsx, dsz;
+  int   nr;  float orx, orz, drx, drz;
+  /* irregular acquisition (Device.h:65-85): when non-NULL these coordinate
+   * arrays (ns resp. nr entries) replace the regular geometry above */
+  const float* src_x; const float* src_z;
+  const float* rec_x; const float* rec_z;
+  /* propagation */
+  int   prop;      /* WEM_PROP_SSF | WEM_PROP_PSPI            ("prop")    */
+  int   nref;      /* reference slownesses, default 1         ("nref")    */
+  int   tap;       /* FFT zero pad each side, default 0       ("tap")     */
+  int   pad;       /* model edge pad + taper width, default 0 ("pad")     */
+  int   tpad;      /* time zero pad at the end, default 0     ("tpad")    */
+  int   ngs, ngr;  /* cos^2 source / receiver half widths     ("ngs","ngr")*/
+  int   ntaylor;   /* Taylor terms of the Born scatter, default 1, max 4 */
+  float eps;       /* evanescent damping, default 0.04        ("eps")     */
+  float fmin;      /* default 1                               ("fmin")    */
+  float fmax;      /* default 0 (then nfreq bins from bin 1)  ("fmax")    */
+  int   nfreq;     /* used when fmax == 0, default 0          ("nfreq")   */
+  /* choices that have no reference key */
+  int   adjoint_mode;  /* WEM_ADJ_COMPAT (default) | WEM_ADJ_EXACT */
+  int   refs_mode;     /* WEM_REFS_ASCODED (default) | WEM_REFS_NEAREST */
+  int   nbin;          /* bins of WEM_DATA_FREQ data; 0 = nt + tpad */
+} wem_params;
+
+void wem_params_default(wem_params* p);
+
+/* number of propagated frequencies for these parameters
+ * (PropParam::get_nfreq, PropParam.h:42; pyWEM.cpp:36-39) */
+int wem_count_freqs(const wem_params* p, const float* wavelet, int* nfreq);
+
+const char* wem_last_error(void);
+const char* wem_version(void);
+
+/* ------------------------------------------------ nonlinear modelling (WEM) */
+typedef struct wem_handle wem_handle;
+
+/* replaces pyWEM.WEM(float1DReg wave, hypercube, paramObj)
+ * (propagator/src/python/pyWEM.cpp:21-23; WEMnl.cpp:11-21) */
+int wem_create(const wem_params* p, const float* wavelet, wem_handle** out);
+void wem_destroy(wem_handle* h);
+int wem_get_nfreq(wem_handle* h, int* nfreq);
+
+/* replaces WEM::forward(vector<complex2DReg> [s2, rho], float3DReg | complex3DReg, add)
+ * (WEMnl.cpp:39-82; wem_prop.cpp:9-78).  slow2/rho: complex [nz][nx];
+ * data: kind WEM_DATA_TIME (float) or WEM_DATA_FREQ (complex). */
+int wem_forward(wem_handle* h, const void* slow2, const void* rho,
+                void* data, int data_kind, int add);
+
+/* -------------------------------------------------- Born operator (BornFull) */
+typedef struct born_handle born_handle;
+
+/* replaces pyWEM.Born(float1DReg wave, vector<complex2DReg> [s2, rho], paramObj)
+ * (pyWEM.cpp:45-47; BornFull.cpp:13-37) */
+int born_create(const wem_params* p, const float* wavelet,
+                const void* bg_slow2, const void* bg_rho, born_handle** out);
+void born_destroy(born_handle* h);
+/* replaces BornFull::setBgSlow (BornFull.h:24-29; pyWEM.cpp:67-69) */
+int born_set_background(born_handle* h, const void* bg_slow2, const void* bg_rho);
+/* replaces BornFull::forward (BornFull.cpp:39-78; born_prop.cpp:11-116) */
+int born_forward(born_handle* h, const void* dslow2, const void* drho,
+                 void* data, int data_kind, int add);
+/* replaces BornFull::adjoint (BornFull.cpp:80-117; born_prop.cpp:119-235) */
+int born_adjoint(born_handle* h, void* dslow2, void* drho,
+                 const void* data, int data_kind, int add);
+
+/* ------------------------------------- frequency-extended operators (ext*) */
+typedef struct extwem_handle extwem_handle;
+typedef struct extborn_handle extborn_handle;
+
+/* replaces pyWEM.extWEM (pyWEM.cpp:142-156; extWEM.cpp:9-70; ext_wem_prop.cpp:8-59).
+ * model: complex [nfreq][nz][nx] slowness^2 and density. */
+int extwem_create(const wem_params* p, const float* wavelet, extwem_handle** out);
+void extwem_destroy(extwem_handle* h);
+int extwem_forward(extwem_handle* h, const void* slow2, const void* rho,
+                   void* data, int data_kind, int add);
+
+/* replaces pyWEM.extBorn (pyWEM.cpp:159-186; extBornFull.cpp:11-121;
+ * ext_born_prop.cpp:8-194) */
+int extborn_create(const wem_params* p, const float* wavelet,
+                   const void* bg_slow2, const void* bg_rho, extborn_handle** out);
+void extborn_destroy(extborn_handle* h);
+int extborn_set_background(extborn_handle* h, const void* bg_slow2, const void* bg_rho);
+int extborn_forward(extborn_handle* h, const void* dslow2, const void* drho,
+                    void* data, int data_kind, int add);
+int extborn_adjoint(extborn_handle* h, void* dslow2, void* drho,
+                    const void* data, int data_kind, int add);
+
+/* --------------------------------------------- row-level operators (wem_ops)
+ * Batched forms of the per-row operators that py_wem_ops binds
+ * (propagator/src/python/py_wem_ops.cpp:24-208, wem_ops.py:6-137).
+ * A wemop handle holds one padded background slowness [nz][nxg] (nxg =
+ * nx + 2 pad, already edge padded, as the drivers pass it) and the
+ * RefSampler built on it. */
+typedef struct wemop_handle wemop_handle;
+
+int wemop_create(const wem_params* p, const void* slow_padded, int nxg,
+                 wemop_handle** out);
+void wemop_destroy(wemop_handle* h);
+
+/* SSF / PSPI depth step of nrow rows [nrow][nxg] at depth iz, frequency
+ * freq (Hz).  Replaces SSF::forward/adjoint and PSPI::forward/adjoint
+ * (SSF.cpp:8-60, PSPI.cpp:8-53).  adj=0: out = P in; adj=1: out = P^H in. */
+int wemop_onestep(wemop_handle* h, int iz, float freq, int adj,
+                  const void* in, void* out, int nrow, int add);
+
+/* Down / Up over whole fields [nrow][nz][nxg].  Replaces Down/Up::forward /
+ * adjoint (OneWay.cpp:32-109).  up=0: Down, up=1: Up.  When in == out the
+ * call is the in-place recursion the drivers use; otherwise the reference's
+ * out-of-place single-step semantics apply. */
+int wemop_oneway(wemop_handle* h, int up, float freq, int adj,
+                 const void* in, void* out, int nrow, int add);
+
+/* Taylor Born scatter of nrow rows at depth iz.  Replaces
+ * Scatter::forward/adjoint (Scatter.cpp:35-66); the adjoint flavour follows
+ * the handle's adjoint_mode. */
+int wemop_scatter(wemop_handle* h, int iz, float freq, int adj,
+                  const void* in, void* out, int nrow, int add);
+
+/* Reference slownesses [nz][nref] (complex) and the reference index of each
+ * grid point [nz][nxg] (-1 = no reference) of the handle's RefSampler.
+ * Replaces RefSampler::getRefSlow / getRefLoc (RefSampler.h:19-20). */
+int wemop_refsampler(wemop_handle* h, void* sref, int* refidx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WEMGPU_H */

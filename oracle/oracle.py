@@ -1,0 +1,186 @@
+"""ORACLE — test infrastructure only.  ctypes front end of the CPU
+restatement in ``wem_oracle.cpp``; only tests/, ``__graft_entry__.smoke()``
+and bench.py's CPU-baseline leg import it, as the checker.
+
+PARITY UNPINNED: the reference cannot be built here (FFTW, TBB, Boost, SEP
+I/O and ISPC are absent) and its tests hold no numeric golden vectors; the
+restatement is pinned by the reference's structural known-answer test
+(extWEM == WEM on a frequency-constant model), dot tests, its fp64 twin and
+numpy.fft.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_ROOT = os.path.dirname(_HERE)
+sys.path.insert(0, os.path.join(_ROOT, "wem-fwi_gb300"))
+from wemgpu.params import WemParams, WEM_DATA_TIME, WEM_DATA_FREQ  # noqa: E402
+
+_LIB = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the restatement with g++ (no external libraries)."""
+    if force or not os.path.exists(_LIB):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = ctypes.CDLL(_LIB)
+        _lib.oracle_last_error.restype = ctypes.c_char_p
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _call(name, *args):
+    rc = getattr(lib(), name)(*args)
+    if rc != 0:
+        raise RuntimeError(f"{name}: {lib().oracle_last_error().decode()} (status {rc})")
+
+
+def _c64(a):
+    return np.ascontiguousarray(a, dtype=np.complex64)
+
+
+def count_freqs(p: WemParams):
+    n = ctypes.c_int()
+    _call("oracle_count_freqs", ctypes.byref(p), ctypes.byref(n), None, None)
+    bins = np.zeros(n.value, np.int32)
+    freqs = np.zeros(n.value, np.float32)
+    _call("oracle_count_freqs", ctypes.byref(p), ctypes.byref(n), _ptr(bins), _ptr(freqs))
+    return n.value, bins, freqs
+
+
+def devices(p: WemParams):
+    sx, sz = np.zeros(p.ns, np.int32), np.zeros(p.ns, np.int32)
+    rx, rz = np.zeros(p.nr, np.int32), np.zeros(p.nr, np.int32)
+    _call("oracle_devices", ctypes.byref(p), _ptr(sx), _ptr(sz), _ptr(rx), _ptr(rz))
+    return sx, sz, rx, rz
+
+
+def fft(x, sign=-1):
+    """Unnormalised DFT in double precision (sign -1 forward)."""
+    v = np.ascontiguousarray(x, dtype=np.complex128).copy()
+    _call("oracle_fft", ctypes.c_int(v.size), _ptr(v), ctypes.c_int(sign))
+    return v
+
+
+def _nbin(p):
+    return p.nbin if p.nbin else p.nt + p.tpad
+
+
+def _data_out(p, kind, data=None):
+    if data is not None:
+        return data
+    if kind == WEM_DATA_TIME:
+        return np.zeros((p.ns, p.nr, p.nt), np.float32)
+    return np.zeros((p.ns, p.nr, _nbin(p)), np.complex64)
+
+
+def wem_forward(p, wavelet, s2, rho, kind=WEM_DATA_FREQ, data=None, add=False, prec=32, nthreads=0):
+    out = _data_out(p, kind, data)
+    _call("oracle_wem_forward", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(s2)), _ptr(_c64(rho)), _ptr(out), kind, int(add), prec, nthreads)
+    return out
+
+
+def born_forward(p, wavelet, bs2, brho, ds2, drho, kind=WEM_DATA_FREQ, data=None, add=False,
+                 prec=32, nthreads=0):
+    out = _data_out(p, kind, data)
+    _call("oracle_born_forward", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(bs2)), _ptr(_c64(brho)), _ptr(_c64(ds2)), _ptr(_c64(drho)), _ptr(out),
+          kind, int(add), prec, nthreads)
+    return out
+
+
+def born_adjoint(p, wavelet, bs2, brho, data, kind=WEM_DATA_FREQ, ds2=None, drho=None, add=False,
+                 prec=32, nthreads=0, fchunks=1):
+    shape = (p.nz, p.nx)
+    ds2 = np.zeros(shape, np.complex64) if ds2 is None else ds2
+    drho = np.zeros(shape, np.complex64) if drho is None else drho
+    d = np.ascontiguousarray(data, np.float32 if kind == WEM_DATA_TIME else np.complex64)
+    _call("oracle_born_adjoint", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(bs2)), _ptr(_c64(brho)), _ptr(ds2), _ptr(drho), _ptr(d), kind, int(add), prec,
+          nthreads, fchunks)
+    return ds2, drho
+
+
+def extwem_forward(p, wavelet, s2, rho, kind=WEM_DATA_FREQ, data=None, add=False, prec=32, nthreads=0):
+    out = _data_out(p, kind, data)
+    _call("oracle_extwem_forward", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(s2)), _ptr(_c64(rho)), _ptr(out), kind, int(add), prec, nthreads)
+    return out
+
+
+def extborn_forward(p, wavelet, bs2, brho, ds2, drho, kind=WEM_DATA_FREQ, data=None, add=False,
+                    prec=32, nthreads=0):
+    out = _data_out(p, kind, data)
+    _call("oracle_extborn_forward", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(bs2)), _ptr(_c64(brho)), _ptr(_c64(ds2)), _ptr(_c64(drho)), _ptr(out),
+          kind, int(add), prec, nthreads)
+    return out
+
+
+def extborn_adjoint(p, wavelet, bs2, brho, data, kind=WEM_DATA_FREQ, add=False, prec=32, nthreads=0):
+    nf = count_freqs(p)[0]
+    ds2 = np.zeros((nf, p.nz, p.nx), np.complex64)
+    drho = np.zeros((nf, p.nz, p.nx), np.complex64)
+    d = np.ascontiguousarray(data, np.float32 if kind == WEM_DATA_TIME else np.complex64)
+    _call("oracle_extborn_adjoint", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(bs2)), _ptr(_c64(brho)), _ptr(ds2), _ptr(drho), _ptr(d), kind, int(add), prec,
+          nthreads)
+    return ds2, drho
+
+
+def onestep(p, slow_padded, iz, freq, adj, x, out=None, add=False, prec=32):
+    x = _c64(x)
+    nxg = slow_padded.shape[-1]
+    out = np.zeros_like(x) if out is None else out
+    _call("oracle_onestep", ctypes.byref(p), _ptr(_c64(slow_padded)), nxg, iz, ctypes.c_float(freq),
+          int(adj), _ptr(x), _ptr(out), x.size // nxg, int(add), prec)
+    return out
+
+
+def oneway(p, slow_padded, up, freq, adj, x, out=None, add=False, prec=32):
+    """out=None with add=True means the in-place recursion (model is data)."""
+    nxg = slow_padded.shape[-1]
+    x = _c64(x)
+    if out is None and add:
+        out = x
+    elif out is None:
+        out = np.zeros_like(x)
+    nrow = x.size // (nxg * p.nz)
+    _call("oracle_oneway", ctypes.byref(p), _ptr(_c64(slow_padded)), nxg, int(up), ctypes.c_float(freq),
+          int(adj), _ptr(x), _ptr(out), nrow, int(add), prec)
+    return out
+
+
+def scatter(p, slow_padded, iz, freq, adj, x, out=None, add=False, prec=32):
+    x = _c64(x)
+    nxg = slow_padded.shape[-1]
+    out = np.zeros_like(x) if out is None else out
+    _call("oracle_scatter", ctypes.byref(p), _ptr(_c64(slow_padded)), nxg, iz, ctypes.c_float(freq),
+          int(adj), _ptr(x), _ptr(out), x.size // nxg, int(add), prec)
+    return out
+
+
+def refsampler(p, slow_padded):
+    nxg = slow_padded.shape[-1]
+    sref = np.zeros((p.nz, p.nref), np.complex64)
+    idx = np.zeros((p.nz, nxg), np.int32)
+    _call("oracle_refsampler", ctypes.byref(p), _ptr(_c64(slow_padded)), nxg, _ptr(sref), _ptr(idx))
+    return sref, idx

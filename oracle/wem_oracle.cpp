@@ -1,0 +1,696 @@
+// ORACLE — test infrastructure only (see wem_oracle.hpp).  Drivers of the
+// CPU restatement and the extern "C" surface that tests/ and bench.py reach
+// through ctypes.  PARITY UNPINNED (no reference build, no golden vectors).
+//
+// Drivers follow the reference's per-(shot, frequency) call sequence
+// literally, without the algebraic fusions the GPU library makes, so that
+// those fusions are checked rather than restated.
+
+#include <atomic>
+#include <functional>
+#include <thread>
+
+#include "wem_oracle.hpp"
+
+namespace wo {
+namespace {
+
+thread_local std::string g_err;
+
+template <class Fn>
+void parallel_for(int ntask, int nthreads, Fn fn) {
+  if (nthreads <= 0) nthreads = (int)std::max(1u, std::thread::hardware_concurrency());
+  nthreads = std::max(1, std::min(nthreads, ntask));
+  if (nthreads == 1) {
+    for (int t = 0; t < ntask; ++t) fn(t, 0);
+    return;
+  }
+  // static block partition, as tbb::static_partitioner over a blocked range
+  // (propagator/src/wem_prop.cpp:11,76)
+  std::vector<std::thread> th;
+  std::exception_ptr err;
+  std::atomic<bool> failed{false};
+  for (int i = 0; i < nthreads; ++i) {
+    int b = (int)((long long)ntask * i / nthreads), e = (int)((long long)ntask * (i + 1) / nthreads);
+    th.emplace_back([&, b, e, i] {
+      try {
+        for (int t = b; t < e; ++t) fn(t, i);
+      } catch (...) {
+        if (!failed.exchange(true)) err = std::current_exception();
+      }
+    });
+  }
+  for (auto& t : th) t.join();
+  if (err) std::rethrow_exception(err);
+}
+
+template <class R>
+std::vector<C<R>> load(const float* p, size_t n) {
+  std::vector<C<R>> v(n);
+  for (size_t i = 0; i < n; ++i) v[i] = C<R>((R)p[2 * i], (R)p[2 * i + 1]);
+  return v;
+}
+
+template <class R>
+void store(float* p, const C<R>* v, size_t n, bool add) {
+  for (size_t i = 0; i < n; ++i) {
+    float re = (float)v[i].real(), im = (float)v[i].imag();
+    if (add) { p[2 * i] += re; p[2 * i + 1] += im; } else { p[2 * i] = re; p[2 * i + 1] = im; }
+  }
+}
+
+// Quantities every driver derives from the parameters (PropParam.h:24-85,
+// Device.h), for one real type.
+template <class R>
+struct Problem {
+  wem_params p;
+  Freqs F;
+  Devices src, rec;
+  int nxg, nbin;
+  std::vector<C<R>> wave_f;  // unitary FFT of the time-padded wavelet
+
+  Problem(const wem_params& p_, const float* wavelet) : p(p_) {
+    check(p.nx > 0 && p.nz > 1, "model must have nx > 0 and nz > 1");
+    check(p.dx > 0 && p.dz > 0, "grid spacing must be positive");
+    check(p.nref >= 1, "nref must be >= 1");
+    check(p.pad >= 0 && p.tap >= 0 && p.tpad >= 0, "pad/tap/tpad must be >= 0");
+    check(p.pad != 1, "pad == 1 makes the taper divide by zero (Taper.h:19)");
+    F = make_freqs(p);
+    src = make_devices(p, true);
+    rec = make_devices(p, false);
+    nxg = p.nx + 2 * p.pad;
+    nbin = p.nbin ? p.nbin : F.nt_pad;
+    for (int b : F.bin) check(b >= 0 && b < F.nt_pad && b < nbin, "frequency bin beyond the data axis");
+    // FFT1_r forward of the wavelet (FFT1_r.cpp:74-83 via PropParam.h:49-54)
+    Fft<R> fft(F.nt_pad);
+    wave_f.assign(F.nt_pad, C<R>(0));
+    for (int i = 0; i < p.nt; ++i) wave_f[i] = C<R>((R)wavelet[i], 0);
+    std::vector<C<R>> scr(F.nt_pad);
+    fft.run(wave_f.data(), -1, scr.data());
+    R s = (R)(1.0 / std::sqrt((double)F.nt_pad));
+    for (auto& v : wave_f) v *= s;
+  }
+  int nfreq() const { return (int)F.freq.size(); }
+  Inject<R> src_inj(int is) const { return Inject<R>({src.ix[is]}, {src.iz[is]}, p.ngs, p.pad); }
+  Inject<R> rec_inj() const { return Inject<R>(rec.ix, rec.iz, p.ngr, p.pad); }
+};
+
+// Complex bins <-> real time traces (FFT1_r.cpp, WEMnl.cpp:39-65,
+// BornFull.cpp:80-102).  data_f [ns][nr][nt_pad].
+template <class R>
+void bins_to_time(const Problem<R>& P, const std::vector<C<R>>& df, float* dt, bool add, int nthreads) {
+  int ntr = P.p.ns * P.p.nr, n = P.F.nt_pad, nt = P.p.nt;
+  Fft<R> fft(n);
+  R s = (R)(1.0 / std::sqrt((double)n));
+  parallel_for(ntr, nthreads, [&](int tr, int) {
+    std::vector<C<R>> x(df.begin() + (size_t)tr * n, df.begin() + (size_t)(tr + 1) * n), scr(n);
+    fft.run(x.data(), +1, scr.data());
+    float* o = dt + (size_t)tr * nt;
+    for (int t = 0; t < nt; ++t) {
+      float v = (float)(x[t].real() * s);
+      o[t] = add ? o[t] + v : v;
+    }
+  });
+}
+
+template <class R>
+std::vector<C<R>> time_to_bins(const Problem<R>& P, const float* dt, int nthreads) {
+  int ntr = P.p.ns * P.p.nr, n = P.F.nt_pad, nt = P.p.nt;
+  std::vector<C<R>> df((size_t)ntr * n);
+  Fft<R> fft(n);
+  R s = (R)(1.0 / std::sqrt((double)n));
+  parallel_for(ntr, nthreads, [&](int tr, int) {
+    C<R>* x = df.data() + (size_t)tr * n;
+    for (int t = 0; t < n; ++t) x[t] = C<R>(t < nt ? (R)dt[(size_t)tr * nt + t] : R(0), 0);
+    std::vector<C<R>> scr(n);
+    fft.run(x, -1, scr.data());
+    for (int t = 0; t < n; ++t) x[t] *= s;
+  });
+  return df;
+}
+
+// complex data view [ns][nr][nb]
+template <class R>
+struct DataF {
+  std::vector<C<R>> v;
+  int ns, nr, nb;
+  C<R>* at(int is, int ir, int b) { return &v[((size_t)is * nr + ir) * nb + b]; }
+};
+
+// ------------------------------------------------------------ WEM forward
+// WEM::full_fwd (propagator/src/wem_prop.cpp:9-78) for one padded model.
+template <class R>
+void wem_row(const Problem<R>& P, const Core<R>& core, const std::vector<C<R>>& r, int is, int f,
+             DataF<R>& D, int bin_col, std::vector<C<R>>& W, Work<R>& wk) {
+  const int nx = core.nxg, nz = core.nz;
+  R w = Core<R>::omega(P.F.freq[f]);
+  std::fill(W.begin(), W.end(), C<R>(0));
+  C<R> wv = P.wave_f[P.F.bin[f]];
+  P.src_inj(is).spread(W.data(), nx, &wv);
+  down_fwd(core, w, W.data(), W.data(), true, wk);
+  Inject<R> rec = P.rec_inj();
+  std::vector<C<R>> vals(rec.ix.size());
+  auto record = [&]() {
+    for (size_t i = 0; i < vals.size(); ++i) vals[i] = *D.at(is, (int)i, bin_col);
+    rec.gather(W.data(), nx, vals.data());
+    for (size_t i = 0; i < vals.size(); ++i) *D.at(is, (int)i, bin_col) = vals[i];
+  };
+  record();
+  for (size_t i = 0; i < W.size(); ++i) W[i] = r[i] * W[i];
+  up_fwd(core, w, W.data(), W.data(), true, wk);
+  record();
+  (void)nz;
+}
+
+// data in/out helpers shared by all drivers
+template <class R>
+DataF<R> new_dataf(const Problem<R>& P) {
+  DataF<R> D;
+  D.ns = P.p.ns; D.nr = P.p.nr; D.nb = P.F.nt_pad;
+  D.v.assign((size_t)D.ns * D.nr * D.nb, C<R>(0));
+  return D;
+}
+
+template <class R>
+void emit_data(const Problem<R>& P, DataF<R>& D, void* data, int kind, bool add, int nthreads) {
+  if (kind == WEM_DATA_TIME) {
+    bins_to_time(P, D.v, (float*)data, add, nthreads);
+  } else {
+    float* o = (float*)data;
+    for (int is = 0; is < D.ns; ++is)
+      for (int ir = 0; ir < D.nr; ++ir)
+        for (int b = 0; b < P.nbin; ++b) {
+          size_t k = (((size_t)is * D.nr + ir) * P.nbin + b) * 2;
+          C<R> v = b < D.nb ? *D.at(is, ir, b) : C<R>(0);
+          if (add) { o[k] += (float)v.real(); o[k + 1] += (float)v.imag(); }
+          else { o[k] = (float)v.real(); o[k + 1] = (float)v.imag(); }
+        }
+  }
+}
+
+template <class R>
+DataF<R> absorb_data(const Problem<R>& P, const void* data, int kind, int nthreads) {
+  DataF<R> D = new_dataf(P);
+  if (kind == WEM_DATA_TIME) {
+    D.v = time_to_bins(P, (const float*)data, nthreads);
+  } else {
+    const float* s = (const float*)data;
+    for (int is = 0; is < D.ns; ++is)
+      for (int ir = 0; ir < D.nr; ++ir)
+        for (int b = 0; b < std::min(P.nbin, D.nb); ++b) {
+          size_t k = (((size_t)is * D.nr + ir) * P.nbin + b) * 2;
+          *D.at(is, ir, b) = C<R>((R)s[k], (R)s[k + 1]);
+        }
+  }
+  return D;
+}
+
+template <class R>
+void wem_forward(const wem_params& p, const float* wavelet, const float* s2, const float* rho,
+                 void* data, int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  const int nx = P.nxg, nz = p.nz;
+  std::vector<C<R>> s = load<R>(s2, (size_t)p.nx * nz), d = load<R>(rho, (size_t)p.nx * nz);
+  std::vector<C<R>> sp((size_t)nx * nz), dp((size_t)nx * nz);
+  pad_x(s.data(), sp.data(), nz, p.nx, p.pad, true);
+  pad_x(d.data(), dp.data(), nz, p.nx, p.pad, true);
+  std::vector<C<R>> r = reflect_coefs(sp.data(), dp.data(), nx, nz);
+  Core<R> core(p, sp.data(), nx, nz);
+  DataF<R> D = new_dataf(P);
+  int nf = P.nfreq(), ns = p.ns;
+  parallel_for(ns * nf, nthreads, [&](int t, int) {
+    int is = t / nf, f = t % nf;
+    Work<R> wk(core.N, nx);
+    std::vector<C<R>> W((size_t)nx * nz);
+    wem_row(P, core, r, is, f, D, P.F.bin[f], W, wk);
+  });
+  emit_data(P, D, data, kind, add, nthreads);
+}
+
+// -------------------------------------------------------------- Born
+// One shot/frequency-range task state (born_prop.cpp:11-235).
+template <class R>
+struct BornBg {
+  std::vector<C<R>> sp, dp, r;  // padded background and reflection coefficients
+  Core<R>* core = nullptr;
+  DRefl<R>* drefl = nullptr;
+};
+
+template <class R>
+void born_row_fwd(const Problem<R>& P, const Core<R>& core, const std::vector<C<R>>& r, const DRefl<R>& dR,
+                  const std::vector<C<R>>& gm0, const std::vector<C<R>>& gm1, int is, int f, DataF<R>& D,
+                  std::vector<C<R>>& bg, std::vector<C<R>>& sc, std::vector<C<R>>& dr, Work<R>& wk) {
+  const int nx = core.nxg;
+  const int bin = P.F.bin[f];
+  R w = Core<R>::omega(P.F.freq[f]);
+  Inject<R> rec = P.rec_inj();
+  std::vector<C<R>> vals(rec.ix.size());
+  auto record = [&](const std::vector<C<R>>& W) {
+    for (size_t i = 0; i < vals.size(); ++i) vals[i] = *D.at(is, (int)i, bin);
+    rec.gather(W.data(), nx, vals.data());
+    for (size_t i = 0; i < vals.size(); ++i) *D.at(is, (int)i, bin) = vals[i];
+  };
+  // down background wavefield
+  std::fill(bg.begin(), bg.end(), C<R>(0));
+  C<R> wv = P.wave_f[bin];
+  P.src_inj(is).spread(bg.data(), nx, &wv);
+  down_fwd(core, w, bg.data(), bg.data(), true, wk);
+  // forward scattering
+  lindown_fwd(core, w, bg.data(), gm0.data(), sc.data(), false, wk);
+  down_fwd(core, w, sc.data(), sc.data(), true, wk);
+  record(sc);
+  // linearisation of the reflectivity: Born_refl::forward (Born_refl.cpp:19-27)
+  std::fill(dr.begin(), dr.end(), C<R>(0));
+  dR.fwd(gm0.data(), gm1.data(), dr.data());
+  for (size_t i = 0; i < sc.size(); ++i) sc[i] = bg[i] * dr[i];
+  up_fwd(core, w, sc.data(), sc.data(), true, wk);
+  record(sc);
+  // down-scattering
+  lindown_fwd(core, w, bg.data(), gm0.data(), sc.data(), false, wk);
+  down_fwd(core, w, sc.data(), sc.data(), true, wk);
+  for (size_t i = 0; i < sc.size(); ++i) sc[i] = r[i] * sc[i];
+  up_fwd(core, w, sc.data(), sc.data(), true, wk);
+  record(sc);
+  // up background wavefield
+  for (size_t i = 0; i < bg.size(); ++i) bg[i] = r[i] * bg[i];
+  up_fwd(core, w, bg.data(), bg.data(), true, wk);
+  // up-scattering
+  linup_fwd(core, w, bg.data(), gm0.data(), sc.data(), false, wk);
+  up_fwd(core, w, sc.data(), sc.data(), true, wk);
+  record(sc);
+}
+
+template <class R>
+void born_row_adj(const Problem<R>& P, const Core<R>& core, const std::vector<C<R>>& r, const DRefl<R>& dR,
+                  std::vector<C<R>>& gm0, std::vector<C<R>>& gm1, int is, int f, DataF<R>& D, bool exact,
+                  bool ext_order, std::vector<C<R>>& bg, std::vector<C<R>>& sc, std::vector<C<R>>& dr,
+                  Work<R>& wk) {
+  const int nx = core.nxg;
+  const int bin = P.F.bin[f];
+  R w = Core<R>::omega(P.F.freq[f]);
+  Inject<R> rec = P.rec_inj();
+  std::vector<C<R>> vals(rec.ix.size());
+  auto inject_data = [&]() {  // Injection::forward 3D, add = 0
+    std::fill(sc.begin(), sc.end(), C<R>(0));
+    for (size_t i = 0; i < vals.size(); ++i) vals[i] = *D.at(is, (int)i, bin);
+    rec.spread(sc.data(), nx, vals.data());
+  };
+  auto born_refl_adj = [&]() {  // Born_refl::adjoint (Born_refl.cpp:29-40)
+    inject_data();
+    up_adj(core, w, sc.data(), sc.data(), true, wk);
+    for (size_t i = 0; i < sc.size(); ++i) dr[i] = std::conj(bg[i]) * sc[i];
+    dR.adj(gm0.data(), gm1.data(), dr.data());
+  };
+  auto fwd_scatter_adj = [&]() {
+    inject_data();
+    down_adj(core, w, sc.data(), sc.data(), true, wk);
+    lindown_adj(core, w, bg.data(), gm0.data(), sc.data(), true, exact, wk);
+  };
+  std::fill(bg.begin(), bg.end(), C<R>(0));
+  C<R> wv = P.wave_f[bin];
+  P.src_inj(is).spread(bg.data(), nx, &wv);
+  down_fwd(core, w, bg.data(), bg.data(), true, wk);
+  // born_prop.cpp:193-199 reflectivity first; ext_born_prop.cpp:159-165 the
+  // forward-scattering term first
+  if (ext_order) { fwd_scatter_adj(); born_refl_adj(); }
+  else { born_refl_adj(); fwd_scatter_adj(); }
+  // down-scattering
+  inject_data();
+  up_adj(core, w, sc.data(), sc.data(), true, wk);
+  for (size_t i = 0; i < sc.size(); ++i) sc[i] = std::conj(r[i]) * sc[i];
+  down_adj(core, w, sc.data(), sc.data(), true, wk);
+  lindown_adj(core, w, bg.data(), gm0.data(), sc.data(), true, exact, wk);
+  // up background wavefield
+  for (size_t i = 0; i < bg.size(); ++i) bg[i] = r[i] * bg[i];
+  up_fwd(core, w, bg.data(), bg.data(), true, wk);
+  // up-scattering
+  inject_data();
+  up_adj(core, w, sc.data(), sc.data(), true, wk);
+  linup_adj(core, w, bg.data(), gm0.data(), sc.data(), true, exact, wk);
+}
+
+template <class R>
+struct PaddedModel {
+  std::vector<C<R>> s, d;
+  PaddedModel(const wem_params& p, const float* s2, const float* rho, bool extend, size_t nslices = 1) {
+    int nxg = p.nx + 2 * p.pad;
+    size_t n = (size_t)p.nx * p.nz, ng = (size_t)nxg * p.nz;
+    s.resize(ng * nslices); d.resize(ng * nslices);
+    for (size_t k = 0; k < nslices; ++k) {
+      std::vector<C<R>> a = load<R>(s2 + 2 * n * k, n), b = load<R>(rho + 2 * n * k, n);
+      pad_x(a.data(), s.data() + ng * k, p.nz, p.nx, p.pad, extend);
+      pad_x(b.data(), d.data() + ng * k, p.nz, p.nx, p.pad, extend);
+    }
+  }
+};
+
+template <class R>
+void born_forward(const wem_params& p, const float* wavelet, const float* bs2, const float* brho,
+                  const float* ds2, const float* drho, void* data, int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  const int nx = P.nxg, nz = p.nz;
+  PaddedModel<R> bgm(p, bs2, brho, true), dm(p, ds2, drho, false);
+  std::vector<C<R>> r = reflect_coefs(bgm.s.data(), bgm.d.data(), nx, nz);
+  DRefl<R> dR(bgm.s.data(), bgm.d.data(), nx, nz);
+  Core<R> core(p, bgm.s.data(), nx, nz);
+  DataF<R> D = new_dataf(P);
+  int nf = P.nfreq(), ns = p.ns;
+  parallel_for(ns * nf, nthreads, [&](int t, int) {
+    int is = t / nf, f = t % nf;
+    Work<R> wk(core.N, nx);
+    std::vector<C<R>> bg((size_t)nx * nz), sc((size_t)nx * nz), dr((size_t)nx * nz);
+    born_row_fwd(P, core, r, dR, dm.s, dm.d, is, f, D, bg, sc, dr, wk);
+  });
+  emit_data(P, D, data, kind, add, nthreads);
+}
+
+// fchunks: tasks per shot over the frequency axis.  1 reproduces the
+// compat semantics exactly (the shot's frequencies in order in one task);
+// more chunks only change the last depth row of the compat gradient.
+template <class R>
+void born_adjoint(const wem_params& p, const float* wavelet, const float* bs2, const float* brho,
+                  float* ds2, float* drho, const void* data, int kind, bool add, int nthreads, int fchunks) {
+  Problem<R> P(p, wavelet);
+  const int nx = P.nxg, nz = p.nz;
+  const bool exact = p.adjoint_mode == WEM_ADJ_EXACT;
+  PaddedModel<R> bgm(p, bs2, brho, true);
+  std::vector<C<R>> r = reflect_coefs(bgm.s.data(), bgm.d.data(), nx, nz);
+  DRefl<R> dR(bgm.s.data(), bgm.d.data(), nx, nz);
+  Core<R> core(p, bgm.s.data(), nx, nz);
+  DataF<R> D = absorb_data(P, data, kind, nthreads);
+  int nf = P.nfreq(), ns = p.ns;
+  fchunks = std::max(1, std::min(fchunks, nf));
+  int ntask = ns * fchunks;
+  size_t ng = (size_t)nx * nz;
+  std::vector<std::vector<C<R>>> g0(ntask), g1(ntask);
+  parallel_for(ntask, nthreads, [&](int t, int) {
+    int is = t / fchunks, ch = t % fchunks;
+    int fb = (int)((long long)nf * ch / fchunks), fe = (int)((long long)nf * (ch + 1) / fchunks);
+    Work<R> wk(core.N, nx);
+    std::vector<C<R>> bg(ng), sc(ng), dr(ng);
+    g0[t].assign(ng, C<R>(0));
+    g1[t].assign(ng, C<R>(0));
+    for (int f = fb; f < fe; ++f)
+      born_row_adj(P, core, r, dR, g0[t], g1[t], is, f, D, exact, false, bg, sc, dr, wk);
+  });
+  // unpad (Pad::adjoint, Pad.h:98-107) and sum the tasks in order: the
+  // reference adds them without a lock (born_prop.cpp:220-232)
+  size_t nm = (size_t)p.nx * nz;
+  std::vector<C<R>> m0(nm, 0), m1(nm, 0);
+  for (int t = 0; t < ntask; ++t)
+    for (int iz = 0; iz < nz; ++iz)
+      for (int ix = 0; ix < p.nx; ++ix) {
+        m0[(size_t)iz * p.nx + ix] += g0[t][(size_t)iz * nx + ix + p.pad];
+        m1[(size_t)iz * p.nx + ix] += g1[t][(size_t)iz * nx + ix + p.pad];
+      }
+  store(ds2, m0.data(), nm, add);
+  store(drho, m1.data(), nm, add);
+}
+
+// --------------------------------------------------- frequency-extended
+// extWEM::full_fwd (ext_wem_prop.cpp:8-59): one model slice per frequency.
+template <class R>
+void extwem_forward(const wem_params& p, const float* wavelet, const float* s2, const float* rho,
+                    void* data, int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
+  PaddedModel<R> m(p, s2, rho, true, nf);
+  size_t ng = (size_t)nx * nz;
+  DataF<R> D = new_dataf(P);
+  parallel_for(nf, nthreads, [&](int f, int) {
+    const C<R>* sp = m.s.data() + ng * f;
+    const C<R>* dp = m.d.data() + ng * f;
+    Core<R> core(p, sp, nx, nz);
+    std::vector<C<R>> r = reflect_coefs(sp, dp, nx, nz);
+    Work<R> wk(core.N, nx);
+    std::vector<C<R>> W(ng);
+    for (int is = 0; is < p.ns; ++is) wem_row(P, core, r, is, f, D, P.F.bin[f], W, wk);
+  });
+  emit_data(P, D, data, kind, add, nthreads);
+}
+
+template <class R>
+void extborn_forward(const wem_params& p, const float* wavelet, const float* bs2, const float* brho,
+                     const float* ds2, const float* drho, void* data, int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
+  PaddedModel<R> bgm(p, bs2, brho, true, nf), dm(p, ds2, drho, false, nf);
+  size_t ng = (size_t)nx * nz;
+  DataF<R> D = new_dataf(P);
+  parallel_for(nf, nthreads, [&](int f, int) {
+    const C<R>* sp = bgm.s.data() + ng * f;
+    const C<R>* dp = bgm.d.data() + ng * f;
+    Core<R> core(p, sp, nx, nz);
+    std::vector<C<R>> r = reflect_coefs(sp, dp, nx, nz);
+    DRefl<R> dR(sp, dp, nx, nz);
+    std::vector<C<R>> g0(dm.s.begin() + ng * f, dm.s.begin() + ng * (f + 1));
+    std::vector<C<R>> g1(dm.d.begin() + ng * f, dm.d.begin() + ng * (f + 1));
+    Work<R> wk(core.N, nx);
+    std::vector<C<R>> bg(ng), sc(ng), dr(ng);
+    for (int is = 0; is < p.ns; ++is) born_row_fwd(P, core, r, dR, g0, g1, is, f, D, bg, sc, dr, wk);
+  });
+  emit_data(P, D, data, kind, add, nthreads);
+}
+
+template <class R>
+void extborn_adjoint(const wem_params& p, const float* wavelet, const float* bs2, const float* brho,
+                     float* ds2, float* drho, const void* data, int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
+  const bool exact = p.adjoint_mode == WEM_ADJ_EXACT;
+  PaddedModel<R> bgm(p, bs2, brho, true, nf);
+  size_t ng = (size_t)nx * nz, nm = (size_t)p.nx * nz;
+  DataF<R> D = absorb_data(P, data, kind, nthreads);
+  std::vector<C<R>> m0(nm * nf), m1(nm * nf);
+  parallel_for(nf, nthreads, [&](int f, int) {
+    const C<R>* sp = bgm.s.data() + ng * f;
+    const C<R>* dp = bgm.d.data() + ng * f;
+    Core<R> core(p, sp, nx, nz);
+    std::vector<C<R>> r = reflect_coefs(sp, dp, nx, nz);
+    DRefl<R> dR(sp, dp, nx, nz);
+    std::vector<C<R>> g0(ng, 0), g1(ng, 0);
+    Work<R> wk(core.N, nx);
+    std::vector<C<R>> bg(ng), sc(ng), dr(ng);
+    for (int is = 0; is < p.ns; ++is) born_row_adj(P, core, r, dR, g0, g1, is, f, D, exact, true, bg, sc, dr, wk);
+    for (int iz = 0; iz < nz; ++iz)
+      for (int ix = 0; ix < p.nx; ++ix) {
+        m0[nm * f + (size_t)iz * p.nx + ix] = g0[(size_t)iz * nx + ix + p.pad];
+        m1[nm * f + (size_t)iz * p.nx + ix] = g1[(size_t)iz * nx + ix + p.pad];
+      }
+  });
+  store(ds2, m0.data(), nm * nf, add);
+  store(drho, m1.data(), nm * nf, add);
+}
+
+// ---------------------------------------------------- row-level operators
+template <class R>
+struct RowOp {
+  std::vector<C<R>> s;
+  Core<R> core;
+  RowOp(const wem_params& p, const float* slow, int nxg)
+      : s(load<R>(slow, (size_t)nxg * p.nz)), core(p, s.data(), nxg, p.nz) {}
+};
+
+int run_guarded(const std::function<void()>& fn) {
+  try {
+    fn();
+    return WEM_OK;
+  } catch (const Error& e) {
+    g_err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return WEM_EINVAL;
+  }
+}
+
+}  // namespace
+}  // namespace wo
+
+using namespace wo;
+
+extern "C" {
+
+const char* oracle_last_error(void) { return g_err.c_str(); }
+
+int oracle_count_freqs(const wem_params* p, int* nfreq, int* bins, float* freqs) {
+  return run_guarded([&] {
+    Freqs F = make_freqs(*p);
+    *nfreq = (int)F.freq.size();
+    if (bins) std::copy(F.bin.begin(), F.bin.end(), bins);
+    if (freqs) std::copy(F.freq.begin(), F.freq.end(), freqs);
+  });
+}
+
+int oracle_devices(const wem_params* p, int* sx, int* sz, int* rx, int* rz) {
+  return run_guarded([&] {
+    Devices s = make_devices(*p, true), r = make_devices(*p, false);
+    std::copy(s.ix.begin(), s.ix.end(), sx);
+    std::copy(s.iz.begin(), s.iz.end(), sz);
+    std::copy(r.ix.begin(), r.ix.end(), rx);
+    std::copy(r.iz.begin(), r.iz.end(), rz);
+  });
+}
+
+// double-precision transform for checking the FFT against numpy
+int oracle_fft(int n, double* x, int sign) {
+  return run_guarded([&] {
+    Fft<double> f(n);
+    std::vector<C<double>> v(n), scr(n);
+    for (int i = 0; i < n; ++i) v[i] = C<double>(x[2 * i], x[2 * i + 1]);
+    f.run(v.data(), sign, scr.data());
+    for (int i = 0; i < n; ++i) { x[2 * i] = v[i].real(); x[2 * i + 1] = v[i].imag(); }
+  });
+}
+
+int oracle_wem_forward(const wem_params* p, const float* wavelet, const float* s2, const float* rho,
+                       void* data, int kind, int add, int prec, int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) wem_forward<double>(*p, wavelet, s2, rho, data, kind, add, nthreads);
+    else wem_forward<float>(*p, wavelet, s2, rho, data, kind, add, nthreads);
+  });
+}
+
+int oracle_born_forward(const wem_params* p, const float* wavelet, const float* bs2, const float* brho,
+                        const float* ds2, const float* drho, void* data, int kind, int add, int prec,
+                        int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) born_forward<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+    else born_forward<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+  });
+}
+
+int oracle_born_adjoint(const wem_params* p, const float* wavelet, const float* bs2, const float* brho,
+                        float* ds2, float* drho, const void* data, int kind, int add, int prec, int nthreads,
+                        int fchunks) {
+  return run_guarded([&] {
+    if (prec == 64) born_adjoint<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads, fchunks);
+    else born_adjoint<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads, fchunks);
+  });
+}
+
+int oracle_extwem_forward(const wem_params* p, const float* wavelet, const float* s2, const float* rho,
+                          void* data, int kind, int add, int prec, int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) extwem_forward<double>(*p, wavelet, s2, rho, data, kind, add, nthreads);
+    else extwem_forward<float>(*p, wavelet, s2, rho, data, kind, add, nthreads);
+  });
+}
+
+int oracle_extborn_forward(const wem_params* p, const float* wavelet, const float* bs2, const float* brho,
+                           const float* ds2, const float* drho, void* data, int kind, int add, int prec,
+                           int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) extborn_forward<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+    else extborn_forward<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+  });
+}
+
+int oracle_extborn_adjoint(const wem_params* p, const float* wavelet, const float* bs2, const float* brho,
+                           float* ds2, float* drho, const void* data, int kind, int add, int prec,
+                           int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) extborn_adjoint<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+    else extborn_adjoint<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+  });
+}
+
+// ---- row-level operators over a padded slowness [nz][nxg]
+extern "C++" {
+template <class R>
+static void onestep_rows(const wem_params& p, const float* slow, int nxg, int iz, float freq, int adj,
+                         const float* in, float* out, int nrow, int add) {
+  RowOp<R> op(p, slow, nxg);
+  Work<R> wk(op.core.N, nxg);
+  R w = Core<R>::omega(freq);
+  for (int r = 0; r < nrow; ++r) {
+    std::vector<C<R>> a = load<R>(in + 2 * (size_t)r * nxg, nxg), b(nxg, C<R>(0));
+    if (add) b = load<R>(out + 2 * (size_t)r * nxg, nxg);
+    if (!adj) onestep_fwd(op.core, iz, w, a.data(), b.data(), add != 0, wk);
+    else onestep_adj(op.core, iz, w, b.data(), a.data(), add != 0, wk);
+    store(out + 2 * (size_t)r * nxg, b.data(), nxg, false);
+  }
+}
+}  // extern "C++"
+
+int oracle_onestep(const wem_params* p, const float* slow, int nxg, int iz, float freq, int adj,
+                   const float* in, float* out, int nrow, int add, int prec) {
+  return run_guarded([&] {
+    check(iz >= 0 && iz < p->nz, "depth index out of range");
+    if (prec == 64) onestep_rows<double>(*p, slow, nxg, iz, freq, adj, in, out, nrow, add);
+    else onestep_rows<float>(*p, slow, nxg, iz, freq, adj, in, out, nrow, add);
+  });
+}
+
+extern "C++" {
+template <class R>
+static void oneway_rows(const wem_params& p, const float* slow, int nxg, int up, float freq, int adj,
+                        const float* in, float* out, int nrow, int add) {
+  RowOp<R> op(p, slow, nxg);
+  Work<R> wk(op.core.N, nxg);
+  R w = Core<R>::omega(freq);
+  size_t n = (size_t)nxg * p.nz;
+  const bool inplace = (in == out);
+  for (int r = 0; r < nrow; ++r) {
+    std::vector<C<R>> a = load<R>(in + 2 * n * r, n);
+    std::vector<C<R>> b = inplace ? a : load<R>(out + 2 * n * r, n);
+    C<R>* A = a.data();
+    C<R>* B = inplace ? a.data() : b.data();
+    if (!adj) {
+      if (up) up_fwd(op.core, w, A, B, add != 0, wk); else down_fwd(op.core, w, A, B, add != 0, wk);
+    } else {
+      if (up) up_adj(op.core, w, B, A, add != 0, wk); else down_adj(op.core, w, B, A, add != 0, wk);
+    }
+    store(out + 2 * n * r, B, n, false);
+  }
+}
+}  // extern "C++"
+
+int oracle_oneway(const wem_params* p, const float* slow, int nxg, int up, float freq, int adj,
+                  const float* in, float* out, int nrow, int add, int prec) {
+  return run_guarded([&] {
+    if (prec == 64) oneway_rows<double>(*p, slow, nxg, up, freq, adj, in, out, nrow, add);
+    else oneway_rows<float>(*p, slow, nxg, up, freq, adj, in, out, nrow, add);
+  });
+}
+
+extern "C++" {
+template <class R>
+static void scatter_rows(const wem_params& p, const float* slow, int nxg, int iz, float freq, int adj,
+                         const float* in, float* out, int nrow, int add) {
+  RowOp<R> op(p, slow, nxg);
+  Work<R> wk(op.core.N, nxg);
+  R w = Core<R>::omega(freq);
+  bool exact = p.adjoint_mode == WEM_ADJ_EXACT;
+  for (int r = 0; r < nrow; ++r) {
+    std::vector<C<R>> a = load<R>(in + 2 * (size_t)r * nxg, nxg), b(nxg, C<R>(0));
+    if (add) b = load<R>(out + 2 * (size_t)r * nxg, nxg);
+    if (!adj) scatter_fwd(op.core, iz, w, a.data(), b.data(), add != 0, wk);
+    else scatter_adj(op.core, iz, w, b.data(), a.data(), add != 0, exact, wk);
+    store(out + 2 * (size_t)r * nxg, b.data(), nxg, false);
+  }
+}
+}  // extern "C++"
+
+int oracle_scatter(const wem_params* p, const float* slow, int nxg, int iz, float freq, int adj,
+                   const float* in, float* out, int nrow, int add, int prec) {
+  return run_guarded([&] {
+    check(iz >= 0 && iz < p->nz, "depth index out of range");
+    if (prec == 64) scatter_rows<double>(*p, slow, nxg, iz, freq, adj, in, out, nrow, add);
+    else scatter_rows<float>(*p, slow, nxg, iz, freq, adj, in, out, nrow, add);
+  });
+}
+
+int oracle_refsampler(const wem_params* p, const float* slow, int nxg, float* sref, int* refidx) {
+  return run_guarded([&] {
+    std::vector<C<float>> s = load<float>(slow, (size_t)nxg * p->nz);
+    RefSampler<float> rs(s.data(), nxg, p->nz, p->nref, p->refs_mode);
+    for (size_t i = 0; i < rs.sref.size(); ++i) { sref[2 * i] = rs.sref[i].real(); sref[2 * i + 1] = rs.sref[i].imag(); }
+    std::fill(refidx, refidx + (size_t)nxg * p->nz, -1);
+    for (int iz = 0; iz < p->nz; ++iz)
+      for (int j = 0; j < p->nref; ++j)
+        for (int x : rs.loc[(size_t)iz * p->nref + j]) refidx[(size_t)iz * nxg + x] = j;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,722 @@
+// C ABI of the GB300 one-way wave-equation library (include/wemgpu.h).
+//
+// An Engine owns the device tables of one parameter set and one background
+// (or one background per frequency for the extended operators), the group
+// schedule and the workspaces.  Every public call validates its arguments
+// on the host, turns every failure into a status code and never throws
+// across the boundary.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "kernels.h"
+#include "planner.h"
+#include "wemgpu.h"
+
+namespace wg {
+namespace {
+
+thread_local std::string g_error;
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return;
+  int code = (e == cudaErrorMemoryAllocation) ? WEM_ENOMEM : WEM_EDEVICE;
+  throw Fail(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// growable device buffer
+struct Buf {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~Buf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  void* get(size_t bytes) {
+    if (bytes > cap) {
+      release();
+      cuda_check(cudaMalloc(&p, bytes ? bytes : 16), "cudaMalloc");
+      cap = bytes;
+    }
+    return p;
+  }
+  template <class T> T* as(size_t n) { return reinterpret_cast<T*>(get(n * sizeof(T))); }
+};
+
+template <class T>
+T* upload(Buf& b, const std::vector<T>& v) {
+  T* d = b.as<T>(v.size());
+  if (!v.empty()) cuda_check(cudaMemcpy(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "upload");
+  return d;
+}
+
+std::vector<float2> to_f2(const std::vector<cd>& v) {
+  std::vector<float2> o(v.size());
+  for (size_t i = 0; i < v.size(); ++i) o[i] = make_float2((float)v[i].real(), (float)v[i].imag());
+  return o;
+}
+
+FftPlan make_plan(int n) {
+  FftPlan P{};
+  P.n = n;
+  std::vector<int> r = fft_radices(n);
+  require((int)r.size() <= kMaxStages, "FFT length has too many factors");
+  P.nstage = (int)r.size();
+  for (size_t i = 0; i < r.size(); ++i) P.radix[i] = r[i];
+  return P;
+}
+
+// host view of a caller buffer: device pointers are used in place, host
+// buffers are staged through a device buffer
+struct Staged {
+  Buf own;
+  void* dev = nullptr;
+  bool host = false;
+  size_t bytes = 0;
+  void in(const void* p, size_t nbytes) {
+    bytes = nbytes;
+    host = !is_device_ptr(p);
+    if (!host) {
+      dev = const_cast<void*>(p);
+      return;
+    }
+    dev = own.get(nbytes);
+    cuda_check(cudaMemcpy(dev, p, nbytes, cudaMemcpyHostToDevice), "H2D");
+  }
+  // output buffer: when add is set the current contents are needed
+  void out(void* p, size_t nbytes, bool need_contents) {
+    bytes = nbytes;
+    host = !is_device_ptr(p);
+    if (!host) {
+      dev = p;
+      return;
+    }
+    dev = own.get(nbytes);
+    if (need_contents) cuda_check(cudaMemcpy(dev, p, nbytes, cudaMemcpyHostToDevice), "H2D");
+  }
+  void finish(void* p) {
+    if (host) cuda_check(cudaMemcpy(p, dev, bytes, cudaMemcpyDeviceToHost), "D2H");
+  }
+};
+
+std::vector<float> host_floats(const void* p, size_t nfloat) {
+  std::vector<float> h(nfloat);
+  if (is_device_ptr(p)) cuda_check(cudaMemcpy(h.data(), p, nfloat * 4, cudaMemcpyDeviceToHost), "D2H");
+  else std::memcpy(h.data(), p, nfloat * 4);
+  return h;
+}
+
+class Engine {
+ public:
+  Engine(const wem_params& p, const float* wavelet, bool ext, bool born) : p_(p), ext_(ext), born_(born) {
+    require(wavelet != nullptr, "wavelet is NULL");
+    geo_ = make_geometry(p, wavelet);
+    F_ = geo_.nfreq();
+    M_ = ext ? F_ : 1;
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    build_static();
+  }
+
+  int nfreq() const { return F_; }
+
+  void set_background(const void* s2, const void* rho) {
+    require(s2 && rho, "background model is NULL");
+    const size_t n = (size_t)M_ * p_.nz * p_.nx;
+    std::vector<float> hs = host_floats(s2, 2 * n), hr = host_floats(rho, 2 * n);
+    build_background(hs.data(), hr.data());
+    have_bg_ = true;
+  }
+
+  void wem_forward(const void* s2, const void* rho, void* data, int kind, int add) {
+    set_background(s2, rho);
+    float2* bins = zero_bins();
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
+    int G = pick_G([&](int g) { return smem_wem(ctx_, g); });
+    for_chunks(G, plane * 8, [&](const Group* gd, int ng, int rows) {
+      float2* A = store1_.as<float2>((size_t)rows * plane);
+      launch_wem(ctx_, gd, ng, G, A, bins, 0);
+      cuda_check(cudaGetLastError(), "k_wem launch");
+    });
+    emit(data, kind, add);
+  }
+
+  void born_forward(const void* ds2, const void* drho, void* data, int kind, int add) {
+    require(have_bg_, "background not set");
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
+    float2* dm0 = dm0_.as<float2>((size_t)M_ * plane);
+    float2* dm1 = dm1_.as<float2>((size_t)M_ * plane);
+    pad_perturbation(ds2, dm0);
+    pad_perturbation(drho, dm1);
+    float2* drm = drm_.as<float2>((size_t)M_ * plane);
+    launch_drefl_fwd(ctx_, M_, a0_, b0_, a1_, b1_, dm0, dm1, drm, 0);
+    float2* bins = zero_bins();
+    int G = pick_G([&](int g) { return smem_born_fwd(ctx_, g); });
+    for_chunks(G, 2 * plane * 8, [&](const Group* gd, int ng, int rows) {
+      float2* A = store1_.as<float2>((size_t)rows * plane);
+      float2* B = store2_.as<float2>((size_t)rows * plane);
+      launch_born_fwd(ctx_, gd, ng, G, dm0, drm, A, B, bins, 0);
+      cuda_check(cudaGetLastError(), "k_born_fwd launch");
+    });
+    emit(data, kind, add);
+  }
+
+  void born_adjoint(void* ds2, void* drho, const void* data, int kind, int add) {
+    require(have_bg_, "background not set");
+    require(ds2 && drho && data, "NULL argument");
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
+    absorb(data, kind);
+    float2* IR = ir_.as<float2>((size_t)M_ * plane);
+    float2* IS = is_.as<float2>((size_t)M_ * plane);
+    cuda_check(cudaMemsetAsync(IR, 0, (size_t)M_ * plane * 8, 0), "memset");
+    cuda_check(cudaMemsetAsync(IS, 0, (size_t)M_ * plane * 8, 0), "memset");
+    int G = pick_G([&](int g) { return smem_born_adj(ctx_, g); });
+    const int compat = p_.adjoint_mode == WEM_ADJ_COMPAT ? 1 : 0;
+    // per row: two stored fields; per group: two partial images
+    for_chunks(G, 2 * plane * 8 + (2 * plane * 8 + G - 1) / G, [&](const Group* gd, int ng, int rows) {
+      float2* BG = store1_.as<float2>((size_t)rows * plane);
+      float2* T = store2_.as<float2>((size_t)rows * plane);
+      float2* pr = part1_.as<float2>((size_t)ng * plane);
+      float2* ps = part2_.as<float2>((size_t)ng * plane);
+      launch_born_adj(ctx_, gd, ng, G, BG, T, bins_, pr, ps, compat, 0);
+      cuda_check(cudaGetLastError(), "k_born_adj launch");
+      // chunk-local group ranges of each model slice
+      std::vector<int> beg(M_ + 1, 0);
+      std::vector<Group> hg(ng);
+      cuda_check(cudaMemcpy(hg.data(), gd, ng * sizeof(Group), cudaMemcpyDeviceToHost), "D2H groups");
+      if (M_ == 1) {
+        beg[1] = ng;
+      } else {
+        int g = 0;
+        for (int m = 0; m <= M_; ++m) {
+          while (g < ng && hg[g].f < m) ++g;
+          beg[m] = g;
+        }
+      }
+      int* dbeg = upload(begbuf_, beg);
+      launch_reduce_images(pr, dbeg, M_, plane, IR, 0);
+      launch_reduce_images(ps, dbeg, M_, plane, IS, 0);
+      cuda_check(cudaGetLastError(), "reduce launch");
+    });
+    const size_t nm = (size_t)M_ * p_.nz * p_.nx;
+    Staged o0, o1;
+    o0.out(ds2, nm * 8, add != 0);
+    o1.out(drho, nm * 8, add != 0);
+    launch_grad_assemble(ctx_, M_, a0_, b0_, a1_, b1_, IR, IS, (float2*)o0.dev, (float2*)o1.dev, p_.nx, add, 0);
+    cuda_check(cudaGetLastError(), "grad launch");
+    cuda_check(cudaStreamSynchronize(0), "born_adjoint");
+    o0.finish(ds2);
+    o1.finish(drho);
+  }
+
+ private:
+  wem_params p_;
+  bool ext_, born_;
+  bool have_bg_ = false;
+  Geometry geo_;
+  int F_ = 0, M_ = 1;
+  DevCtx ctx_{};
+  FftPlan tplan_{};
+  // static tables
+  Buf tw_, kx_, taper_, omega_, bin_, wave_, sx_, sz_, gs_, gr_, rptr_, rid_, rxs_, ttw_;
+  // background tables
+  Buf sref_, ref_, q_, sc_, rc_, a0b_, b0b_, a1b_, b1b_, ph_, fac_;
+  float2 *a0_ = nullptr, *b0_ = nullptr, *a1_ = nullptr, *b1_ = nullptr;
+  // workspaces
+  Buf binsbuf_, groups_, store1_, store2_, part1_, part2_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
+  float2* bins_ = nullptr;
+
+  void build_static() {
+    const Geometry& g = geo_;
+    std::vector<cd> tw = twiddles(g.N);
+    std::vector<double> k = k_grid(g.N, p_.dx), tp = taper(g.nxg, p_.pad);
+    std::vector<float> kf(k.begin(), k.end()), tpf(g.nxg), om(F_);
+    for (int i = 0; i < g.nxg; ++i) tpf[i] = (float)(tp[i] / g.N);
+    for (int f = 0; f < F_; ++f) om[f] = (float)(2 * 3.14159265358979323846 * (double)g.freq[f]);
+    std::vector<float> gsf(g.gs.begin(), g.gs.end()), grf(g.gr.begin(), g.gr.end());
+    // receivers sorted by (depth, x, id)
+    std::vector<int> ord(g.nr);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) {
+      return g.rz[a] != g.rz[b] ? g.rz[a] < g.rz[b] : g.rx[a] < g.rx[b];
+    });
+    std::vector<int> rptr(p_.nz + 1, 0), rxs(g.nr);
+    for (int i = 0; i < g.nr; ++i) rptr[g.rz[ord[i]] + 1]++;
+    for (int z = 0; z < p_.nz; ++z) rptr[z + 1] += rptr[z];
+    for (int i = 0; i < g.nr; ++i) rxs[i] = g.rx[ord[i]];
+    ctx_.plan = make_plan(g.N);
+    ctx_.N = g.N;
+    ctx_.nxg = g.nxg;
+    ctx_.tap = p_.tap;
+    ctx_.pad = p_.pad;
+    ctx_.nz = p_.nz;
+    ctx_.nref = p_.nref;
+    ctx_.prop = p_.prop;
+    ctx_.ntaylor = p_.ntaylor;
+    ctx_.nfreq = F_;
+    ctx_.ext = ext_ ? 1 : 0;
+    ctx_.ns = g.ns;
+    ctx_.nr = g.nr;
+    ctx_.ngs = p_.ngs;
+    ctx_.ngr = p_.ngr;
+    ctx_.nbin = g.nt_pad;
+    ctx_.dz = p_.dz;
+    ctx_.invN = 1.0f / g.N;
+    ctx_.tw = upload(tw_, to_f2(tw));
+    ctx_.kx = upload(kx_, kf);
+    ctx_.taperN = upload(taper_, tpf);
+    ctx_.omega = upload(omega_, om);
+    ctx_.bin = upload(bin_, g.bin);
+    ctx_.wave = upload(wave_, to_f2(g.wave_at));
+    ctx_.sx = upload(sx_, g.sx);
+    ctx_.sz = upload(sz_, g.sz);
+    ctx_.gs = upload(gs_, gsf);
+    ctx_.gr = upload(gr_, grf);
+    ctx_.rptr = upload(rptr_, rptr);
+    ctx_.rid = upload(rid_, ord);
+    ctx_.rxs = upload(rxs_, rxs);
+    tplan_ = make_plan(g.nt_pad);
+    upload(ttw_, to_f2(twiddles(g.nt_pad)));
+    bins_ = binsbuf_.as<float2>((size_t)g.ns * g.nr * g.nt_pad);
+  }
+
+  void build_background(const float* s2, const float* rho) {
+    const int nz = p_.nz, nx = p_.nx, nxg = geo_.nxg;
+    const size_t plane = (size_t)nz * nxg, mplane = (size_t)nz * nx;
+    const int nt = p_.ntaylor + 1;
+    std::vector<float2> sref((size_t)M_ * nz * p_.nref), q, sc, rc((size_t)M_ * plane), a0, b0, a1, b1;
+    std::vector<signed char> ref((size_t)M_ * plane);
+    if (p_.prop == WEM_PROP_SSF) q.resize((size_t)M_ * plane);
+    if (born_) {
+      sc.resize((size_t)M_ * nt * plane);
+      a0.resize((size_t)M_ * plane); b0.resize(a0.size()); a1.resize(a0.size()); b1.resize(a0.size());
+    }
+    for (int m = 0; m < M_; ++m) {
+      std::vector<cd> sp = pad_model(s2 + 2 * mplane * m, nz, nx, p_.pad, true);
+      std::vector<cd> dp = pad_model(rho + 2 * mplane * m, nz, nx, p_.pad, true);
+      SliceTables t = make_slice_tables(p_, sp, dp, nxg, born_);
+      auto put = [&](std::vector<float2>& dst, const std::vector<cd>& src, size_t off) {
+        for (size_t i = 0; i < src.size(); ++i)
+          dst[off + i] = make_float2((float)src[i].real(), (float)src[i].imag());
+      };
+      put(sref, t.sref, (size_t)m * nz * p_.nref);
+      std::copy(t.ref.begin(), t.ref.end(), ref.begin() + (size_t)m * plane);
+      if (!q.empty()) put(q, t.q, (size_t)m * plane);
+      put(rc, t.rc, (size_t)m * plane);
+      if (born_) {
+        put(sc, t.sc, (size_t)m * nt * plane);
+        put(a0, t.a0, (size_t)m * plane); put(b0, t.b0, (size_t)m * plane);
+        put(a1, t.a1, (size_t)m * plane); put(b1, t.b1, (size_t)m * plane);
+      }
+    }
+    float2* dsref = upload(sref_, sref);
+    ctx_.ref = upload(ref_, ref);
+    ctx_.rc = upload(rc_, rc);
+    if (born_) {
+      ctx_.sc = upload(sc_, sc);
+      a0_ = upload(a0b_, a0); b0_ = upload(b0b_, b0); a1_ = upload(a1b_, a1); b1_ = upload(b1b_, b1);
+    }
+    float2* ph = ph_.as<float2>((size_t)F_ * nz * p_.nref * geo_.N);
+    launch_phase_tables(ctx_, dsref, p_.eps, ph, 0);
+    ctx_.ph = ph;
+    if (p_.prop == WEM_PROP_SSF) {
+      float2* dq = upload(q_, q);
+      float2* fac = fac_.as<float2>((size_t)F_ * plane);
+      launch_fac_tables(ctx_, dq, fac, 0);
+      ctx_.fac = fac;
+    } else {
+      ctx_.fac = nullptr;
+    }
+    cuda_check(cudaGetLastError(), "table kernels");
+  }
+
+  template <class F>
+  int pick_G(F smem_of) {
+    int lim = max_smem_per_block();
+    int G = std::min(geo_.ns, 8);
+    while (G > 1 && (int)smem_of(G) > lim) --G;
+    require((int)smem_of(G) <= lim, "row too long for one CTA's shared memory");
+    return G;
+  }
+
+  // groups of up to G shots of one frequency, sorted by frequency, run in
+  // chunks whose storage fits the memory budget
+  template <class F>
+  void for_chunks(int G, size_t bytes_per_row, F run) {
+    std::vector<Group> all;
+    for (int f = 0; f < F_; ++f)
+      for (int s0 = 0; s0 < geo_.ns; s0 += G) all.push_back(Group{f, s0, std::min(G, geo_.ns - s0), 0});
+    size_t freeb = 0, totalb = 0;
+    cuda_check(cudaMemGetInfo(&freeb, &totalb), "cudaMemGetInfo");
+    size_t budget = std::min<size_t>((size_t)(0.6 * (double)freeb), (size_t)96 << 30);
+    size_t max_rows = std::max<size_t>(G, budget / std::max<size_t>(bytes_per_row, 1));
+    size_t i = 0;
+    while (i < all.size()) {
+      std::vector<Group> chunk;
+      int rows = 0;
+      while (i < all.size() && (size_t)(rows + all[i].n) <= max_rows) {
+        Group g = all[i++];
+        g.row0 = rows;
+        rows += g.n;
+        chunk.push_back(g);
+      }
+      if (chunk.empty()) {
+        Group g = all[i++];
+        g.row0 = 0;
+        rows = g.n;
+        chunk.push_back(g);
+      }
+      Group* gd = upload(groups_, chunk);
+      run(gd, (int)chunk.size(), rows);
+    }
+  }
+
+  float2* zero_bins() {
+    cuda_check(cudaMemsetAsync(bins_, 0, (size_t)geo_.ns * geo_.nr * geo_.nt_pad * 8, 0), "memset");
+    return bins_;
+  }
+
+  void pad_perturbation(const void* m, float2* out) {
+    require(m != nullptr, "perturbation is NULL");
+    Staged s;
+    s.in(m, (size_t)M_ * p_.nz * p_.nx * 8);
+    launch_pad_model((const float2*)s.dev, out, M_, p_.nz, p_.nx, p_.pad, 0);
+    cuda_check(cudaGetLastError(), "pad launch");
+    cuda_check(cudaStreamSynchronize(0), "pad");
+  }
+
+  // internal bins [ns][nr][nt_pad] -> caller data
+  void emit(void* data, int kind, int add) {
+    require(data != nullptr, "data is NULL");
+    const int ntr = geo_.ns * geo_.nr;
+    Staged o;
+    if (kind == WEM_DATA_TIME) {
+      o.out(data, (size_t)ntr * p_.nt * 4, add != 0);
+      launch_bins_to_time(tplan_, (const float2*)ttw_.p, bins_, (float*)o.dev, ntr, p_.nt, add, 0);
+    } else {
+      require(kind == WEM_DATA_FREQ, "unknown data kind");
+      o.out(data, (size_t)ntr * geo_.nbin * 8, add != 0);
+      launch_copy_rows(bins_, geo_.nt_pad, (float2*)o.dev, geo_.nbin, ntr, std::min(geo_.nbin, geo_.nt_pad), add,
+                       0);
+    }
+    cuda_check(cudaGetLastError(), "emit launch");
+    cuda_check(cudaStreamSynchronize(0), "operator");
+    o.finish(data);
+  }
+
+  // caller data -> internal bins
+  void absorb(const void* data, int kind) {
+    const int ntr = geo_.ns * geo_.nr;
+    Staged s;
+    if (kind == WEM_DATA_TIME) {
+      s.in(data, (size_t)ntr * p_.nt * 4);
+      launch_time_to_bins(tplan_, (const float2*)ttw_.p, (const float*)s.dev, bins_, ntr, p_.nt, 0);
+    } else {
+      require(kind == WEM_DATA_FREQ, "unknown data kind");
+      s.in(data, (size_t)ntr * geo_.nbin * 8);
+      launch_copy_rows((const float2*)s.dev, geo_.nbin, bins_, geo_.nt_pad, ntr, std::min(geo_.nbin, geo_.nt_pad),
+                       0, 0);
+    }
+    cuda_check(cudaGetLastError(), "absorb launch");
+    cuda_check(cudaStreamSynchronize(0), "absorb");
+  }
+};
+
+// ------------------------------------------------------------ wemop
+class RowOps {
+ public:
+  RowOps(const wem_params& p, const void* slow, int nxg) : p_(p), nxg_(nxg) {
+    require(slow != nullptr, "slowness is NULL");
+    require(nxg >= 2 && p.nz > 1, "bad grid");
+    require(p.pad >= 0 && p.tap >= 0 && p.pad != 1 && 2 * p.pad <= nxg, "bad pad/tap");
+    require(p.ntaylor >= 0 && p.ntaylor <= 4, "ntaylor must be in [0,4]");
+    std::vector<float> hs = host_floats(slow, 2 * (size_t)p.nz * nxg);
+    std::vector<cd> sp((size_t)p.nz * nxg), dp(sp.size(), cd(1.0, 0.0));
+    for (size_t i = 0; i < sp.size(); ++i) sp[i] = cd(hs[2 * i], hs[2 * i + 1]);
+    t_ = make_slice_tables(p, sp, dp, nxg, true);
+    N_ = nxg + 2 * p.tap;
+    std::vector<double> k = k_grid(N_, p.dx), tp = taper(nxg, p.pad);
+    std::vector<float> kf(k.begin(), k.end()), tpf(nxg);
+    for (int i = 0; i < nxg; ++i) tpf[i] = (float)(tp[i] / N_);
+    c_.plan = make_plan(N_);
+    c_.N = N_;
+    c_.nxg = nxg;
+    c_.tap = p.tap;
+    c_.pad = p.pad;
+    c_.nz = p.nz;
+    c_.nref = p.nref;
+    c_.prop = p.prop;
+    c_.ntaylor = p.ntaylor;
+    c_.nfreq = 1;
+    c_.ext = 0;
+    c_.dz = p.dz;
+    c_.invN = 1.0f / N_;
+    c_.tw = upload(tw_, to_f2(twiddles(N_)));
+    c_.kx = upload(kx_, kf);
+    c_.taperN = upload(taper_, tpf);
+    c_.ref = upload(ref_, t_.ref);
+    c_.sc = upload(sc_, to_f2(t_.sc));
+    c_.rc = upload(rc_, to_f2(t_.rc));
+    sref_d_ = upload(sref_, to_f2(t_.sref));
+    q_d_ = upload(q_, to_f2(t_.q));
+  }
+
+  void set_freq(float freq) {
+    if (have_freq_ && freq == freq_) return;
+    float om = (float)(2 * 3.14159265358979323846 * (double)freq);
+    c_.omega = upload(omega_, std::vector<float>{om});
+    c_.ph = nullptr;
+    float2* ph = ph_.as<float2>((size_t)p_.nz * p_.nref * N_);
+    launch_phase_tables(c_, sref_d_, p_.eps, ph, 0);
+    c_.ph = ph;
+    if (p_.prop == WEM_PROP_SSF) {
+      float2* fac = fac_.as<float2>((size_t)p_.nz * nxg_);
+      launch_fac_tables(c_, q_d_, fac, 0);
+      c_.fac = fac;
+    } else {
+      c_.fac = nullptr;
+    }
+    cuda_check(cudaGetLastError(), "table kernels");
+    freq_ = freq;
+    have_freq_ = true;
+  }
+
+  int G() const {
+    int lim = max_smem_per_block(), G = 8;
+    while (G > 1 && (int)smem_rows(c_, G) > lim) --G;
+    require((int)smem_rows(c_, G) <= lim, "row too long for one CTA's shared memory");
+    return G;
+  }
+
+  template <class L>
+  void run_rows(const void* in, void* out, size_t per_row, int nrow, int add, L launch) {
+    require(in && out && nrow >= 0, "bad arguments");
+    const bool alias = in == out;
+    Staged si, so;
+    so.out(out, per_row * nrow * 8, add != 0 || alias);
+    if (alias) si.dev = so.dev; else si.in(in, per_row * nrow * 8);
+    launch((const float2*)si.dev, (float2*)so.dev, alias);
+    cuda_check(cudaGetLastError(), "row kernel");
+    cuda_check(cudaStreamSynchronize(0), "row kernel");
+    so.finish(out);
+  }
+
+  wem_params p_;
+  int nxg_, N_ = 0;
+  SliceTables t_;
+  DevCtx c_{};
+  Buf tw_, kx_, taper_, ref_, sc_, rc_, sref_, q_, omega_, ph_, fac_;
+  float2 *sref_d_ = nullptr, *q_d_ = nullptr;
+  float freq_ = 0;
+  bool have_freq_ = false;
+};
+
+template <class Fn>
+int guard(Fn fn) {
+  try {
+    fn();
+    return WEM_OK;
+  } catch (const Fail& e) {
+    g_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_error = "host allocation failed";
+    return WEM_ENOMEM;
+  } catch (const std::exception& e) {
+    g_error = e.what();
+    return WEM_EINVAL;
+  }
+}
+
+}  // namespace
+}  // namespace wg
+
+using namespace wg;
+
+struct wem_handle { std::unique_ptr<Engine> e; };
+struct born_handle { std::unique_ptr<Engine> e; };
+struct extwem_handle { std::unique_ptr<Engine> e; };
+struct extborn_handle { std::unique_ptr<Engine> e; };
+struct wemop_handle { std::unique_ptr<RowOps> r; };
+
+extern "C" {
+
+void wem_params_default(wem_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->prop = WEM_PROP_SSF;
+  p->nref = 1;
+  p->ntaylor = 1;
+  p->eps = 0.04f;
+  p->fmin = 1.0f;
+  p->adjoint_mode = WEM_ADJ_COMPAT;
+  p->refs_mode = WEM_REFS_ASCODED;
+}
+
+const char* wem_last_error(void) { return g_error.c_str(); }
+const char* wem_version(void) { return "wemgpu 0.1 (sm_103a)"; }
+
+int wem_count_freqs(const wem_params* p, const float* wavelet, int* nfreq) {
+  (void)wavelet;
+  return guard([&] {
+    require(p && nfreq, "NULL argument");
+    *nfreq = count_frequencies(*p);
+  });
+}
+
+// ---- WEM
+int wem_create(const wem_params* p, const float* wavelet, wem_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<wem_handle>();
+    h->e = std::make_unique<Engine>(*p, wavelet, false, false);
+    *out = h.release();
+  });
+}
+void wem_destroy(wem_handle* h) { delete h; }
+int wem_get_nfreq(wem_handle* h, int* n) {
+  return guard([&] { require(h && n, "NULL argument"); *n = h->e->nfreq(); });
+}
+int wem_forward(wem_handle* h, const void* s2, const void* rho, void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->wem_forward(s2, rho, data, kind, add); });
+}
+
+// ---- Born
+int born_create(const wem_params* p, const float* wavelet, const void* s2, const void* rho, born_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<born_handle>();
+    h->e = std::make_unique<Engine>(*p, wavelet, false, true);
+    h->e->set_background(s2, rho);
+    *out = h.release();
+  });
+}
+void born_destroy(born_handle* h) { delete h; }
+int born_set_background(born_handle* h, const void* s2, const void* rho) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->set_background(s2, rho); });
+}
+int born_forward(born_handle* h, const void* ds2, const void* drho, void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->born_forward(ds2, drho, data, kind, add); });
+}
+int born_adjoint(born_handle* h, void* ds2, void* drho, const void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->born_adjoint(ds2, drho, data, kind, add); });
+}
+
+// ---- extended
+int extwem_create(const wem_params* p, const float* wavelet, extwem_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<extwem_handle>();
+    h->e = std::make_unique<Engine>(*p, wavelet, true, false);
+    *out = h.release();
+  });
+}
+void extwem_destroy(extwem_handle* h) { delete h; }
+int extwem_forward(extwem_handle* h, const void* s2, const void* rho, void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->wem_forward(s2, rho, data, kind, add); });
+}
+int extborn_create(const wem_params* p, const float* wavelet, const void* s2, const void* rho,
+                   extborn_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<extborn_handle>();
+    h->e = std::make_unique<Engine>(*p, wavelet, true, true);
+    h->e->set_background(s2, rho);
+    *out = h.release();
+  });
+}
+void extborn_destroy(extborn_handle* h) { delete h; }
+int extborn_set_background(extborn_handle* h, const void* s2, const void* rho) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->set_background(s2, rho); });
+}
+int extborn_forward(extborn_handle* h, const void* ds2, const void* drho, void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->born_forward(ds2, drho, data, kind, add); });
+}
+int extborn_adjoint(extborn_handle* h, void* ds2, void* drho, const void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->born_adjoint(ds2, drho, data, kind, add); });
+}
+
+// ---- row-level operators
+int wemop_create(const wem_params* p, const void* slow, int nxg, wemop_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<wemop_handle>();
+    h->r = std::make_unique<RowOps>(*p, slow, nxg);
+    *out = h.release();
+  });
+}
+void wemop_destroy(wemop_handle* h) { delete h; }
+
+int wemop_onestep(wemop_handle* h, int iz, float freq, int adj, const void* in, void* out, int nrow, int add) {
+  return guard([&] {
+    require(h != nullptr, "NULL handle");
+    RowOps& R = *h->r;
+    require(iz >= 0 && iz < R.p_.nz, "depth index out of range");
+    R.set_freq(freq);
+    int G = R.G();
+    R.run_rows(in, out, R.nxg_, nrow, add, [&](const float2* a, float2* b, bool alias) {
+      require(!alias, "onestep needs distinct input and output");
+      launch_onestep(R.c_, 0, iz, adj, a, b, nrow, add, G, 0);
+    });
+  });
+}
+
+int wemop_oneway(wemop_handle* h, int up, float freq, int adj, const void* in, void* out, int nrow, int add) {
+  return guard([&] {
+    require(h != nullptr, "NULL handle");
+    RowOps& R = *h->r;
+    R.set_freq(freq);
+    int G = R.G();
+    R.run_rows(in, out, (size_t)R.nxg_ * R.p_.nz, nrow, add, [&](const float2* a, float2* b, bool alias) {
+      launch_oneway(R.c_, 0, up, adj, alias ? 1 : 0, a, b, nrow, add, G, 0);
+    });
+  });
+}
+
+int wemop_scatter(wemop_handle* h, int iz, float freq, int adj, const void* in, void* out, int nrow, int add) {
+  return guard([&] {
+    require(h != nullptr, "NULL handle");
+    RowOps& R = *h->r;
+    require(iz >= 0 && iz < R.p_.nz, "depth index out of range");
+    R.set_freq(freq);
+    int G = R.G();
+    int exact = R.p_.adjoint_mode == WEM_ADJ_EXACT ? 1 : 0;
+    R.run_rows(in, out, R.nxg_, nrow, add, [&](const float2* a, float2* b, bool alias) {
+      require(!alias, "scatter needs distinct input and output");
+      launch_scatter(R.c_, 0, iz, adj, exact, a, b, nrow, add, G, 0);
+    });
+  });
+}
+
+int wemop_refsampler(wemop_handle* h, void* sref, int* refidx) {
+  return guard([&] {
+    require(h && sref && refidx, "NULL argument");
+    RowOps& R = *h->r;
+    float* s = (float*)sref;
+    for (size_t i = 0; i < R.t_.sref.size(); ++i) {
+      s[2 * i] = (float)R.t_.sref[i].real();
+      s[2 * i + 1] = (float)R.t_.sref[i].imag();
+    }
+    for (size_t i = 0; i < R.t_.ref.size(); ++i) refidx[i] = R.t_.ref[i];
+  });
+}
+
+}  // extern "C"

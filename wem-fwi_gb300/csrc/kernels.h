@@ -1,0 +1,97 @@
+// Device-side context and host launchers of the GB300 kernels.
+//
+// Work unit: a row = one (shot, frequency) wavefield of nxg complex values.
+// Rows are batched in groups of up to G shots of one frequency; one CTA
+// runs a group through every depth step of a pass with the rows resident in
+// shared memory, so a depth step costs no grid-wide synchronisation and the
+// per-(frequency, depth) tables are read once per group.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "fft_plan.h"
+
+namespace wg {
+
+constexpr int kThreads = 512;  // threads per CTA of every pass kernel
+
+struct DevCtx {
+  FftPlan plan;                 // length N = nxg + 2 tap
+  int N, nxg, tap, pad, nz, nref, prop, ntaylor, nfreq, ext, ns, nr, ngs, ngr, nbin;
+  float dz, invN;
+  const float2* tw;             // [N] exp(-2 pi i t/N)
+  const float2* ph;             // [F][nz][nref][N] phase-shift factors (phase_shift.ispc)
+  const float2* fac;            // SSF: [F][nz][nxg] taper * split-step / N; PSPI: null
+  const float* taperN;          // [nxg] taper / N
+  const signed char* ref;       // [M][nz][nxg] reference of each point, -1 none
+  const float2* sc;             // [M][ntaylor+1][nz][nxg] Scatter coefficients
+  const float2* rc;             // [M][nz][nxg] Reflect coefficients
+  const float* kx;              // [N] k grid
+  const float* omega;           // [F] 2 pi f
+  const int* bin;               // [F] data bin of each frequency
+  const float2* wave;           // [F] wavelet spectrum at bin[f]
+  const int* sx;                // [ns] source x (unpadded grid index)
+  const int* sz;                // [ns] source depth index
+  const float* gs;              // [2 ngs + 1] source window
+  const float* gr;              // [2 ngr + 1] receiver window
+  const int* rptr;              // [nz + 1] receivers by depth (CSR over rid)
+  const int* rid;               // receiver ids sorted by (depth, x)
+  const int* rxs;               // x of rid[k] (sorted within a depth)
+};
+
+// group g: frequency f, first shot s0, row count n, first storage row
+struct Group {
+  int f, s0, n, row0;
+};
+
+// shared-memory bytes of each pass for G rows per group
+size_t smem_wem(const DevCtx& c, int G);
+size_t smem_born_fwd(const DevCtx& c, int G);
+size_t smem_born_adj(const DevCtx& c, int G);
+size_t smem_rows(const DevCtx& c, int G);
+int max_smem_per_block();
+
+// ---- table builders
+void launch_phase_tables(const DevCtx& c, const float2* sref /*[M][nz][nref]*/, float eps, float2* ph,
+                         cudaStream_t st);
+void launch_fac_tables(const DevCtx& c, const float2* q /*[M][nz][nxg]*/, float2* fac, cudaStream_t st);
+
+// ---- passes (one CTA per group)
+void launch_wem(const DevCtx& c, const Group* groups, int ngroups, int G, float2* store, float2* bins,
+                cudaStream_t st);
+void launch_born_fwd(const DevCtx& c, const Group* groups, int ngroups, int G, const float2* dm,
+                     const float2* drm, float2* storeA, float2* storeB, float2* bins, cudaStream_t st);
+// compat: 0 exact, 1 compat (Scatter order + last-row rule).  last_f/last_s:
+// the frequency / shot whose LinUp term keeps the last depth row in compat mode
+void launch_born_adj(const DevCtx& c, const Group* groups, int ngroups, int G, float2* storeBG, float2* storeT,
+                     const float2* bins, float2* imgR, float2* imgS, int compat, cudaStream_t st);
+
+// row-level operators over rows of one frequency index f
+void launch_onestep(const DevCtx& c, int f, int z, int adj, const float2* in, float2* out, int nrow, int add,
+                    int G, cudaStream_t st);
+void launch_scatter(const DevCtx& c, int f, int z, int adj, int exact, const float2* in, float2* out, int nrow,
+                    int add, int G, cudaStream_t st);
+// whole-field Down/Up; recursive = model aliases data (in-place drivers)
+void launch_oneway(const DevCtx& c, int f, int up, int adj, int recursive, const float2* in, float2* out,
+                   int nrow, int add, int G, cudaStream_t st);
+
+// ---- helpers
+void launch_pad_model(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st);
+void launch_drefl_fwd(const DevCtx& c, int M, const float2* a0, const float2* b0, const float2* a1,
+                      const float2* b1, const float2* dm0, const float2* dm1, float2* out, cudaStream_t st);
+void launch_reduce_images(const float2* parts, const int* slice_beg, int M, size_t plane, float2* out,
+                          cudaStream_t st);
+void launch_grad_assemble(const DevCtx& c, int M, const float2* a0, const float2* b0, const float2* a1,
+                          const float2* b1, const float2* IR, const float2* IS, float2* g0, float2* g1, int nx,
+                          int add, cudaStream_t st);
+// traces: time [ntr][nt] <-> bins [ntr][n]
+void launch_time_to_bins(const FftPlan& P, const float2* tw, const float* t, float2* b, int ntr, int nt,
+                         cudaStream_t st);
+void launch_bins_to_time(const FftPlan& P, const float2* tw, const float2* b, float* t, int ntr, int nt, int add,
+                         cudaStream_t st);
+// complex copy with row reshape: dst[r][j] (+)= src[r][j] for j < ncopy, zero beyond (unless add)
+void launch_copy_rows(const float2* src, int lds, float2* dst, int ldd, int nrows, int ncopy, int add,
+                      cudaStream_t st);
+void launch_scale_add(float2* y, const float2* x, size_t n, cudaStream_t st);
+
+}  // namespace wg

@@ -1,0 +1,86 @@
+"""ctypes binding of ``libwemgpu.so`` (the C ABI in include/wemgpu.h).
+
+The library is the only compute path: importing a compute entry point
+without it raises, there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .params import WemParams
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libwemgpu.so")
+
+_lib = None
+
+_h = ctypes.c_void_p
+_v = ctypes.c_void_p
+_i = ctypes.c_int
+_f = ctypes.c_float
+_pp = ctypes.POINTER(WemParams)
+
+_SIGS = {
+    "wem_params_default": (None, [_pp]),
+    "wem_count_freqs": (_i, [_pp, _v, ctypes.POINTER(_i)]),
+    "wem_last_error": (ctypes.c_char_p, []),
+    "wem_version": (ctypes.c_char_p, []),
+    "wem_create": (_i, [_pp, _v, ctypes.POINTER(_h)]),
+    "wem_destroy": (None, [_h]),
+    "wem_get_nfreq": (_i, [_h, ctypes.POINTER(_i)]),
+    "wem_forward": (_i, [_h, _v, _v, _v, _i, _i]),
+    "born_create": (_i, [_pp, _v, _v, _v, ctypes.POINTER(_h)]),
+    "born_destroy": (None, [_h]),
+    "born_set_background": (_i, [_h, _v, _v]),
+    "born_forward": (_i, [_h, _v, _v, _v, _i, _i]),
+    "born_adjoint": (_i, [_h, _v, _v, _v, _i, _i]),
+    "extwem_create": (_i, [_pp, _v, ctypes.POINTER(_h)]),
+    "extwem_destroy": (None, [_h]),
+    "extwem_forward": (_i, [_h, _v, _v, _v, _i, _i]),
+    "extborn_create": (_i, [_pp, _v, _v, _v, ctypes.POINTER(_h)]),
+    "extborn_destroy": (None, [_h]),
+    "extborn_set_background": (_i, [_h, _v, _v]),
+    "extborn_forward": (_i, [_h, _v, _v, _v, _i, _i]),
+    "extborn_adjoint": (_i, [_h, _v, _v, _v, _i, _i]),
+    "wemop_create": (_i, [_pp, _v, _i, ctypes.POINTER(_h)]),
+    "wemop_destroy": (None, [_h]),
+    "wemop_onestep": (_i, [_h, _i, _f, _i, _v, _v, _i, _i]),
+    "wemop_oneway": (_i, [_h, _i, _f, _i, _v, _v, _i, _i]),
+    "wemop_scatter": (_i, [_h, _i, _f, _i, _v, _v, _i, _i]),
+    "wemop_refsampler": (_i, [_h, _v, _v]),
+}
+
+EXPORTED = tuple(_SIGS)
+
+
+def load(path: str = LIB_PATH):
+    """Load (once) and type the library.  Raises when it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build the CUDA library first (python -c 'import wemgpu; wemgpu.build()')")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class WemError(RuntimeError):
+    """A non-zero status of the C ABI, with the library's message."""
+
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn}: {msg} (status {code})")
+        self.code = code
+
+
+def call(name: str, *args) -> None:
+    lib = load()
+    rc = getattr(lib, name)(*args)
+    if rc != 0:
+        raise WemError(name, rc, lib.wem_last_error().decode(errors="replace"))

@@ -1,0 +1,234 @@
+"""Array-level handles over the C ABI.
+
+Arrays may be numpy (host; the library stages them through the GPU and the
+call returns when the result is back) or torch CUDA tensors (device; used
+in place).  Shapes follow the reference: models ``[nz][nx]`` (or
+``[nfreq][nz][nx]`` for the extended operators), data ``[ns][nr][nt]``
+float32 for time traces or ``[ns][nr][nbin]`` complex64 for bins.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .params import WemParams, WEM_DATA_FREQ, WEM_DATA_TIME
+
+try:
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+def _is_torch(a) -> bool:
+    return torch is not None and isinstance(a, torch.Tensor)
+
+
+def ptr(a, dtype, shape=None, name="array", writable=False):
+    """Raw pointer of a C-contiguous numpy array or torch tensor of the
+    expected dtype (complex64 / float32) and shape."""
+    if a is None:
+        raise ValueError(f"{name} is None")
+    if _is_torch(a):
+        tdt = {np.complex64: torch.complex64, np.float32: torch.float32}[dtype]
+        if a.dtype != tdt or not a.is_contiguous():
+            raise TypeError(f"{name}: need a contiguous {tdt} tensor, got {a.dtype}")
+        if shape is not None and tuple(a.shape) != tuple(shape):
+            raise ValueError(f"{name}: shape {tuple(a.shape)} != {tuple(shape)}")
+        return ctypes.c_void_p(a.data_ptr())
+    if not isinstance(a, np.ndarray) or a.dtype != dtype or not a.flags["C_CONTIGUOUS"]:
+        raise TypeError(f"{name}: need a C-contiguous numpy {np.dtype(dtype)} array")
+    if writable and not a.flags["WRITEABLE"]:
+        raise ValueError(f"{name} is read-only")
+    if shape is not None and tuple(a.shape) != tuple(shape):
+        raise ValueError(f"{name}: shape {tuple(a.shape)} != {tuple(shape)}")
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _data_kind(data):
+    if _is_torch(data):
+        return WEM_DATA_FREQ if data.is_complex() else WEM_DATA_TIME
+    return WEM_DATA_FREQ if np.iscomplexobj(data) else WEM_DATA_TIME
+
+
+class _Base:
+    _destroy = None
+
+    def __init__(self, p: WemParams, wavelet):
+        self.p = p.copy()
+        self.wavelet = np.ascontiguousarray(np.asarray(wavelet, dtype=np.float32)).reshape(-1)
+        if self.wavelet.size != p.nt:
+            raise ValueError(f"wavelet has {self.wavelet.size} samples, params say nt={p.nt}")
+        self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and h.value and self._destroy:
+            try:
+                getattr(_lib.load(), self._destroy)(h)
+            except Exception:
+                pass
+            self.h = ctypes.c_void_p()
+
+    # ---- shapes
+    @property
+    def model_shape(self):
+        return (self.p.nz, self.p.nx)
+
+    @property
+    def nbin(self):
+        return self.p.nbin if self.p.nbin else self.p.nt + self.p.tpad
+
+    def data_shape(self, kind):
+        return (self.p.ns, self.p.nr, self.p.nt if kind == WEM_DATA_TIME else self.nbin)
+
+    def _data_ptr(self, data, writable):
+        kind = _data_kind(data)
+        dt = np.float32 if kind == WEM_DATA_TIME else np.complex64
+        return ptr(data, dt, self.data_shape(kind), "data", writable), kind
+
+    def nfreq(self) -> int:
+        n = ctypes.c_int()
+        _lib.call("wem_count_freqs", ctypes.byref(self.p), None, ctypes.byref(n))
+        return n.value
+
+
+class WemOp(_Base):
+    """Nonlinear modelling (WEM::forward, propagator/src/WEMnl.cpp:39-82)."""
+
+    _destroy = "wem_destroy"
+
+    def __init__(self, p: WemParams, wavelet):
+        super().__init__(p, wavelet)
+        _lib.call("wem_create", ctypes.byref(self.p), self.wavelet.ctypes.data_as(ctypes.c_void_p),
+                  ctypes.byref(self.h))
+
+    def forward(self, s2, rho, data, add=False):
+        d, kind = self._data_ptr(data, True)
+        _lib.call("wem_forward", self.h, ptr(s2, np.complex64, self.model_shape, "slowness"),
+                  ptr(rho, np.complex64, self.model_shape, "density"), d, kind, int(bool(add)))
+        return data
+
+
+class BornOp(_Base):
+    """Born operator (BornFull, propagator/src/BornFull.cpp:13-117)."""
+
+    _destroy = "born_destroy"
+    _prefix = "born"
+
+    def __init__(self, p: WemParams, wavelet, bg_s2, bg_rho):
+        super().__init__(p, wavelet)
+        _lib.call(f"{self._prefix}_create", ctypes.byref(self.p), self.wavelet.ctypes.data_as(ctypes.c_void_p),
+                  ptr(bg_s2, np.complex64, self.model_shape, "slowness"),
+                  ptr(bg_rho, np.complex64, self.model_shape, "density"), ctypes.byref(self.h))
+
+    def set_background(self, s2, rho):
+        _lib.call(f"{self._prefix}_set_background", self.h, ptr(s2, np.complex64, self.model_shape, "slowness"),
+                  ptr(rho, np.complex64, self.model_shape, "density"))
+
+    def forward(self, ds2, drho, data, add=False):
+        d, kind = self._data_ptr(data, True)
+        _lib.call(f"{self._prefix}_forward", self.h, ptr(ds2, np.complex64, self.model_shape, "dslow"),
+                  ptr(drho, np.complex64, self.model_shape, "drho"), d, kind, int(bool(add)))
+        return data
+
+    def adjoint(self, ds2, drho, data, add=False):
+        d, kind = self._data_ptr(data, False)
+        _lib.call(f"{self._prefix}_adjoint", self.h, ptr(ds2, np.complex64, self.model_shape, "dslow", True),
+                  ptr(drho, np.complex64, self.model_shape, "drho", True), d, kind, int(bool(add)))
+        return ds2, drho
+
+
+class ExtWemOp(WemOp):
+    """Frequency-extended modelling (extWEM, propagator/src/extWEM.cpp:9-70)."""
+
+    _destroy = "extwem_destroy"
+
+    def __init__(self, p: WemParams, wavelet):
+        _Base.__init__(self, p, wavelet)
+        _lib.call("extwem_create", ctypes.byref(self.p), self.wavelet.ctypes.data_as(ctypes.c_void_p),
+                  ctypes.byref(self.h))
+
+    @property
+    def model_shape(self):
+        return (self.nfreq(), self.p.nz, self.p.nx)
+
+    def forward(self, s2, rho, data, add=False):
+        d, kind = self._data_ptr(data, True)
+        _lib.call("extwem_forward", self.h, ptr(s2, np.complex64, self.model_shape, "slowness"),
+                  ptr(rho, np.complex64, self.model_shape, "density"), d, kind, int(bool(add)))
+        return data
+
+
+class ExtBornOp(BornOp):
+    """Frequency-extended Born operator (extBornFull, ext_born_prop.cpp:8-194)."""
+
+    _destroy = "extborn_destroy"
+    _prefix = "extborn"
+
+    @property
+    def model_shape(self):
+        return (self.nfreq(), self.p.nz, self.p.nx)
+
+
+class RowOps:
+    """Row-level operators of one padded slowness grid [nz][nxg]
+    (py_wem_ops: SSF/PSPI, Down/Up, Scatter, RefSampler)."""
+
+    def __init__(self, p: WemParams, slow_padded):
+        self.p = p.copy()
+        self.nz, self.nxg = slow_padded.shape[-2], slow_padded.shape[-1]
+        if self.nz != p.nz:
+            raise ValueError("slowness depth axis does not match params.nz")
+        self.h = ctypes.c_void_p()
+        _lib.call("wemop_create", ctypes.byref(self.p), ptr(slow_padded, np.complex64, None, "slowness"),
+                  self.nxg, ctypes.byref(self.h))
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and h.value:
+            try:
+                _lib.load().wemop_destroy(h)
+            except Exception:
+                pass
+
+    def _rows(self, x, per_row):
+        n = int(np.prod(x.shape)) if not _is_torch(x) else x.numel()
+        if n % per_row:
+            raise ValueError("input size is not a whole number of rows")
+        return n // per_row
+
+    def onestep(self, iz, freq, adj, x, out=None, add=False):
+        out = _like(x) if out is None else out
+        n = self._rows(x, self.nxg)
+        _lib.call("wemop_onestep", self.h, int(iz), float(freq), int(adj), ptr(x, np.complex64), ptr(out, np.complex64),
+                  n, int(bool(add)))
+        return out
+
+    def oneway(self, up, freq, adj, x, out=None, add=False):
+        """``out is x`` (with add=True) is the drivers' in-place recursion."""
+        out = _like(x) if out is None else out
+        n = self._rows(x, self.nxg * self.nz)
+        _lib.call("wemop_oneway", self.h, int(up), float(freq), int(adj), ptr(x, np.complex64),
+                  ptr(out, np.complex64), n, int(bool(add)))
+        return out
+
+    def scatter(self, iz, freq, adj, x, out=None, add=False):
+        out = _like(x) if out is None else out
+        n = self._rows(x, self.nxg)
+        _lib.call("wemop_scatter", self.h, int(iz), float(freq), int(adj), ptr(x, np.complex64),
+                  ptr(out, np.complex64), n, int(bool(add)))
+        return out
+
+    def refsampler(self):
+        sref = np.zeros((self.nz, self.p.nref), np.complex64)
+        idx = np.zeros((self.nz, self.nxg), np.int32)
+        _lib.call("wemop_refsampler", self.h, ptr(sref, np.complex64), ctypes.c_void_p(idx.ctypes.data))
+        return sref, idx
+
+
+def _like(x):
+    if _is_torch(x):
+        return torch.zeros_like(x)
+    return np.zeros_like(x)

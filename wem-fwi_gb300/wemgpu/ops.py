@@ -1,0 +1,193 @@
+"""The reference's Python operator API, on the GB300 library.
+
+Class names, constructor arguments and ``forward(add, model, data)`` /
+``adjoint(add, model, data)`` follow propagator/src/python/WEM.py:8-134 and
+newExtWEM.py:8-38, so FWI/EFWI scripts written against the reference
+(scripts/fwi.py:70-71, scripts/efwi.py:97-98, scripts/mig.py:57-63) run on
+these classes unchanged apart from the import.  Models are a
+``superVector(slowness^2, density)``; data are real ``[ns][nr][nt]`` traces
+or complex ``[ns][nr][nbin]`` bins (the dtype of the data vector decides).
+"""
+from __future__ import annotations
+
+from typing import Any
+
+import numpy as np
+
+from . import core
+from .params import make_params
+from .vector import Hypercube, SuperVector, Vector
+
+
+def _grid_params(par, model_hyper: Hypercube, wave: Vector, data: Vector = None):
+    ax1, ax2 = model_hyper.getAxis(1), model_hyper.getAxis(2)
+    wt = wave.getHyper().getAxis(1)
+    p = make_params(par, nx=ax1.n, nz=ax2.n, dx=ax1.d, dz=ax2.d, ox=ax1.o, oz=ax2.o,
+                    nt=wt.n, dt=wt.d, ot=wt.o)
+    if data is not None and data.is_complex:
+        p.nbin = data.getHyper().getAxis(1).n
+    return p
+
+
+def _vecs(model):
+    if isinstance(model, SuperVector):
+        return model.vecs
+    if isinstance(model, (list, tuple)):
+        return list(model)
+    raise TypeError("Model vector should be a superVector")
+
+
+class Propagator:
+    """Base of the modelling operators (WEM.py:8-35)."""
+
+    def __init__(self, model, data, wave, par):
+        if not isinstance(model, SuperVector):
+            raise TypeError("Model vector should be a superVector")
+        self.wave = wave
+        self.par = par
+        self.domain = model
+        self.range = data
+
+    def setDomainRange(self, model, data):
+        self.domain, self.range = model, data
+
+    def _op(self):
+        raise NotImplementedError
+
+    @classmethod
+    def from_subspace(cls, subdomain, subrange, wave, par, *args, **kw):
+        """Operator for a block of shots (WEM.py:24-30): ns and osx come from
+        the sub-range's third axis."""
+        pars = dict(par.pars if hasattr(par, "pars") else par)
+        ax3 = subrange.getHyper().getAxis(3)
+        pars["ns"] = ax3.n
+        pars["osx"] = ax3.o
+        return cls(subdomain, subrange, wave, pars, *args, **kw)
+
+    def __getstate__(self):
+        state = self.__dict__.copy()
+        state.pop("cppMode", None)
+        return state
+
+    def dotTest(self, verbose=False, seed=0):
+        """<L m, d> versus <m, L^H d> for random m and d, add=False and add=True
+        (operator/src/Operator.h:23-48).  Returns the two relative errors."""
+        m = self.domain.clone().rand(seed)
+        d = self.range.clone().rand(seed + 7)
+        m1, d1 = self.domain.clone().zero(), self.range.clone().zero()
+        out = []
+        for add in (False, True):
+            if add:
+                m1.rand(seed + 11)
+                d1.rand(seed + 13)
+                m1c, d1c = m1.clone(), d1.clone()
+            self.forward(add, m, d1)
+            self.adjoint(add, m1, d)
+            if add:
+                lhs = d1.dot(d) - d1c.dot(d)
+                rhs = m1.dot(m) - m1c.dot(m)
+            else:
+                lhs, rhs = d1.dot(d), m1.dot(m)
+            err = abs(lhs - rhs) / max(abs(lhs), abs(rhs), 1e-300)
+            if verbose:
+                print(f"add={add}: <Lm,d>={lhs:.8e} <m,L'd>={rhs:.8e} rel={err:.3e}")
+            out.append(err)
+        return out
+
+
+class WEM(Propagator):
+    """Nonlinear one-way modelling (WEM.py:37-50; WEMnl.cpp, wem_prop.cpp)."""
+
+    def __init__(self, model, data, wave, par):
+        super().__init__(model, data, wave, par)
+        self.params = _grid_params(par, _vecs(model)[0].getHyper(), wave, data)
+        self.cppMode = core.WemOp(self.params, wave.getNdArray())
+
+    def __setstate__(self, state):
+        self.__dict__ = state.copy()
+        self.cppMode = core.WemOp(self.params, self.wave.getNdArray())
+
+    def get_nfreq(self):
+        return self.cppMode.nfreq()
+
+    def forward(self, add, model, data):
+        m = _vecs(model)
+        self.cppMode.forward(m[0].getNdArray(), m[1].getNdArray(), data.getNdArray(), add)
+
+
+class Born(Propagator):
+    """Born operator (WEM.py:52-80; BornFull).  ``mode='real'`` zeroes the
+    imaginary part of the model around the calls, as the reference does."""
+
+    def __init__(self, model, data, wave, par, mode=None):
+        super().__init__(model, data, wave, par)
+        self.mode = mode
+        m = _vecs(model)
+        self.params = _grid_params(par, m[0].getHyper(), wave, data)
+        self.cppMode = core.BornOp(self.params, wave.getNdArray(), m[0].getNdArray(), m[1].getNdArray())
+
+    def __setstate__(self, state):
+        self.__dict__ = state.copy()
+        m = _vecs(self.domain)
+        self.cppMode = core.BornOp(self.params, self.wave.getNdArray(), m[0].getNdArray(), m[1].getNdArray())
+
+    @classmethod
+    def from_subspace(cls, subdomain, subrange, wave, par, mode=None):
+        return super().from_subspace(subdomain, subrange, wave, par, mode=mode)
+
+    def set_background(self, slow):
+        m = _vecs(slow)
+        self.cppMode.set_background(m[0].getNdArray(), m[1].getNdArray())
+
+    def forward(self, add, model, data):
+        m = _vecs(model)
+        if self.mode == "real":
+            for v in m:
+                v.getNdArray().imag[...] = 0
+        self.cppMode.forward(m[0].getNdArray(), m[1].getNdArray(), data.getNdArray(), add)
+
+    def adjoint(self, add, model, data):
+        m = _vecs(model)
+        self.cppMode.adjoint(m[0].getNdArray(), m[1].getNdArray(), data.getNdArray(), add)
+        if self.mode == "real":
+            for v in m:
+                v.getNdArray().imag[...] = 0
+
+
+class extWEM(Propagator):
+    """Frequency-extended modelling (newExtWEM.py:8-24): model axis 3 is the
+    propagated frequency."""
+
+    def __init__(self, model, data, wave, par):
+        super().__init__(model, data, wave, par)
+        self.params = _grid_params(par, _vecs(model)[0].getHyper(), wave, data)
+        self.cppMode = core.ExtWemOp(self.params, wave.getNdArray())
+        nw = _vecs(model)[0].getHyper().getAxis(3).n
+        if nw != self.cppMode.nfreq():
+            raise ValueError("Model is of the wrong size!")
+
+    def forward(self, add, model, data):
+        m = _vecs(model)
+        self.cppMode.forward(m[0].getNdArray(), m[1].getNdArray(), data.getNdArray(), add)
+
+
+class extBorn(Propagator):
+    """Frequency-extended Born operator (newExtWEM.py:26-38)."""
+
+    def __init__(self, model, data, wave, par):
+        super().__init__(model, data, wave, par)
+        m = _vecs(model)
+        self.params = _grid_params(par, m[0].getHyper(), wave, data)
+        self.cppMode = core.ExtBornOp(self.params, wave.getNdArray(), m[0].getNdArray(), m[1].getNdArray())
+
+    def set_background(self, slow):
+        m = _vecs(slow)
+        self.cppMode.set_background(m[0].getNdArray(), m[1].getNdArray())
+
+    def forward(self, add, model, data):
+        m = _vecs(model)
+        self.cppMode.forward(m[0].getNdArray(), m[1].getNdArray(), data.getNdArray(), add)
+
+    def adjoint(self, add, model, data):
+        m = _vecs(model)
+        self.cppMode.adjoint(m[0].getNdArray(), m[1].getNdArray(), data.getNdArray(), add)

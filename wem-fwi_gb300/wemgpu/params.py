@@ -1,0 +1,114 @@
+"""Parameter block of the C ABI (include/wemgpu.h ``wem_params``).
+
+The reference reads its operator parameters from a SEP ``paramObj`` filled
+from a JSON/dict (``genericIO.pythonParams``, scripts/fwi.py:33-35) and takes
+the grid from the model's hypercube.  :func:`make_params` accepts the same
+keys (``ns, osx, dsx, osz, nr, orx, drx, orz, prop, nref, tap, pad, tpad, eps,
+fmin, fmax, nfreq, ngs, ngr, ntaylor``) plus the grid and wavelet axes, with
+the defaults the reference's ``getInt/getFloat`` calls use.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Any, Mapping
+
+import numpy as np
+
+WEM_OK, WEM_EINVAL, WEM_ENOMEM, WEM_EDEVICE, WEM_ETIMEOUT, WEM_ENOTIMPL = range(6)
+WEM_PROP_SSF, WEM_PROP_PSPI = 0, 1
+WEM_ADJ_COMPAT, WEM_ADJ_EXACT = 0, 1
+WEM_REFS_ASCODED, WEM_REFS_NEAREST = 0, 1
+WEM_DATA_TIME, WEM_DATA_FREQ = 0, 1
+
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+class WemParams(ctypes.Structure):
+    """ctypes mirror of ``struct wem_params``; field order is the ABI."""
+
+    _fields_ = [
+        ("nx", ctypes.c_int), ("nz", ctypes.c_int),
+        ("ox", ctypes.c_float), ("oz", ctypes.c_float),
+        ("dx", ctypes.c_float), ("dz", ctypes.c_float),
+        ("nt", ctypes.c_int), ("ot", ctypes.c_float), ("dt", ctypes.c_float),
+        ("ns", ctypes.c_int), ("osx", ctypes.c_float), ("osz", ctypes.c_float),
+        ("dsx", ctypes.c_float), ("dsz", ctypes.c_float),
+        ("nr", ctypes.c_int), ("orx", ctypes.c_float), ("orz", ctypes.c_float),
+        ("drx", ctypes.c_float), ("drz", ctypes.c_float),
+        ("src_x", _fp), ("src_z", _fp), ("rec_x", _fp), ("rec_z", _fp),
+        ("prop", ctypes.c_int), ("nref", ctypes.c_int), ("tap", ctypes.c_int),
+        ("pad", ctypes.c_int), ("tpad", ctypes.c_int),
+        ("ngs", ctypes.c_int), ("ngr", ctypes.c_int), ("ntaylor", ctypes.c_int),
+        ("eps", ctypes.c_float), ("fmin", ctypes.c_float), ("fmax", ctypes.c_float),
+        ("nfreq", ctypes.c_int),
+        ("adjoint_mode", ctypes.c_int), ("refs_mode", ctypes.c_int), ("nbin", ctypes.c_int),
+    ]
+
+    def __init__(self, *a, **kw):
+        super().__init__(*a, **kw)
+        self._keep: list = []  # keeps coordinate arrays alive
+
+    def copy(self) -> "WemParams":
+        c = WemParams()
+        ctypes.pointer(c)[0] = self
+        c._keep = list(self._keep)
+        return c
+
+    def as_dict(self) -> dict:
+        return {n: getattr(self, n) for n, _ in self._fields_ if not n.endswith(("_x", "_z"))}
+
+
+_DEFAULTS = dict(
+    ox=0.0, oz=0.0, ot=0.0,
+    ns=0, osx=0.0, osz=0.0, dsx=0.0, dsz=0.0,
+    nr=0, orx=0.0, orz=0.0, drx=0.0, drz=0.0,
+    prop="ssf", nref=1, tap=0, pad=0, tpad=0, ngs=0, ngr=0, ntaylor=1,
+    eps=0.04, fmin=1.0, fmax=0.0, nfreq=0,
+    adjoint_mode="compat", refs_mode="ascoded", nbin=0,
+)
+
+
+def _as_mapping(par: Any) -> Mapping:
+    if par is None:
+        return {}
+    if isinstance(par, Mapping):
+        return par
+    if hasattr(par, "pars"):  # genericIO.pythonParams
+        return par.pars
+    raise TypeError("par must be a dict or an object with a .pars dict")
+
+
+def make_params(par: Any, *, nx: int, nz: int, dx: float, dz: float,
+                nt: int, dt: float, ox: float = 0.0, oz: float = 0.0,
+                ot: float = 0.0) -> WemParams:
+    """Build the ABI parameter block from reference-style keys."""
+    m = dict(_DEFAULTS)
+    m.update({k: v for k, v in _as_mapping(par).items()})
+    p = WemParams()
+    p.nx, p.nz, p.dx, p.dz = int(nx), int(nz), float(dx), float(dz)
+    given = _as_mapping(par)
+    p.ox = float(given["ox"]) if "ox" in given else float(ox)
+    p.oz = float(given["oz"]) if "oz" in given else float(oz)
+    p.nt, p.dt, p.ot = int(nt), float(dt), float(ot)
+    for k in ("ns", "nr", "nref", "tap", "pad", "tpad", "ngs", "ngr", "ntaylor", "nfreq", "nbin"):
+        setattr(p, k, int(m[k]))
+    for k in ("osx", "osz", "dsx", "dsz", "orx", "orz", "drx", "drz", "eps", "fmin", "fmax"):
+        setattr(p, k, float(m[k]))
+    prop = m["prop"]
+    p.prop = WEM_PROP_PSPI if str(prop).lower() == "pspi" or prop == WEM_PROP_PSPI else WEM_PROP_SSF
+    am = m["adjoint_mode"]
+    p.adjoint_mode = WEM_ADJ_EXACT if str(am).lower() == "exact" or am == WEM_ADJ_EXACT else WEM_ADJ_COMPAT
+    rm = m["refs_mode"]
+    p.refs_mode = WEM_REFS_NEAREST if str(rm).lower() == "nearest" or rm == WEM_REFS_NEAREST else WEM_REFS_ASCODED
+    # irregular geometry: explicit coordinate lists replace the regular grid
+    for key, field, count in (("sx", "src_x", "ns"), ("sz", "src_z", "ns"),
+                              ("rx", "rec_x", "nr"), ("rz", "rec_z", "nr")):
+        if key in m and m[key] is not None:
+            arr = np.ascontiguousarray(np.asarray(m[key], dtype=np.float32))
+            if count == "ns":
+                p.ns = int(arr.size)
+            else:
+                p.nr = int(arr.size)
+            p._keep.append(arr)
+            setattr(p, field, arr.ctypes.data_as(_fp))
+    return p
