@@ -1,0 +1,367 @@
+#!/usr/bin/env python
+"""FWI gradient benchmark (configuration c3) on GB300.
+
+One step = one FWI gradient evaluation as the reference's FWI scripts do it
+(scripts/fwi.py:70-113): nonlinear modelling of the current model (WEM
+forward), the data residual, and the gradient as the Born adjoint of the
+residual at the current model (BornFull::adjoint, compat mode), over all
+32 shots x 96 frequencies of a 768 x 300 model (SSF, N = 768).
+
+Reported: ``value`` = depth-steps/s with inputs resident on the GPU, where a
+depth-step is one (shot, frequency) row advanced one depth in one one-way or
+linearised pass of the reference's call sequence (2 passes for WEM forward,
+10 for the Born adjoint), so the figure is comparable with the reference's
+own work; ``s_per_iter`` = seconds per gradient; ``e2e`` = the same through
+the C ABI with host buffers (copies inside the timed region); ``roofline``
+for the dominant kernel from CUDA events on its launch stream;
+``cpu_baseline`` = the CPU restatement on the host cores on a bounded sample.
+
+``--impl reference`` times the CPU restatement of the reference (the
+reference itself cannot be built: FFTW, TBB, Boost, SEP I/O and ISPC are
+absent) on the same configuration and metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "wem-fwi_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "FWI gradient s/iter & depth-steps/s, batched+adjoint vs plain GPU at L2<=1e-4"
+PASSES_WEM = 2       # Down + Up (wem_prop.cpp:57,68)
+PASSES_BORN_ADJ = 10  # born_prop.cpp:190-215: 1 down, 3 Up^H, 2 Down^H, 2 LinDown^H, 1 up, 1 LinUp^H
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return float(m["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def workload(small=False):
+    from wemgpu import synthetic as S
+    cfg = S.c3()
+    if small:  # a reduced case of the same kernels for profiling captures
+        cfg["par"] = dict(cfg["par"], ns=8, dsx=cfg["par"]["dsx"] * 4, fmax=6.0)
+    return cfg
+
+
+def row_steps(p, nfreq):
+    return (PASSES_WEM + PASSES_BORN_ADJ) * p.ns * nfreq * (p.nz - 1)
+
+
+def algorithmic_bytes(kernel, p, nfreq, G):
+    """HBM bytes a launch must move (roofline section)."""
+    nxg = p.nx + 2 * p.pad
+    N = nxg + 2 * p.tap
+    rows = p.ns * nfreq
+    groups = nfreq * ((p.ns + G - 1) // G)
+    tables = nfreq * p.nz * (N * p.nref + nxg) * 8  # phase + split-step rows per (f, z)
+    if kernel == "k_wem":
+        return rows * p.nz * 16 * nxg + 2 * tables
+    if kernel == "k_born_adj":
+        return rows * p.nz * 32 * nxg + groups * p.nz * 16 * nxg + 4 * tables
+    if kernel == "k_born_fwd":
+        return rows * p.nz * 32 * nxg + 2 * tables
+    return None
+
+
+def run_gpu(args, rank, world):
+    import torch
+    import wemgpu
+    from wemgpu import _lib, synthetic as S
+    from wemgpu.core import BornOp, WemOp
+
+    wemgpu.build()
+    lib = _lib.load()
+    dev = torch.device(f"cuda:{int(os.environ.get('LOCAL_RANK', 0))}")
+    torch.cuda.set_device(dev)
+    cfg = workload(args.small)
+    p = S.params_of(cfg)
+    # weak scaling: every rank owns its own block of shots of the same size
+    nf = WemOp(p, cfg["wavelet"]).nfreq()
+    wav = cfg["wavelet"]
+    s_true = torch.from_numpy(cfg["slow_true"]).to(dev)
+    s0 = torch.from_numpy(cfg["slow"]).to(dev)
+    rho = torch.from_numpy(cfg["rho"]).to(dev)
+    wem = WemOp(p, wav)
+    born = BornOp(p, wav, s0, rho)
+    d_obs = torch.zeros((p.ns, p.nr, p.nt), dtype=torch.float32, device=dev)
+    wem.forward(s_true, rho, d_obs)
+    d_syn = torch.zeros_like(d_obs)
+    g0, g1 = torch.zeros_like(s0), torch.zeros_like(s0)
+
+    def step():
+        wem.forward(s0, rho, d_syn)
+        res = d_syn - d_obs
+        born.set_background(s0, rho)
+        born.adjoint(g0, g1, res)
+        if world > 1:
+            torch.distributed.all_reduce(g0)
+        return g0
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    lib.wem_stats_reset()
+    lib.wem_stats_enable(1)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev.index) as clk:
+        torch.cuda.synchronize()
+        ev0.record()
+        for _ in range(args.steps):
+            step()
+        ev1.record()
+        torch.cuda.synchronize()
+    lib.wem_stats_enable(0)
+    ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    s_per_iter = ms / 1e3 / args.steps
+    steps_per_iter = row_steps(p, nf) * world
+    value = steps_per_iter / s_per_iter
+
+    # dominant kernel and its roofline
+    kstats = {k: _lib.kernel_stats(k) for k in ("k_wem", "k_born_adj", "k_born_fwd")}
+    kstats = {k: v for k, v in kstats.items() if v[1] > 0}
+    top = max(kstats, key=lambda k: kstats[k][0])
+    top_ms, top_n = kstats[top]
+    G = min(p.ns, 8)
+    algo = algorithmic_bytes(top, p, nf, G)
+    peak, peak_src = peaks()
+    achieved = algo / (top_ms / top_n / 1e3) / 1e9
+    launches = sum(v[1] for v in kstats.values())
+    # other kernels (tables, reductions, transforms) per step: counted from the pass structure
+    gpu_launches = int(launches + args.steps * 9)
+
+    # end to end through the C ABI with host buffers
+    s0h, rhoh = cfg["slow"], cfg["rho"]
+    d_obs_h = d_obs.cpu().numpy()
+    d_syn_h = np.zeros_like(d_obs_h)
+    g0h, g1h = np.zeros_like(s0h), np.zeros_like(s0h)
+
+    def step_host():
+        wem.forward(s0h, rhoh, d_syn_h)
+        res = d_syn_h - d_obs_h
+        born.set_background(s0h, rhoh)
+        born.adjoint(g0h, g1h, res)
+
+    step_host()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step_host()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    h2d = 2 * s0h.nbytes + 2 * rhoh.nbytes + d_obs_h.nbytes  # model twice (WEM, Born), residual
+    d2h = d_syn_h.nbytes + g0h.nbytes + g1h.nbytes
+
+    # plain form: every (shot, frequency) row in its own launch, timed on a
+    # sample of shots and scaled to the whole job
+    plain = None
+    if not args.no_plain and rank == 0:
+        cfgp = dict(cfg)
+        ns_p = 1
+        cfgp["par"] = dict(cfg["par"], ns=ns_p)
+        pp = S.params_of(cfgp)
+        wp = WemOp(pp, wav)
+        bp = BornOp(pp, wav, s0, rho)
+        dp = torch.zeros((pp.ns, pp.nr, pp.nt), dtype=torch.float32, device=dev)
+        a0, a1 = torch.zeros_like(s0), torch.zeros_like(s0)
+        lib.wem_set_plain(1)
+        try:
+            wp.forward(s0, rho, dp)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            wp.forward(s0, rho, dp)
+            bp.set_background(s0, rho)
+            bp.adjoint(a0, a1, dp)
+            e1.record()
+            torch.cuda.synchronize()
+            plain_s = e0.elapsed_time(e1) / 1e3 * p.ns / ns_p
+        finally:
+            lib.wem_set_plain(0)
+        plain = {"s_per_iter": plain_s, "sample": f"{ns_p} shots x {nf} freqs, scaled to {p.ns} shots",
+                 "batched_speedup": plain_s / s_per_iter}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_sample(cfg, seconds=args.cpu_seconds)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "depth-steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded c3 model, see wemgpu/synthetic.py)",
+        "config": {"workload": "c3 FWI gradient: WEM fwd + residual + Born adjoint (compat)",
+                   "nx": p.nx, "nz": p.nz, "dx": p.dx, "shots": p.ns * world, "freqs": nf, "fft_n": p.nx,
+                   "prop": "ssf", "depth_steps_per_iter": steps_per_iter,
+                   "l2": "inputs larger than L2 (stored wavefields ~11 GB per pass)",
+                   "small": bool(args.small)},
+        "s_per_iter": s_per_iter,
+        "e2e": {"value": steps_per_iter / e2e_s, "unit": "depth-steps/s", "s_per_iter": e2e_s,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
+                     "algorithmic_bytes": algo, "ms_per_launch": top_ms / top_n, "traffic": None},
+        "kernels": {k: {"ms": v[0] / args.steps, "launches": v[1] // args.steps} for k, v in kstats.items()},
+        "gpu_launches": gpu_launches,
+        "plain_gpu": plain,
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def cpu_sample(cfg, seconds=15.0, nthreads=0):
+    """The CPU restatement (oracle, fp32) on a bounded sample of the same
+    workload: the first shots and frequencies, all depths."""
+    from oracle import oracle as O
+    from wemgpu import synthetic as S
+    O.build()
+    nthreads = nthreads or os.cpu_count() or 1
+    # grow the sample (frequencies first) until it takes a few seconds, then
+    # scale to the budget
+    nfk = 4
+    p_full = S.params_of(cfg)
+    tmax = p_full.ot + p_full.dt * (p_full.nt + p_full.tpad - 1)
+    while True:
+        par = dict(cfg["par"], ns=1, fmax=cfg["par"]["fmin"] + (nfk - 0.5) / tmax)
+        c = dict(cfg, par=par)
+        p = S.params_of(c)
+        nf = O.count_freqs(p)[0]
+        t0 = time.perf_counter()
+        syn = O.wem_forward(p, cfg["wavelet"], cfg["slow"], cfg["rho"], kind=0, prec=32, nthreads=nthreads)
+        O.born_adjoint(p, cfg["wavelet"], cfg["slow"], cfg["rho"], syn, kind=0, prec=32, nthreads=nthreads,
+                       fchunks=max(1, nthreads))
+        dt = time.perf_counter() - t0
+        if dt > 0.5 * seconds or nfk >= 96:
+            break
+        nfk = min(96, max(nfk * 2, int(nfk * seconds / max(dt, 1e-3))))
+    rate = row_steps(p, nf) / dt
+    return {"value": rate, "unit": "depth-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"1 shot x {nf} freqs of c3 (all {p.nz} depths), WEM fwd + Born adjoint, {dt:.1f} s",
+            "s_per_iter_extrapolated": row_steps(S.params_of(cfg), 96) / rate}
+
+
+def run_reference(args, rank, world):
+    """CPU restatement on the host cores, same config / metric / unit."""
+    if rank != 0:
+        return
+    cfg = workload(args.small)
+    res = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(cfg, seconds=10.0)
+        if i >= args.warmup:
+            res.append(r["value"])
+    v = float(np.median(res))
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "depth-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded c3 model)",
+            "config": {"workload": "c3 FWI gradient: WEM fwd + residual + Born adjoint (compat)"},
+            "cpu_baseline": {"value": v, "unit": "depth-steps/s", "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": v, "unit": "depth-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--small", action="store_true", help="reduced case (profiling captures)")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "gpu" else "gloo")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -109,6 +109,20 @@ int wem_count_freqs(const wem_params* p, const float* wavelet, int* nfreq);
 const char* wem_last_error(void);
 const char* wem_version(void);
 
+/* Kernel timing (no counterpart in the reference: measurement support).
+ * While enabled, every pass kernel is bracketed by CUDA events on the stream
+ * it is launched on; per-kernel totals accumulate until reset.  Kernel names:
+ * "k_wem", "k_born_fwd", "k_born_adj". */
+int wem_stats_enable(int on);
+int wem_stats_get(const char* kernel, double* total_ms, long long* launches);
+int wem_stats_reset(void);
+
+/* Launch shape (no counterpart in the reference: measurement support).
+ * plain = 1 runs every (shot, frequency) row as its own kernel launch, one
+ * CTA per launch: the unbatched GPU form the batched path is compared with.
+ * plain = 0 (default) runs all groups of rows in one launch per pass. */
+int wem_set_plain(int plain);
+
 /* ------------------------------------------------ nonlinear modelling (WEM) */
 typedef struct wem_handle wem_handle;
 

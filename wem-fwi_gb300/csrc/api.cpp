@@ -24,6 +24,22 @@ namespace {
 
 thread_local std::string g_error;
 
+// per-kernel CUDA-event timing (wem_stats_*)
+struct KStat {
+  double ms = 0;
+  long long n = 0;
+};
+bool g_stats_on = false;
+bool g_plain = false;
+std::vector<std::pair<std::string, KStat>> g_stats;
+
+KStat& stat_of(const std::string& name) {
+  for (auto& kv : g_stats)
+    if (kv.first == name) return kv.second;
+  g_stats.emplace_back(name, KStat{});
+  return g_stats.back().second;
+}
+
 void cuda_check(cudaError_t e, const char* what) {
   if (e == cudaSuccess) return;
   int code = (e == cudaErrorMemoryAllocation) ? WEM_ENOMEM : WEM_EDEVICE;
@@ -117,6 +133,29 @@ struct Staged {
   }
 };
 
+// launches `fn` on stream 0, bracketed by events when timing is enabled
+template <class Fn>
+void timed(const char* name, Fn fn) {
+  if (!g_stats_on) {
+    fn();
+    return;
+  }
+  cudaEvent_t a, b;
+  cuda_check(cudaEventCreate(&a), "event");
+  cuda_check(cudaEventCreate(&b), "event");
+  cuda_check(cudaEventRecord(a, 0), "event");
+  fn();
+  cuda_check(cudaEventRecord(b, 0), "event");
+  cuda_check(cudaEventSynchronize(b), "event");
+  float ms = 0;
+  cuda_check(cudaEventElapsedTime(&ms, a, b), "event");
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  KStat& k = stat_of(name);
+  k.ms += ms;
+  k.n += 1;
+}
+
 std::vector<float> host_floats(const void* p, size_t nfloat) {
   std::vector<float> h(nfloat);
   if (is_device_ptr(p)) cuda_check(cudaMemcpy(h.data(), p, nfloat * 4, cudaMemcpyDeviceToHost), "D2H");
@@ -153,7 +192,7 @@ class Engine {
     int G = pick_G([&](int g) { return smem_wem(ctx_, g); });
     for_chunks(G, plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = store1_.as<float2>((size_t)rows * plane);
-      launch_wem(ctx_, gd, ng, G, A, bins, 0);
+      timed("k_wem", [&] { launch_wem(ctx_, gd, ng, G, A, bins, 0); });
       cuda_check(cudaGetLastError(), "k_wem launch");
     });
     emit(data, kind, add);
@@ -173,7 +212,7 @@ class Engine {
     for_chunks(G, 2 * plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = store1_.as<float2>((size_t)rows * plane);
       float2* B = store2_.as<float2>((size_t)rows * plane);
-      launch_born_fwd(ctx_, gd, ng, G, dm0, drm, A, B, bins, 0);
+      timed("k_born_fwd", [&] { launch_born_fwd(ctx_, gd, ng, G, dm0, drm, A, B, bins, 0); });
       cuda_check(cudaGetLastError(), "k_born_fwd launch");
     });
     emit(data, kind, add);
@@ -196,7 +235,7 @@ class Engine {
       float2* T = store2_.as<float2>((size_t)rows * plane);
       float2* pr = part1_.as<float2>((size_t)ng * plane);
       float2* ps = part2_.as<float2>((size_t)ng * plane);
-      launch_born_adj(ctx_, gd, ng, G, BG, T, bins_, pr, ps, compat, 0);
+      timed("k_born_adj", [&] { launch_born_adj(ctx_, gd, ng, G, BG, T, bins_, pr, ps, compat, 0); });
       cuda_check(cudaGetLastError(), "k_born_adj launch");
       // chunk-local group ranges of each model slice
       std::vector<int> beg(M_ + 1, 0);
@@ -351,7 +390,7 @@ class Engine {
   template <class F>
   int pick_G(F smem_of) {
     int lim = max_smem_per_block();
-    int G = std::min(geo_.ns, 8);
+    int G = g_plain ? 1 : std::min(geo_.ns, 8);
     while (G > 1 && (int)smem_of(G) > lim) --G;
     require((int)smem_of(G) <= lim, "row too long for one CTA's shared memory");
     return G;
@@ -368,6 +407,7 @@ class Engine {
     cuda_check(cudaMemGetInfo(&freeb, &totalb), "cudaMemGetInfo");
     size_t budget = std::min<size_t>((size_t)(0.6 * (double)freeb), (size_t)96 << 30);
     size_t max_rows = std::max<size_t>(G, budget / std::max<size_t>(bytes_per_row, 1));
+    if (g_plain) max_rows = 1;  // one row per launch
     size_t i = 0;
     while (i < all.size()) {
       std::vector<Group> chunk;
@@ -572,6 +612,27 @@ void wem_params_default(wem_params* p) {
 }
 
 const char* wem_last_error(void) { return g_error.c_str(); }
+
+int wem_stats_enable(int on) {
+  g_stats_on = on != 0;
+  return WEM_OK;
+}
+int wem_stats_get(const char* kernel, double* total_ms, long long* launches) {
+  return guard([&] {
+    require(kernel && total_ms && launches, "NULL argument");
+    KStat& k = stat_of(kernel);
+    *total_ms = k.ms;
+    *launches = k.n;
+  });
+}
+int wem_set_plain(int plain) {
+  g_plain = plain != 0;
+  return WEM_OK;
+}
+int wem_stats_reset(void) {
+  g_stats.clear();
+  return WEM_OK;
+}
 const char* wem_version(void) { return "wemgpu 0.1 (sm_103a)"; }
 
 int wem_count_freqs(const wem_params* p, const float* wavelet, int* nfreq) {

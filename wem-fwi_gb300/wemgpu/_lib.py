@@ -26,6 +26,10 @@ _SIGS = {
     "wem_count_freqs": (_i, [_pp, _v, ctypes.POINTER(_i)]),
     "wem_last_error": (ctypes.c_char_p, []),
     "wem_version": (ctypes.c_char_p, []),
+    "wem_stats_enable": (_i, [_i]),
+    "wem_stats_get": (_i, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
+    "wem_stats_reset": (_i, []),
+    "wem_set_plain": (_i, [_i]),
     "wem_create": (_i, [_pp, _v, ctypes.POINTER(_h)]),
     "wem_destroy": (None, [_h]),
     "wem_get_nfreq": (_i, [_h, ctypes.POINTER(_i)]),
@@ -77,6 +81,13 @@ class WemError(RuntimeError):
     def __init__(self, fn: str, code: int, msg: str):
         super().__init__(f"{fn}: {msg} (status {code})")
         self.code = code
+
+
+def kernel_stats(name: str):
+    """(total ms, launches) of one pass kernel since the last reset."""
+    ms, n = ctypes.c_double(), ctypes.c_longlong()
+    call("wem_stats_get", name.encode(), ctypes.byref(ms), ctypes.byref(n))
+    return ms.value, n.value
 
 
 def call(name: str, *args) -> None:
