@@ -123,6 +123,13 @@ int wem_stats_reset(void);
  * plain = 0 (default) runs all groups of rows in one launch per pass. */
 int wem_set_plain(int plain);
 
+/* Kernel family (no counterpart in the reference: test and measurement
+ * support).  0 automatic (warp-per-row kernels when N = 32 E with E in
+ * {8, 12, 16, 24, 32}, shared-memory kernels otherwise), 1 shared-memory
+ * kernels only, 2 warp-per-row kernels only (WEM_EINVAL when N is not
+ * supported). */
+int wem_set_kernel_path(int path);
+
 /* ------------------------------------------------ nonlinear modelling (WEM) */
 typedef struct wem_handle wem_handle;
 

@@ -207,3 +207,66 @@ def test_ext_born(gpu_lib, oracle, mode):
     b0, b1 = oracle.extborn_adjoint(p, wav, s3, r3, d, prec=32)
     assert rel_l2(a0, b0) < TOL_OP, rel_l2(a0, b0)
     assert rel_l2(a1, b1) < TOL_OP, rel_l2(a1, b1)
+
+
+# ---------------------------------------------------------------- warp path
+# Row lengths N = 32 E run on the warp-per-row kernels (automatic choice);
+# the same cases also run on the shared-memory kernels (path 1) so both
+# families are held to the oracle.
+WARP_CASES = {
+    "n256": dict(nx=240, pad=4, tap=4, prop="ssf", nref=1),
+    "n384": dict(nx=376, pad=0, tap=4, prop="pspi", nref=2),
+    "n768": dict(nx=752, pad=4, tap=4, prop="ssf", nref=1),
+    "n1024": dict(nx=1016, pad=0, tap=4, prop="pspi", nref=2),
+}
+
+
+@pytest.fixture
+def kernel_path(gpu_lib, request):
+    from wemgpu import _lib
+    _lib.call("wem_set_kernel_path", request.param)
+    yield request.param
+    _lib.call("wem_set_kernel_path", 0)
+
+
+@pytest.mark.parametrize("case", list(WARP_CASES))
+@pytest.mark.parametrize("kernel_path", [0, 1], indirect=True)
+def test_paths_wem_and_born(gpu_lib, oracle, case, kernel_path):
+    from wemgpu.core import BornOp, WemOp
+    kw = WARP_CASES[case]
+    for mode in ("compat", "exact"):
+        p, par, wav, s, rho = small_case(nz=16, ns=2, adjoint_mode=mode, **kw)
+        rng = np.random.default_rng(11)
+        if mode == "compat":
+            d = np.zeros((p.ns, p.nr, p.nt), np.float32)
+            WemOp(p, wav).forward(s, rho, d)
+            o = oracle.wem_forward(p, wav, s, rho, kind=WEM_DATA_TIME, prec=64)
+            assert rel_l2(d, o) < TOL_OP, ("wem", rel_l2(d, o))
+            ds = (rand_c(rng, s.shape) * 1e-8).astype(np.complex64)
+            dr = (rand_c(rng, s.shape) * 0.1).astype(np.complex64)
+            op = BornOp(p, wav, s, rho)
+            g = np.zeros((p.ns, p.nr, p.nt), np.float32)
+            op.forward(ds, dr, g)
+            o = oracle.born_forward(p, wav, s, rho, ds, dr, kind=WEM_DATA_TIME, prec=64)
+            assert rel_l2(g, o) < TOL_OP, ("born fwd", rel_l2(g, o))
+        op = BornOp(p, wav, s, rho)
+        dd = (rng.random((p.ns, p.nr, p.nt)) - .5).astype(np.float32)
+        a0, a1 = np.zeros_like(s), np.zeros_like(s)
+        op.adjoint(a0, a1, dd)
+        q0, q1 = oracle.born_adjoint(p, wav, s, rho, dd, kind=WEM_DATA_TIME, prec=64)
+        assert rel_l2(a0, q0) < TOL_OP, (mode, "adj s", rel_l2(a0, q0))
+        assert rel_l2(a1, q1) < TOL_OP, (mode, "adj rho", rel_l2(a1, q1))
+
+
+@pytest.mark.parametrize("case", ["n256", "n768"])
+def test_warp_path_is_deterministic(gpu_lib, case):
+    from wemgpu.core import BornOp
+    p, par, wav, s, rho = small_case(nz=16, ns=2, **WARP_CASES[case])
+    op = BornOp(p, wav, s, rho)
+    d = (np.random.default_rng(12).random((p.ns, p.nr, p.nt)) - .5).astype(np.float32)
+    outs = []
+    for _ in range(2):
+        a0, a1 = np.zeros_like(s), np.zeros_like(s)
+        op.adjoint(a0, a1, d)
+        outs.append((a0, a1))
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])

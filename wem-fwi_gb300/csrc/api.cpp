@@ -31,6 +31,7 @@ struct KStat {
 };
 bool g_stats_on = false;
 bool g_plain = false;
+int g_path = 0;  // 0 automatic, 1 shared-memory kernels, 2 warp-per-row kernels
 std::vector<std::pair<std::string, KStat>> g_stats;
 
 KStat& stat_of(const std::string& name) {
@@ -185,14 +186,25 @@ class Engine {
     have_bg_ = true;
   }
 
+  bool warp_path() const {
+    if (g_path == 1) return false;
+    bool ok = warp_path_supported(ctx_);
+    require(ok || g_path != 2, "warp-per-row kernels need N = 32 E with E in {8,12,16,24,32}");
+    return ok;
+  }
+
+  int warp_G() const { return g_plain ? 1 : std::min(geo_.ns, warp_rows_per_group()); }
+
   void wem_forward(const void* s2, const void* rho, void* data, int kind, int add) {
     set_background(s2, rho);
     float2* bins = zero_bins();
     const size_t plane = (size_t)p_.nz * geo_.nxg;
-    int G = pick_G([&](int g) { return smem_wem(ctx_, g); });
+    const bool wp = warp_path();
+    int G = wp ? warp_G() : pick_G([&](int g) { return smem_wem(ctx_, g); });
     for_chunks(G, plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = store1_.as<float2>((size_t)rows * plane);
-      timed("k_wem", [&] { launch_wem(ctx_, gd, ng, G, A, bins, 0); });
+      if (wp) timed("k_wem", [&] { launch_pass_warp(0, ctx_, gd, ng, nullptr, nullptr, A, nullptr, bins, nullptr, nullptr, 0, 0); });
+      else timed("k_wem", [&] { launch_wem(ctx_, gd, ng, G, A, bins, 0); });
       cuda_check(cudaGetLastError(), "k_wem launch");
     });
     emit(data, kind, add);
@@ -208,11 +220,13 @@ class Engine {
     float2* drm = drm_.as<float2>((size_t)M_ * plane);
     launch_drefl_fwd(ctx_, M_, a0_, b0_, a1_, b1_, dm0, dm1, drm, 0);
     float2* bins = zero_bins();
-    int G = pick_G([&](int g) { return smem_born_fwd(ctx_, g); });
+    const bool wp = warp_path();
+    int G = wp ? warp_G() : pick_G([&](int g) { return smem_born_fwd(ctx_, g); });
     for_chunks(G, 2 * plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = store1_.as<float2>((size_t)rows * plane);
       float2* B = store2_.as<float2>((size_t)rows * plane);
-      timed("k_born_fwd", [&] { launch_born_fwd(ctx_, gd, ng, G, dm0, drm, A, B, bins, 0); });
+      if (wp) timed("k_born_fwd", [&] { launch_pass_warp(1, ctx_, gd, ng, dm0, drm, A, B, bins, nullptr, nullptr, 0, 0); });
+      else timed("k_born_fwd", [&] { launch_born_fwd(ctx_, gd, ng, G, dm0, drm, A, B, bins, 0); });
       cuda_check(cudaGetLastError(), "k_born_fwd launch");
     });
     emit(data, kind, add);
@@ -227,7 +241,8 @@ class Engine {
     float2* IS = is_.as<float2>((size_t)M_ * plane);
     cuda_check(cudaMemsetAsync(IR, 0, (size_t)M_ * plane * 8, 0), "memset");
     cuda_check(cudaMemsetAsync(IS, 0, (size_t)M_ * plane * 8, 0), "memset");
-    int G = pick_G([&](int g) { return smem_born_adj(ctx_, g); });
+    const bool wp = warp_path();
+    int G = wp ? warp_G() : pick_G([&](int g) { return smem_born_adj(ctx_, g); });
     const int compat = p_.adjoint_mode == WEM_ADJ_COMPAT ? 1 : 0;
     // per row: two stored fields; per group: two partial images
     for_chunks(G, 2 * plane * 8 + (2 * plane * 8 + G - 1) / G, [&](const Group* gd, int ng, int rows) {
@@ -235,7 +250,8 @@ class Engine {
       float2* T = store2_.as<float2>((size_t)rows * plane);
       float2* pr = part1_.as<float2>((size_t)ng * plane);
       float2* ps = part2_.as<float2>((size_t)ng * plane);
-      timed("k_born_adj", [&] { launch_born_adj(ctx_, gd, ng, G, BG, T, bins_, pr, ps, compat, 0); });
+      if (wp) timed("k_born_adj", [&] { launch_pass_warp(2, ctx_, gd, ng, nullptr, nullptr, BG, T, bins_, pr, ps, compat, 0); });
+      else timed("k_born_adj", [&] { launch_born_adj(ctx_, gd, ng, G, BG, T, bins_, pr, ps, compat, 0); });
       cuda_check(cudaGetLastError(), "k_born_adj launch");
       // chunk-local group ranges of each model slice
       std::vector<int> beg(M_ + 1, 0);
@@ -623,6 +639,12 @@ int wem_stats_get(const char* kernel, double* total_ms, long long* launches) {
     KStat& k = stat_of(kernel);
     *total_ms = k.ms;
     *launches = k.n;
+  });
+}
+int wem_set_kernel_path(int path) {
+  return guard([&] {
+    require(path >= 0 && path <= 2, "path must be 0, 1 or 2");
+    g_path = path;
   });
 }
 int wem_set_plain(int plain) {

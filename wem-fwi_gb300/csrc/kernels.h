@@ -75,6 +75,14 @@ void launch_scatter(const DevCtx& c, int f, int z, int adj, int exact, const flo
 void launch_oneway(const DevCtx& c, int f, int up, int adj, int recursive, const float2* in, float2* out,
                    int nrow, int add, int G, cudaStream_t st);
 
+// ---- warp-per-row passes (kernels_w.cu), N = 32 E with E in {8,12,16,24,32}
+bool warp_path_supported(const DevCtx& c);
+int warp_rows_per_group();
+size_t warp_smem_bytes(const DevCtx& c, int which);
+// which: 0 WEM, 1 Born forward, 2 Born adjoint (arguments as the launchers above)
+void launch_pass_warp(int which, const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm,
+                      float2* s1, float2* s2, float2* bins, float2* ir, float2* is, int compat, cudaStream_t st);
+
 // ---- helpers
 void launch_pad_model(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st);
 void launch_drefl_fwd(const DevCtx& c, int M, const float2* a0, const float2* b0, const float2* a1,

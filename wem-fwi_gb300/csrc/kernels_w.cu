@@ -1,0 +1,43 @@
+// Dispatch of the warp-per-row pass kernels (kernels_w.cuh) by row length.
+#include "kernels.h"
+
+namespace wg {
+
+template <int E>
+void launch_pass_w_e(int which, const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm,
+                     float2* s1, float2* s2, float2* bins, float2* ir, float2* is, int compat, cudaStream_t st);
+template <int E>
+size_t smem_w_e(const DevCtx& c, bool slots);
+
+int warp_rows_per_group() { return 8; }
+
+bool warp_path_supported(const DevCtx& c) {
+  if (c.N % 32 || c.ntaylor > 1) return false;
+  int E = c.N / 32;
+  return E == 8 || E == 12 || E == 16 || E == 24 || E == 32;
+}
+
+size_t warp_smem_bytes(const DevCtx& c, int which) {
+  switch (c.N / 32) {
+    case 8: return smem_w_e<8>(c, which == 2);
+    case 12: return smem_w_e<12>(c, which == 2);
+    case 16: return smem_w_e<16>(c, which == 2);
+    case 24: return smem_w_e<24>(c, which == 2);
+    case 32: return smem_w_e<32>(c, which == 2);
+    default: return 0;
+  }
+}
+
+void launch_pass_warp(int which, const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm,
+                      float2* s1, float2* s2, float2* bins, float2* ir, float2* is, int compat, cudaStream_t st) {
+  switch (c.N / 32) {
+    case 8: launch_pass_w_e<8>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st); break;
+    case 12: launch_pass_w_e<12>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st); break;
+    case 16: launch_pass_w_e<16>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st); break;
+    case 24: launch_pass_w_e<24>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st); break;
+    case 32: launch_pass_w_e<32>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st); break;
+    default: break;
+  }
+}
+
+}  // namespace wg

@@ -1,0 +1,164 @@
+// Warp-per-row register FFT for row lengths N = 32 E (sm_103a).
+//
+// Lane t of a warp holds the E points n = t + 32 j (j < E) of one row in
+// registers: the "natural layout".  A transform is a short Stockham sequence
+// whose first radix is E (a DFT held entirely in one lane's registers) and
+// whose later radices divide E, so every butterfly of a stage reads its R
+// inputs from the lane's own registers; between stages the row is
+// redistributed through a per-warp shared buffer (write scattered, read
+// natural, __syncwarp only).  The last stage of a Stockham sequence writes
+// natural order, so it needs no exchange: a transform costs (stages - 1)
+// exchanges, e.g. one for N = 1024 (32 x 32) and two for N = 768 (24 x 8 x 4).
+//
+// In-register DFTs are unrolled mixed-radix decompositions with compile-time
+// indices; their twiddles W_R^k (R | 96) come from a 96-entry table in
+// constant memory, computed in double on the host.  Inter-stage twiddles
+// W_N^(r l N/(L R)) come from an N-entry table staged in shared memory.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fft.cuh"
+
+namespace wg {
+
+// W_96^k = exp(-2 pi i k / 96); one copy per translation unit, filled by
+// that unit's launcher
+static __constant__ float2 c_w96[96];
+
+template <int R>
+__device__ __forceinline__ float2 wr(int k, bool inv) {
+  float2 w = c_w96[(k % R) * (96 / R)];
+  return inv ? make_float2(w.x, -w.y) : w;
+}
+
+// ------------------------------------------------ in-register small DFTs
+template <int R, bool INV>
+struct Dft;
+
+template <bool INV>
+struct Dft<1, INV> {
+  __device__ __forceinline__ static void run(float2*) {}
+};
+template <bool INV>
+struct Dft<2, INV> {
+  __device__ __forceinline__ static void run(float2* v) { dft2(v); }
+};
+template <bool INV>
+struct Dft<3, INV> {
+  __device__ __forceinline__ static void run(float2* v) { dft3(v, INV); }
+};
+template <bool INV>
+struct Dft<4, INV> {
+  __device__ __forceinline__ static void run(float2* v) { dft4(v, INV); }
+};
+
+// composite size: R = P M, decimation in time, P in {4, 2, 3}
+template <int R, bool INV>
+struct Dft {
+  static constexpr int P = (R % 4 == 0 && R != 8) ? 4 : ((R % 2 == 0) ? 2 : 3);
+  static constexpr int M = R / P;
+  __device__ __forceinline__ static void run(float2* v) {
+    float2 sub[P][M];
+#pragma unroll
+    for (int q = 0; q < P; ++q)
+#pragma unroll
+      for (int i = 0; i < M; ++i) sub[q][i] = v[q + P * i];
+#pragma unroll
+    for (int q = 0; q < P; ++q) Dft<M, INV>::run(sub[q]);
+#pragma unroll
+    for (int k = 0; k < M; ++k) {
+      float2 a[P];
+#pragma unroll
+      for (int q = 0; q < P; ++q) a[q] = (q * k == 0) ? sub[q][k] : c_mul(sub[q][k], wr<R>(q * k, INV));
+      Dft<P, INV>::run(a);
+#pragma unroll
+      for (int r = 0; r < P; ++r) v[k + M * r] = a[r];
+    }
+  }
+};
+
+// ------------------------------------------------ stage plans
+// radices of N = 32 E: first E, then factors of 32 that divide E
+template <int E>
+struct WPlan;
+template <>
+struct WPlan<8> {
+  static constexpr int n = 3;
+  __host__ __device__ static constexpr int r(int s) { return s == 0 ? 8 : (s == 1 ? 8 : 4); }
+};
+template <>
+struct WPlan<12> {
+  static constexpr int n = 4;
+  __host__ __device__ static constexpr int r(int s) { return s == 0 ? 12 : (s == 3 ? 2 : 4); }
+};
+template <>
+struct WPlan<16> {
+  static constexpr int n = 3;
+  __host__ __device__ static constexpr int r(int s) { return s == 2 ? 2 : 16; }
+};
+template <>
+struct WPlan<24> {
+  static constexpr int n = 3;
+  __host__ __device__ static constexpr int r(int s) { return s == 0 ? 24 : (s == 1 ? 8 : 4); }
+};
+template <>
+struct WPlan<32> {
+  static constexpr int n = 2;
+  __host__ __device__ static constexpr int r(int) { return 32; }
+};
+
+// padded index of the exchange buffer (one pad slot per 16 points keeps the
+// natural-order reads conflict-free and spreads the strided writes)
+__device__ __forceinline__ int swz(int i) { return i + (i >> 4); }
+template <int E>
+__host__ __device__ constexpr int wbuf_len() {
+  return 32 * E + (32 * E) / 16 + 2;
+}
+
+template <int E, bool INV, int S, int L>
+__device__ __forceinline__ void wfft_stage(float2 (&v)[E], float2* sb, const float2* tw, int lane) {
+  constexpr int R = WPlan<E>::r(S);
+  constexpr int M = E / R;
+  constexpr int N = 32 * E;
+  constexpr bool LAST = (S == WPlan<E>::n - 1);
+  constexpr int TWS = N / (L * R);
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    const int b = lane + 32 * m;
+    const int l = (L == 1) ? 0 : (b % L);
+    float2 a[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      float2 x = v[m + r * M];
+      if (L > 1 && r > 0) {
+        float2 w = tw[r * l * TWS];
+        x = INV ? c_mulc(x, w) : c_mul(x, w);
+      }
+      a[r] = x;
+    }
+    Dft<R, INV>::run(a);
+    if constexpr (LAST) {
+#pragma unroll
+      for (int q = 0; q < R; ++q) v[m + q * M] = a[q];
+    } else {
+      const int o = (b - l) * R + l;
+#pragma unroll
+      for (int q = 0; q < R; ++q) sb[swz(o + q * L)] = a[q];
+    }
+  }
+  if constexpr (!LAST) {
+    __syncwarp();
+#pragma unroll
+    for (int j = 0; j < E; ++j) v[j] = sb[swz(lane + 32 * j)];
+    __syncwarp();
+    wfft_stage<E, INV, S + 1, L * R>(v, sb, tw, lane);
+  }
+}
+
+// unnormalised DFT of the row held by this warp, natural layout in and out
+template <int E, bool INV>
+__device__ __forceinline__ void wfft(float2 (&v)[E], float2* sb, const float2* tw, int lane) {
+  wfft_stage<E, INV, 0, 1>(v, sb, tw, lane);
+}
+
+}  // namespace wg

@@ -30,6 +30,7 @@ _SIGS = {
     "wem_stats_get": (_i, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
     "wem_stats_reset": (_i, []),
     "wem_set_plain": (_i, [_i]),
+    "wem_set_kernel_path": (_i, [_i]),
     "wem_create": (_i, [_pp, _v, ctypes.POINTER(_h)]),
     "wem_destroy": (None, [_h]),
     "wem_get_nfreq": (_i, [_h, ctypes.POINTER(_i)]),

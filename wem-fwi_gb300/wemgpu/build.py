@@ -21,7 +21,8 @@ LIB = os.path.join(OUT_DIR, "libwemgpu.so")
 OBJ_DIR = os.path.join(OUT_DIR, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels.cu", "api.cpp", "planner.cpp"]
+SOURCES = ["kernels.cu", "kernels_w.cu", "kw_e8.cu", "kw_e12.cu", "kw_e16.cu", "kw_e24.cu", "kw_e32.cu",
+           "api.cpp", "planner.cpp"]
 
 
 def _nvcc() -> str:
@@ -56,6 +57,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        if verbose and (r.stdout or r.stderr):
+            print(r.stdout + r.stderr, file=sys.stderr)
         return obj
 
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
