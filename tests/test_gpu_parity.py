@@ -270,3 +270,15 @@ def test_warp_path_is_deterministic(gpu_lib, case):
         op.adjoint(a0, a1, d)
         outs.append((a0, a1))
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+
+
+def test_refsampler_history_exhausted(gpu_lib, oracle):
+    """nref = 1 with nz > nxg - 2: the reference's zero history runs out and
+    the as-coded partition drops points (RefSampler.cpp:63-81); the library
+    then builds the partition on the host exactly as the oracle does."""
+    from wemgpu.core import WemOp
+    p, par, wav, s, rho = small_case(nx=20, nz=24, pad=0, tap=6, ns=1)
+    d = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    WemOp(p, wav).forward(s, rho, d)
+    o = oracle.wem_forward(p, wav, s, rho, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(d, o) < TOL_OP, rel_l2(d, o)

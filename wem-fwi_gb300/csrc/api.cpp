@@ -180,16 +180,14 @@ class Engine {
 
   void set_background(const void* s2, const void* rho) {
     require(s2 && rho, "background model is NULL");
-    const size_t n = (size_t)M_ * p_.nz * p_.nx;
-    std::vector<float> hs = host_floats(s2, 2 * n), hr = host_floats(rho, 2 * n);
-    build_background(hs.data(), hr.data());
+    build_background(s2, rho);
     have_bg_ = true;
   }
 
   bool warp_path() const {
     if (g_path == 1) return false;
     bool ok = warp_path_supported(ctx_);
-    require(ok || g_path != 2, "warp-per-row kernels need N = 32 E with E in {8,12,16,24,32}");
+    require(ok || g_path != 2, "warp-per-row kernels need N = 32 E with E in {8,12,16,24,32} and ntaylor <= 1");
     return ok;
   }
 
@@ -293,7 +291,7 @@ class Engine {
   // static tables
   Buf tw_, kx_, taper_, omega_, bin_, wave_, sx_, sz_, gs_, gr_, rptr_, rid_, rxs_, ttw_;
   // background tables
-  Buf sref_, ref_, q_, sc_, rc_, a0b_, b0b_, a1b_, b1b_, ph_, fac_;
+  Buf sref_, ref_, q_, sc_, rc_, a0b_, b0b_, a1b_, b1b_, ph_, fac_, sp_, dp_;
   float2 *a0_ = nullptr, *b0_ = nullptr, *a1_ = nullptr, *b1_ = nullptr;
   // workspaces
   Buf binsbuf_, groups_, store1_, store2_, part1_, part2_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
@@ -353,49 +351,70 @@ class Engine {
     bins_ = binsbuf_.as<float2>((size_t)g.ns * g.nr * g.nt_pad);
   }
 
-  void build_background(const float* s2, const float* rho) {
-    const int nz = p_.nz, nx = p_.nx, nxg = geo_.nxg;
-    const size_t plane = (size_t)nz * nxg, mplane = (size_t)nz * nx;
-    const int nt = p_.ntaylor + 1;
-    std::vector<float2> sref((size_t)M_ * nz * p_.nref), q, sc, rc((size_t)M_ * plane), a0, b0, a1, b1;
-    std::vector<signed char> ref((size_t)M_ * plane);
-    if (p_.prop == WEM_PROP_SSF) q.resize((size_t)M_ * plane);
-    if (born_) {
-      sc.resize((size_t)M_ * nt * plane);
-      a0.resize((size_t)M_ * plane); b0.resize(a0.size()); a1.resize(a0.size()); b1.resize(a0.size());
-    }
-    for (int m = 0; m < M_; ++m) {
-      std::vector<cd> sp = pad_model(s2 + 2 * mplane * m, nz, nx, p_.pad, true);
-      std::vector<cd> dp = pad_model(rho + 2 * mplane * m, nz, nx, p_.pad, true);
-      SliceTables t = make_slice_tables(p_, sp, dp, nxg, born_);
-      auto put = [&](std::vector<float2>& dst, const std::vector<cd>& src, size_t off) {
-        for (size_t i = 0; i < src.size(); ++i)
-          dst[off + i] = make_float2((float)src[i].real(), (float)src[i].imag());
-      };
-      put(sref, t.sref, (size_t)m * nz * p_.nref);
-      std::copy(t.ref.begin(), t.ref.end(), ref.begin() + (size_t)m * plane);
-      if (!q.empty()) put(q, t.q, (size_t)m * plane);
-      put(rc, t.rc, (size_t)m * plane);
-      if (born_) {
-        put(sc, t.sc, (size_t)m * nt * plane);
-        put(a0, t.a0, (size_t)m * plane); put(b0, t.b0, (size_t)m * plane);
-        put(a1, t.a1, (size_t)m * plane); put(b1, t.b1, (size_t)m * plane);
+  // Background tables on the device: edge-padded model, RefSampler (on the
+  // host only when its sort can change the partition: nref > 1, or the
+  // as-coded history running out for nref == 1), point tables, and the
+  // per-(frequency, depth) phase-shift and split-step tables.
+  void build_background(const void* s2, const void* rho) {
+    const int nz = p_.nz, nx = p_.nx, nxg = geo_.nxg, nref = p_.nref;
+    const size_t plane = (size_t)nz * nxg, n = (size_t)M_ * nz * nx;
+    Staged ss, sr;
+    ss.in(s2, n * 8);
+    sr.in(rho, n * 8);
+    float2* sp = sp_.as<float2>((size_t)M_ * plane);
+    float2* dp = dp_.as<float2>((size_t)M_ * plane);
+    launch_pad_edge((const float2*)ss.dev, sp, M_, nz, nx, p_.pad, 0);
+    launch_pad_edge((const float2*)sr.dev, dp, M_, nz, nx, p_.pad, 0);
+    float2* dsref = sref_.as<float2>((size_t)M_ * nz * nref);
+    signed char* dref = ref_.as<signed char>((size_t)M_ * plane);
+    const bool device_refs = nref == 1 && (p_.refs_mode == WEM_REFS_NEAREST || nz <= nxg - 2);
+    if (device_refs) {
+      launch_sref(sp, dsref, M_, nz, nxg, nref, 0);
+      cuda_check(cudaMemsetAsync(dref, 0, (size_t)M_ * plane, 0), "memset");
+      std::vector<float2> h((size_t)M_ * nz * nref);
+      cuda_check(cudaMemcpy(h.data(), dsref, h.size() * 8, cudaMemcpyDeviceToHost), "D2H sref");
+      for (size_t i = 0; i < h.size(); ++i)
+        if (!(h[i].x > 0))
+          throw Fail(WEM_EINVAL, "Ref velocity " + std::to_string(h[i].x) + " at the layer " +
+                                     std::to_string((i / nref) % nz));
+    } else {
+      std::vector<float> hs = host_floats(s2, 2 * n);
+      std::vector<float2> sref((size_t)M_ * nz * nref);
+      std::vector<signed char> ref((size_t)M_ * plane);
+      for (int m = 0; m < M_; ++m) {
+        std::vector<cd> spm = pad_model(hs.data() + 2 * (size_t)m * nz * nx, nz, nx, p_.pad, true);
+        std::vector<cd> sr_m;
+        std::vector<signed char> ref_m;
+        refsampler(p_, spm, nxg, nz, sr_m, ref_m);
+        for (size_t i = 0; i < sr_m.size(); ++i)
+          sref[(size_t)m * nz * nref + i] = make_float2((float)sr_m[i].real(), (float)sr_m[i].imag());
+        std::copy(ref_m.begin(), ref_m.end(), ref.begin() + (size_t)m * plane);
       }
+      cuda_check(cudaMemcpy(dsref, sref.data(), sref.size() * 8, cudaMemcpyHostToDevice), "H2D sref");
+      cuda_check(cudaMemcpy(dref, ref.data(), ref.size(), cudaMemcpyHostToDevice), "H2D ref");
     }
-    float2* dsref = upload(sref_, sref);
-    ctx_.ref = upload(ref_, ref);
-    ctx_.rc = upload(rc_, rc);
+    ctx_.ref = dref;
+    const bool ssf = p_.prop == WEM_PROP_SSF;
+    float2* q = ssf ? q_.as<float2>((size_t)M_ * plane) : nullptr;
+    float2* rc = rc_.as<float2>((size_t)M_ * plane);
+    float2* sc = nullptr;
     if (born_) {
-      ctx_.sc = upload(sc_, sc);
-      a0_ = upload(a0b_, a0); b0_ = upload(b0b_, b0); a1_ = upload(a1b_, a1); b1_ = upload(b1b_, b1);
+      sc = sc_.as<float2>((size_t)M_ * (p_.ntaylor + 1) * plane);
+      a0_ = a0b_.as<float2>((size_t)M_ * plane);
+      b0_ = b0b_.as<float2>((size_t)M_ * plane);
+      a1_ = a1b_.as<float2>((size_t)M_ * plane);
+      b1_ = b1b_.as<float2>((size_t)M_ * plane);
     }
-    float2* ph = ph_.as<float2>((size_t)F_ * nz * p_.nref * geo_.N);
+    launch_point_tables(M_, nz, nxg, nref, p_.ntaylor, p_.eps, sp, dp, dsref, dref, q, rc, sc, a0_, b0_, a1_, b1_,
+                        0);
+    ctx_.rc = rc;
+    ctx_.sc = sc;
+    float2* ph = ph_.as<float2>((size_t)F_ * nz * nref * geo_.N);
     launch_phase_tables(ctx_, dsref, p_.eps, ph, 0);
     ctx_.ph = ph;
-    if (p_.prop == WEM_PROP_SSF) {
-      float2* dq = upload(q_, q);
+    if (ssf) {
       float2* fac = fac_.as<float2>((size_t)F_ * plane);
-      launch_fac_tables(ctx_, dq, fac, 0);
+      launch_fac_tables(ctx_, q, fac, 0);
       ctx_.fac = fac;
     } else {
       ctx_.fac = nullptr;

@@ -83,6 +83,15 @@ size_t warp_smem_bytes(const DevCtx& c, int which);
 void launch_pass_warp(int which, const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm,
                       float2* s1, float2* s2, float2* bins, float2* ir, float2* is, int compat, cudaStream_t st);
 
+// ---- background tables on the device (tables.cu)
+void launch_pad_edge(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st);
+void launch_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref, cudaStream_t st);
+// q (SSF split step, may be null), rc, and for the Born operators sc and the
+// dReflect pairs (null to skip) of every padded point
+void launch_point_tables(int M, int nz, int nxg, int nref, int ntaylor, float eps, const float2* sp,
+                         const float2* dp, const float2* sref, const signed char* ref, float2* q, float2* rc,
+                         float2* sc, float2* a0, float2* b0, float2* a1, float2* b1, cudaStream_t st);
+
 // ---- helpers
 void launch_pad_model(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st);
 void launch_drefl_fwd(const DevCtx& c, int M, const float2* a0, const float2* b0, const float2* a1,

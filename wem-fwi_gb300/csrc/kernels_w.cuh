@@ -33,12 +33,22 @@ __device__ __forceinline__ bool in_grid(const DevCtx& c, int lane, int j, int& x
   return x >= 0 && x < c.nxg;
 }
 
+// clamped grid index of register j: loads through it are issued without a
+// branch (so a lane's E loads are all in flight together) and the result is
+// selected with `in` afterwards
+__device__ __forceinline__ int xclamp(const DevCtx& c, int lane, int j, bool& in) {
+  const int x = lane + 32 * j - c.tap;
+  in = (unsigned)x < (unsigned)c.nxg;
+  return in ? x : 0;
+}
+
 template <int E>
 __device__ __forceinline__ void w_load(const DevCtx& c, int lane, const float2* row, float2 (&v)[E]) {
 #pragma unroll
   for (int j = 0; j < E; ++j) {
-    int x;
-    v[j] = in_grid<E>(c, lane, j, x) ? row[x] : make_float2(0.f, 0.f);
+    bool in;
+    const float2 a = row[xclamp(c, lane, j, in)];
+    v[j] = in ? a : make_float2(0.f, 0.f);
   }
 }
 
@@ -51,7 +61,9 @@ __device__ __forceinline__ void w_store(const DevCtx& c, int lane, float2* row, 
   }
 }
 
-// o = P_z u  (SSF.cpp:8-32, PSPI.cpp:8-29); u and o may be the same array
+// o = P_z u  (SSF.cpp:8-32, PSPI.cpp:8-29); u and o may be the same array.
+// SSF: the split-step table is zero where a point has no reference, so the
+// reference index is only read for PSPI with several references.
 template <int E>
 __device__ void w_step_fwd(const WRow& w, int f, int z, const float2 (&u)[E], float2 (&o)[E]) {
   const DevCtx& c = w.c;
@@ -68,12 +80,22 @@ __device__ void w_step_fwd(const WRow& w, int f, int z, const float2 (&u)[E], fl
 #pragma unroll
     for (int j = 0; j < E; ++j) X[j] = c_mul(X[j], ph[w.lane + 32 * j]);
     wfft<E, true>(X, w.sb, w.tw, w.lane);
+    if (fac) {
 #pragma unroll
-    for (int j = 0; j < E; ++j) {
-      int x;
-      float2 v = make_float2(0.f, 0.f);
-      if (in_grid<E>(c, w.lane, j, x) && ref[x] == 0) v = fac ? c_mul(X[j], fac[x]) : c_scale(X[j], c.taperN[x]);
-      o[j] = v;
+      for (int j = 0; j < E; ++j) {
+        bool in;
+        const float2 fx = fac[xclamp(c, w.lane, j, in)];
+        o[j] = in ? c_mul(X[j], fx) : make_float2(0.f, 0.f);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        bool in;
+        const int x = xclamp(c, w.lane, j, in);
+        const float tp = c.taperN[x];
+        const int r = ref[x];
+        o[j] = (in && r == 0) ? c_scale(X[j], tp) : make_float2(0.f, 0.f);
+      }
     }
   } else {
 #pragma unroll
@@ -86,9 +108,11 @@ __device__ void w_step_fwd(const WRow& w, int f, int z, const float2 (&u)[E], fl
       wfft<E, true>(Y, w.sb, w.tw, w.lane);
 #pragma unroll
       for (int j = 0; j < E; ++j) {
-        int x;
-        if (in_grid<E>(c, w.lane, j, x) && ref[x] == jr)
-          o[j] = fac ? c_mul(Y[j], fac[x]) : c_scale(Y[j], c.taperN[x]);
+        bool in;
+        const int x = xclamp(c, w.lane, j, in);
+        const int r = ref[x];
+        const float2 v = fac ? c_mul(Y[j], fac[x]) : c_scale(Y[j], c.taperN[x]);
+        if (in && r == jr) o[j] = v;
       }
     }
   }
@@ -107,10 +131,16 @@ __device__ void w_step_adj(const WRow& w, int f, int z, const float2 (&d)[E], fl
   if (c.nref == 1) {
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      int x;
-      float2 v = make_float2(0.f, 0.f);
-      if (in_grid<E>(c, w.lane, j, x) && ref[x] == 0) v = fac ? c_mulc(d[j], fac[x]) : c_scale(d[j], c.taperN[x]);
-      A[j] = v;
+      bool in;
+      const int x = xclamp(c, w.lane, j, in);
+      if (fac) {
+        const float2 fx = fac[x];
+        A[j] = in ? c_mulc(d[j], fx) : make_float2(0.f, 0.f);
+      } else {
+        const float tp = c.taperN[x];
+        const int r = ref[x];
+        A[j] = (in && r == 0) ? c_scale(d[j], tp) : make_float2(0.f, 0.f);
+      }
     }
     wfft<E, false>(A, w.sb, w.tw, w.lane);
 #pragma unroll
@@ -122,11 +152,11 @@ __device__ void w_step_adj(const WRow& w, int f, int z, const float2 (&d)[E], fl
     for (int jr = 0; jr < c.nref; ++jr) {
 #pragma unroll
       for (int j = 0; j < E; ++j) {
-        int x;
-        float2 v = make_float2(0.f, 0.f);
-        if (in_grid<E>(c, w.lane, j, x) && ref[x] == jr)
-          v = fac ? c_mulc(d[j], fac[x]) : c_scale(d[j], c.taperN[x]);
-        A[j] = v;
+        bool in;
+        const int x = xclamp(c, w.lane, j, in);
+        const int r = ref[x];
+        const float2 v = fac ? c_mulc(d[j], fac[x]) : c_scale(d[j], c.taperN[x]);
+        A[j] = (in && r == jr) ? v : make_float2(0.f, 0.f);
       }
       wfft<E, false>(A, w.sb, w.tw, w.lane);
       const float2* pj = ph + (size_t)jr * N;
@@ -139,8 +169,9 @@ __device__ void w_step_adj(const WRow& w, int f, int z, const float2 (&d)[E], fl
   wfft<E, true>(A, w.sb, w.tw, w.lane);
 #pragma unroll
   for (int j = 0; j < E; ++j) {
-    int x;
-    o[j] = in_grid<E>(c, w.lane, j, x) ? A[j] : make_float2(0.f, 0.f);
+    bool in;
+    xclamp(c, w.lane, j, in);
+    o[j] = in ? A[j] : make_float2(0.f, 0.f);
   }
 }
 
@@ -162,13 +193,13 @@ __device__ void w_scatter(const WRow& w, int f, int z, int mode, const float2 (&
   float2 X[E];
 #pragma unroll
   for (int j = 0; j < E; ++j) {
-    int x;
-    const bool in = in_grid<E>(c, w.lane, j, x);
+    bool in;
+    const int x = xclamp(c, w.lane, j, in);
+    const float2 k0 = c0[x];
+    const float2 k1 = t1 ? c1[x] : make_float2(0.f, 0.f);
     // transform input: u, or conj(c_1) u for the exact adjoint
-    X[j] = (mode == 2 && in && t1) ? c_mulc(u[j], c1[x]) : u[j];
-    float2 v = make_float2(0.f, 0.f);
-    if (in) v = c_mul(iw, mode == 0 ? c_mul(c0[x], u[j]) : c_mulc(u[j], c0[x]));
-    o[j] = v;
+    X[j] = (mode == 2 && t1) ? (in ? c_mulc(u[j], k1) : make_float2(0.f, 0.f)) : u[j];
+    o[j] = in ? c_mul(iw, mode == 0 ? c_mul(k0, u[j]) : c_mulc(u[j], k0)) : make_float2(0.f, 0.f);
   }
   if (!t1) return;
   wfft<E, false>(X, w.sb, w.tw, w.lane);
@@ -180,13 +211,13 @@ __device__ void w_scatter(const WRow& w, int f, int z, int mode, const float2 (&
   wfft<E, true>(X, w.sb, w.tw, w.lane);
 #pragma unroll
   for (int j = 0; j < E; ++j) {
-    int x;
-    if (in_grid<E>(c, w.lane, j, x)) {
-      float2 y = X[j];
-      if (mode == 0) y = c_mul(c1[x], y);
-      else if (mode == 1) y = c_mulc(y, c1[x]);
-      o[j] = c_add(o[j], c_mul(iw, y));
-    }
+    bool in;
+    const int x = xclamp(c, w.lane, j, in);
+    const float2 k1 = c1[x];
+    float2 y = X[j];
+    if (mode == 0) y = c_mul(k1, y);
+    else if (mode == 1) y = c_mulc(y, k1);
+    if (in) o[j] = c_add(o[j], c_mul(iw, y));
   }
 }
 
@@ -288,8 +319,10 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_wem(DevCtx c, const Group* grou
     const float2* rc = c.rc + ((size_t)m * nz + z) * nxg;
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      int x;
-      if (in_grid<E>(c, lane, j, x)) A[(size_t)z * nxg + x] = c_mul(rc[x], W[j]);
+      bool in;
+      const int x = xclamp(c, lane, j, in);
+      const float2 r = rc[x];
+      if (in) A[(size_t)z * nxg + x] = c_mul(r, W[j]);
     }
     if (z == nz - 1) break;
     w_step_fwd<E>(w, f, z, W, W);
@@ -303,8 +336,9 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_wem(DevCtx c, const Group* grou
     const float2* a = A + (size_t)(z - 1) * nxg;
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      int x;
-      if (in_grid<E>(c, lane, j, x)) W[j] = c_add(W[j], a[x]);
+      bool in;
+      const float2 v = a[xclamp(c, lane, j, in)];
+      if (in) W[j] = c_add(W[j], v);
     }
   }
 }
@@ -337,12 +371,13 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, const Group*
     const float2 *rc = c.rc + zo, *dr = drm + zo, *dmz = dm + zo;
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      int x;
-      t[j] = make_float2(0.f, 0.f);
-      if (in_grid<E>(c, lane, j, x)) {
-        A[(size_t)z * nxg + x] = c_mul(rc[x], bg[j]);
-        B[(size_t)z * nxg + x] = c_add(c_mul(bg[j], dr[x]), c_mul(rc[x], sd[j]));
-        t[j] = c_mul(bg[j], dmz[x]);
+      bool in;
+      const int x = xclamp(c, lane, j, in);
+      const float2 r = rc[x], d = dr[x], q = dmz[x];
+      t[j] = in ? c_mul(bg[j], q) : make_float2(0.f, 0.f);
+      if (in) {
+        A[(size_t)z * nxg + x] = c_mul(r, bg[j]);
+        B[(size_t)z * nxg + x] = c_add(c_mul(bg[j], d), c_mul(r, sd[j]));
       }
     }
     if (z == nz - 1) break;
@@ -361,8 +396,9 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, const Group*
     const float2* dmz = dm + ((size_t)m * nz + z) * nxg;
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      int x;
-      t[j] = in_grid<E>(c, lane, j, x) ? c_mul(bg[j], dmz[x]) : make_float2(0.f, 0.f);
+      bool in;
+      const float2 q = dmz[xclamp(c, lane, j, in)];
+      t[j] = in ? c_mul(bg[j], q) : make_float2(0.f, 0.f);
     }
     w_scatter<E>(w, f, z, 0, t, t);
 #pragma unroll
@@ -373,10 +409,12 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, const Group*
     const float2* b = B + (size_t)(z - 1) * nxg;
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      int x;
-      if (in_grid<E>(c, lane, j, x)) {
-        bg[j] = c_add(bg[j], a[x]);
-        sd[j] = c_add(sd[j], b[x]);
+      bool in;
+      const int x = xclamp(c, lane, j, in);
+      const float2 va = a[x], vb = b[x];
+      if (in) {
+        bg[j] = c_add(bg[j], va);
+        sd[j] = c_add(sd[j], vb);
       }
     }
   }
@@ -458,13 +496,10 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, const Group*
     w_inject_rec<E>(w, t, s, bin, nz - 1, bins);  // wu[nz-1]
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      int x;
-      if (in_grid<E>(c, lane, j, x)) {
-        bu[j] = c_mul(rc[x], bu[j]);
-        wd[j] = c_mulc(t[j], rc[x]);
-      } else {
-        bu[j] = wd[j] = zero;
-      }
+      bool in;
+      const float2 r = rc[xclamp(c, lane, j, in)];
+      bu[j] = in ? c_mul(r, bu[j]) : zero;
+      wd[j] = in ? c_mulc(t[j], r) : zero;
     }
     w_inject_rec<E>(w, wd, s, bin, nz - 1, bins);
   }
@@ -497,24 +532,29 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, const Group*
     const float2* rc = c.rc + ((size_t)m * nz + z - 1) * nxg;
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      int x;
-      if (in_grid<E>(c, lane, j, x)) slot[x] = c_mulc(t[j], bgp[x]);
+      bool in;
+      const int x = xclamp(c, lane, j, in);
+      const float2 b = bgp[x];
+      if (in) slot[x] = c_mulc(t[j], b);
     }
     // wd[z-1] = q + rec + conj(R) (T[z-1] + rec)
     w_load<E>(c, lane, tp, t);
     w_inject_rec<E>(w, t, s, bin, z - 1, bins);
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      int x;
-      if (in_grid<E>(c, lane, j, x)) wd[j] = c_add(wd[j], c_mulc(t[j], rc[x]));
+      bool in;
+      const float2 r = rc[xclamp(c, lane, j, in)];
+      if (in) wd[j] = c_add(wd[j], c_mulc(t[j], r));
     }
     w_inject_rec<E>(w, wd, s, bin, z - 1, bins);
     // bu[z-1] = P_z bu + R[z-1] bg[z-1]
     w_step_fwd<E>(w, f, z, bu, bu);
 #pragma unroll
     for (int j = 0; j < E; ++j) {
-      int x;
-      if (in_grid<E>(c, lane, j, x)) bu[j] = c_add(bu[j], c_mul(rc[x], bgp[x]));
+      bool in;
+      const int x = xclamp(c, lane, j, in);
+      const float2 r = rc[x], b = bgp[x];
+      if (in) bu[j] = c_add(bu[j], c_mul(r, b));
     }
   }
 }

@@ -177,8 +177,8 @@ std::vector<double> taper(int nxg, int pad) {
 // reference's member array does; the one deviation is that the scans stop
 // at nx where the reference reads past the end (possible only for nref == 1
 // once nz >= nx - 1).
-static void refsampler(const wem_params& p, const std::vector<cd>& s, int nx, int nz, std::vector<cd>& sref,
-                       std::vector<signed char>& ref) {
+void refsampler(const wem_params& p, const std::vector<cd>& s, int nx, int nz, std::vector<cd>& sref,
+                std::vector<signed char>& ref) {
   const int nref = p.nref;
   sref.assign((size_t)nz * nref, 0);
   ref.assign((size_t)nz * nx, -1);

@@ -57,6 +57,11 @@ struct SliceTables {
 SliceTables make_slice_tables(const wem_params& p, const std::vector<cd>& sp, const std::vector<cd>& dp,
                               int nxg, bool need_born);
 
+// RefSampler of one padded slowness [nz][nx]: reference slownesses [nz][nref]
+// and the reference index of every point [nz][nx] (-1 none)
+void refsampler(const wem_params& p, const std::vector<cd>& s, int nx, int nz, std::vector<cd>& sref,
+                std::vector<signed char>& ref);
+
 // edge- or zero-pad [nz][nx] complex floats to [nz][nx+2pad] doubles
 std::vector<cd> pad_model(const float* m, int nz, int nx, int pad, bool extend);
 

@@ -1,0 +1,140 @@
+// Background tables built on the GPU, in double precision: the per-task
+// set-up the reference repeats for every shot (propagator/src/wem_prop.cpp:
+// 26-41, born_prop.cpp:36-58), computed once per background for all rows.
+#include <cmath>
+
+#include "kernels.h"
+
+namespace wg {
+namespace {
+
+struct cdd {
+  double x, y;
+};
+__device__ __forceinline__ cdd mk(double x, double y) { return cdd{x, y}; }
+__device__ __forceinline__ cdd mk(float2 v) { return cdd{(double)v.x, (double)v.y}; }
+__device__ __forceinline__ cdd add(cdd a, cdd b) { return mk(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ cdd sub(cdd a, cdd b) { return mk(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ cdd mul(cdd a, cdd b) { return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ cdd dvd(cdd a, cdd b) {
+  double d = b.x * b.x + b.y * b.y;
+  return mk((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+// principal square root
+__device__ __forceinline__ cdd csqrt(cdd a) {
+  double r = hypot(a.x, a.y);
+  double re = sqrt(fmax(0.5 * (r + a.x), 0.0));
+  double im = sqrt(fmax(0.5 * (r - a.x), 0.0));
+  return mk(re, a.y < 0 ? -im : im);
+}
+// principal power a^p for real p: |a|^p exp(i p arg a)
+__device__ __forceinline__ cdd cpow(cdd a, double p) {
+  double r = hypot(a.x, a.y), t = atan2(a.y, a.x);
+  double m = exp(p * log(r));
+  double s, c;
+  sincos(p * t, &s, &c);
+  return mk(m * c, m * s);
+}
+__device__ __forceinline__ float2 f2(cdd a) { return make_float2((float)a.x, (float)a.y); }
+
+// edge-extended pad along x (operator/src/Pad.h:77-96, extend = true)
+__global__ void k_pad_edge(const float2* in, float2* out, int M, int nz, int nx, int pad) {
+  const int nxg = nx + 2 * pad;
+  const size_t total = (size_t)M * nz * nxg;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    int x = (int)(i % nxg) - pad;
+    size_t rz = i / nxg;
+    x = x < 0 ? 0 : (x >= nx ? nx - 1 : x);
+    out[i] = in[rz * nx + x];
+  }
+}
+
+// reference slownesses sampled at x = nxg/(2 nref) + j nxg/nref (RefSampler.cpp:28-39)
+__global__ void k_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref) {
+  const size_t total = (size_t)M * nz * nref;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    int j = (int)(i % nref);
+    size_t mz = i / nref;
+    int off = nxg / (2 * nref) + j * nxg / nref;
+    sref[i] = sp[mz * nxg + off];
+  }
+}
+
+// split step q (SplitStep.cpp:12-13), Reflect (Reflect.h:19-26), Scatter
+// coefficients (Scatter.cpp:77-86, Scatter.h:36) and dReflect pairs
+// (dReflect.h:18-27, 40-47) of every padded point
+__global__ void k_point_tables(int M, int nz, int nxg, int nref, int nt, double eps, const float2* sp,
+                               const float2* dp, const float2* sref, const signed char* ref, float2* q,
+                               float2* rc, float2* sc, float2* a0, float2* b0, float2* a1, float2* b1) {
+  const size_t plane = (size_t)nz * nxg;
+  const size_t total = (size_t)M * plane;
+  const double coef[5] = {1., 1. / 2., 3. / 8., 5. / 16., 35. / 128.};
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const int m = (int)(i / plane);
+    const size_t p = i - (size_t)m * plane;
+    const int z = (int)(p / nxg);
+    const cdd s = mk(sp[i]), d = mk(dp[i]);
+    if (q) {
+      int j = ref[i];
+      cdd v = mk(0, 0);
+      if (j >= 0) {
+        cdd sr = mk(sref[((size_t)m * nz + z) * nref + j]);
+        v = dvd(sub(s, sr), csqrt(sr));
+      }
+      q[i] = f2(v);
+    }
+    cdd r = mk(0, 0), va0 = r, vb0 = r, va1 = r, vb1 = r;
+    if (z >= 1) {
+      const cdd su = mk(sp[i - nxg]), du = mk(dp[i - nxg]);
+      const cdd u = mul(d, csqrt(su)), w = mul(du, csqrt(s));
+      r = dvd(sub(u, w), add(u, w));
+      if (sc) {
+        cdd v = cpow(add(u, w), -2.0);
+        cdd s1s2 = dvd(mul(du, d), v);
+        cdd r1r2 = dvd(mul(mk(2, 0), mul(su, s)), v);
+        cdd cc = csqrt(dvd(s, su));
+        va0 = mul(cc, s1s2);
+        vb0 = mul(dvd(mk(1, 0), cc), s1s2);
+        va1 = mul(du, r1r2);
+        vb1 = mul(d, r1r2);
+      }
+    }
+    rc[i] = f2(r);
+    if (sc) {
+      a0[i] = f2(va0);
+      b0[i] = f2(vb0);
+      a1[i] = f2(va1);
+      b1[i] = f2(vb1);
+      const cdd base = mk(s.x - eps * s.x, s.y);
+      for (int it = 0; it < nt; ++it)
+        sc[((size_t)m * nt + it) * plane + p] = f2(mul(mk(coef[it], 0), cpow(base, -0.5 - it)));
+    }
+  }
+}
+
+int grid_of(size_t n) {
+  size_t b = (n + 255) / 256;
+  return (int)(b < 152 * 32 ? (b ? b : 1) : 152 * 32);
+}
+
+}  // namespace
+
+void launch_pad_edge(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st) {
+  size_t n = (size_t)M * nz * (nx + 2 * pad);
+  k_pad_edge<<<grid_of(n), 256, 0, st>>>(in, out, M, nz, nx, pad);
+}
+
+void launch_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref, cudaStream_t st) {
+  size_t n = (size_t)M * nz * nref;
+  k_sref<<<grid_of(n), 256, 0, st>>>(sp, sref, M, nz, nxg, nref);
+}
+
+void launch_point_tables(int M, int nz, int nxg, int nref, int ntaylor, float eps, const float2* sp,
+                         const float2* dp, const float2* sref, const signed char* ref, float2* q, float2* rc,
+                         float2* sc, float2* a0, float2* b0, float2* a1, float2* b1, cudaStream_t st) {
+  size_t n = (size_t)M * nz * nxg;
+  k_point_tables<<<grid_of(n), 256, 0, st>>>(M, nz, nxg, nref, ntaylor + 1, (double)eps, sp, dp, sref, ref, q, rc,
+                                             sc, a0, b0, a1, b1);
+}
+
+}  // namespace wg
