@@ -216,6 +216,7 @@ def test_ext_born(gpu_lib, oracle, mode):
 WARP_CASES = {
     "n256": dict(nx=240, pad=4, tap=4, prop="ssf", nref=1),
     "n384": dict(nx=376, pad=0, tap=4, prop="pspi", nref=2),
+    "n512": dict(nx=504, pad=4, tap=0, prop="pspi", nref=3),
     "n768": dict(nx=752, pad=4, tap=4, prop="ssf", nref=1),
     "n1024": dict(nx=1016, pad=0, tap=4, prop="pspi", nref=2),
 }
