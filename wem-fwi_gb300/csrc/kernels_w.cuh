@@ -50,6 +50,10 @@ __device__ __forceinline__ void cta_copy(void* dst, const void* src, int bytes) 
   for (int i = threadIdx.x * 16; i < bytes; i += blockDim.x * 16)
     cp16(static_cast<char*>(dst) + i, static_cast<const char*>(src) + i);
 }
+// bring a row into L2 ahead of its loads (bulk prefetch; bytes multiple of 16)
+__device__ __forceinline__ void l2_prefetch(const void* src, int bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(src), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void warp_copy(void* dst, const void* src, int bytes, int lane) {
   for (int i = lane * 16; i < bytes; i += 32 * 16)
     cp16(static_cast<char*>(dst) + i, static_cast<const char*>(src) + i);
@@ -578,6 +582,10 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, SlotLayout L
     if (!act) continue;
     w_record<E>(w, sd, s, bin, z, bins);
     if (z == 0) break;
+    if (lane == 0 && z >= 2) {
+      l2_prefetch(A + (size_t)(z - 2) * nxg, nxg * 8);
+      l2_prefetch(B + (size_t)(z - 2) * nxg, nxg * 8);
+    }
     const Tabs T = ring.tabs(z);
 #pragma unroll
     for (int j = 0; j < E; ++j) {
@@ -688,6 +696,10 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
   cp_commit();
   ring.issue(nz - 2);
   cp_commit();
+  if (act && lane == 0) {
+    l2_prefetch(SBG + (size_t)(nz - 2) * nxg, nxg * 8);
+    l2_prefetch(ST + (size_t)(nz - 2) * nxg, nxg * 8);
+  }
 #pragma unroll
   for (int j = 0; j < E; ++j) {
     bool in;
@@ -730,6 +742,10 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
     __syncthreads();
     if (z == 0) break;
     if (!act) continue;  // the slot of an idle warp stays zero
+    if (lane == 0 && z >= 2) {
+      l2_prefetch(SBG + (size_t)(z - 2) * nxg, nxg * 8);
+      l2_prefetch(ST + (size_t)(z - 2) * nxg, nxg * 8);
+    }
     const Tabs Tz = ring.tabs(z), Tp = ring.tabs(z - 1);
     // q = P^H_{z-1} wd;  LinDown^H: conj(bg[z-1]) Sc^H_{z-1} q
     w_step_adj<E>(w, Tp, wd, wd);  // wd holds q
