@@ -220,6 +220,29 @@ int wemop_scatter(wemop_handle* h, int iz, float freq, int adj,
  * Replaces RefSampler::getRefSlow / getRefLoc (RefSampler.h:19-20). */
 int wemop_refsampler(wemop_handle* h, void* sref, int* refidx);
 
+/* One SSF/PSPI depth step that allocates no memory (no counterpart in the
+ * reference).  It exists for callers that cannot call cudaMalloc while they
+ * run: code that owns all device memory up front (a fixed arena or memory
+ * pool, a real-time loop that must not touch the allocator) or whose
+ * allocator is unavailable at that point.  Unlike wemop_onestep it needs no
+ * handle: the caller passes the depth's inputs and the output, all in
+ * device memory, and the per-call tables live in a 1 MiB device array that
+ * the library holds on every GPU that loads it, until the process exits.
+ *   slow_row  padded slowness^2 of the depth, complex [nxg]
+ *   sref      reference slownesses of the depth, complex [nref]
+ *   refidx    reference of each point [nxg] (-1: none), e.g. one row of
+ *             wemop_refsampler's table
+ *   in, out   complex [nrow][nxg]; adj and add as wemop_onestep
+ * Limits: N = nxg + 2 tap <= 4096 and nref <= 16 (WEM_EINVAL otherwise).
+ * Every call reuses the same array, so calls that overlap on the GPU race:
+ * serialise them.  The first call on a device looks the array up with
+ * cudaGetSymbolAddress: make it before any stream capture.  The work is
+ * queued on `stream` (a cudaStream_t, NULL for the default stream) and the
+ * call returns without waiting for it. */
+int wemop_onestep_noalloc(const wem_params* p, const void* slow_row, const void* sref,
+                          const signed char* refidx, int nxg, float freq, int adj,
+                          const void* in, void* out, int nrow, int add, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -622,6 +622,10 @@ int guard(Fn fn) {
 }
 
 }  // namespace
+
+// error text of a failed call on this thread (also used by noalloc.cu)
+void set_last_error(const char* msg) { g_error = msg; }
+
 }  // namespace wg
 
 using namespace wg;

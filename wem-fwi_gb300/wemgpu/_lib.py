@@ -54,6 +54,7 @@ _SIGS = {
     "wemop_oneway": (_i, [_h, _i, _f, _i, _v, _v, _i, _i]),
     "wemop_scatter": (_i, [_h, _i, _f, _i, _v, _v, _i, _i]),
     "wemop_refsampler": (_i, [_h, _v, _v]),
+    "wemop_onestep_noalloc": (_i, [_pp, _v, _v, _v, _i, _f, _i, _v, _v, _i, _i, _v]),
 }
 
 EXPORTED = tuple(_SIGS)

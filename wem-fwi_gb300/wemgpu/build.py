@@ -22,7 +22,7 @@ OBJ_DIR = os.path.join(OUT_DIR, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["kernels.cu", "kernels_w.cu", "tables.cu", "kw_e8.cu", "kw_e12.cu", "kw_e16.cu", "kw_e24.cu", "kw_e32.cu",
-           "api.cpp", "planner.cpp"]
+           "noalloc.cu", "api.cpp", "planner.cpp"]
 
 
 def _nvcc() -> str:
