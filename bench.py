@@ -113,12 +113,22 @@ def workload(small=False):
     return cfg
 
 
+# DRAM bytes (read + write) per (row, depth) of the pass kernels, from ncu
+# captures of the reduced case (8 shots x 21 frequencies, nz 300, N 768;
+# profiles/kw_born_adj_e24_c3_small.md): the traffic of a launch scales with
+# the rows it carries, so a full launch is this figure x rows x depths.
+TRAFFIC_PER_ROW_DEPTH = {
+    "k_born_adj": (711913728 + 707227904) / (168 * 300),
+}
+
+
 def row_steps(p, nfreq):
     return (PASSES_WEM + PASSES_BORN_ADJ) * p.ns * nfreq * (p.nz - 1)
 
 
 def algorithmic_bytes(kernel, p, nfreq, G):
-    """HBM bytes a launch must move (roofline section)."""
+    """HBM bytes a launch must move: each row's wavefield read and written once per
+    depth, plus the per-(frequency, depth) phase and split-step tables."""
     nxg = p.nx + 2 * p.pad
     N = nxg + 2 * p.tap
     rows = p.ns * nfreq
@@ -175,6 +185,7 @@ def run_gpu(args, rank, world):
     lib.wem_stats_reset()
     lib.wem_stats_enable(1)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n_launch0 = _lib.launch_count()
     with Clocks(dev.index) as clk:
         torch.cuda.synchronize()
         ev0.record()
@@ -182,6 +193,7 @@ def run_gpu(args, rank, world):
             step()
         ev1.record()
         torch.cuda.synchronize()
+    gpu_launches = _lib.launch_count() - n_launch0
     lib.wem_stats_enable(0)
     ms = ev0.elapsed_time(ev1)
     if world > 1:
@@ -201,9 +213,9 @@ def run_gpu(args, rank, world):
     algo = algorithmic_bytes(top, p, nf, G)
     peak, peak_src = peaks()
     achieved = algo / (top_ms / top_n / 1e3) / 1e9
-    launches = sum(v[1] for v in kstats.values())
-    # other kernels (tables, reductions, transforms) per step: counted from the pass structure
-    gpu_launches = int(launches + args.steps * 9)
+    traffic = None
+    if top in TRAFFIC_PER_ROW_DEPTH:
+        traffic = TRAFFIC_PER_ROW_DEPTH[top] * p.ns * nf * p.nz
 
     # end to end through the C ABI with host buffers
     s0h, rhoh = cfg["slow"], cfg["rho"]
@@ -274,7 +286,7 @@ def run_gpu(args, rank, world):
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
-                     "algorithmic_bytes": algo, "ms_per_launch": top_ms / top_n, "traffic": None},
+                     "algorithmic_bytes": algo, "ms_per_launch": top_ms / top_n, "traffic": traffic},
         "kernels": {k: {"ms": v[0] / args.steps, "launches": v[1] // args.steps} for k, v in kstats.items()},
         "gpu_launches": gpu_launches,
         "plain_gpu": plain,

@@ -116,6 +116,9 @@ const char* wem_version(void);
 int wem_stats_enable(int on);
 int wem_stats_get(const char* kernel, double* total_ms, long long* launches);
 int wem_stats_reset(void);
+/* Number of kernel launches the library has made in this process (all
+ * kernels, every entry point); never reset. */
+long long wem_launch_count(void);
 
 /* Launch shape (no counterpart in the reference: measurement support).
  * plain = 1 runs every (shot, frequency) row as its own kernel launch, one

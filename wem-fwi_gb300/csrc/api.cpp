@@ -678,6 +678,7 @@ int wem_stats_reset(void) {
   g_stats.clear();
   return WEM_OK;
 }
+long long wem_launch_count(void) { return launch_count(); }
 const char* wem_version(void) { return "wemgpu 0.1 (sm_103a)"; }
 
 int wem_count_freqs(const wem_params* p, const float* wavelet, int* nfreq) {

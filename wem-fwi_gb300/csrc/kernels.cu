@@ -6,6 +6,7 @@
 // (propagator/src/wem_prop.cpp:52-74, born_prop.cpp:75-113, 178-216); the
 // Born passes here use the linearity of the one-way operators to merge the
 // reference's seven one-way sweeps per row into two (see the pass comments).
+#include <atomic>
 #include <cmath>
 
 #include "fft.cuh"
@@ -839,6 +840,10 @@ size_t al(size_t n) { return (n + 1) & ~size_t(1); }
 
 }  // namespace
 
+static std::atomic<long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
 int max_smem_per_block() {
   int dev = 0, v = 0;
   cudaGetDevice(&dev);
@@ -865,11 +870,13 @@ size_t smem_rows(const DevCtx& c, int G) { return 8 * (al(c.N) + fft_bufs(c, G, 
 void launch_phase_tables(const DevCtx& c, const float2* sref, float eps, float2* ph, cudaStream_t st) {
   size_t n = (size_t)c.nfreq * c.nz * c.nref * c.N;
   k_phase<<<grid_for(n), 256, 0, st>>>(c, sref, eps, ph);
+  note_launch();
 }
 
 void launch_fac_tables(const DevCtx& c, const float2* q, float2* fac, cudaStream_t st) {
   size_t n = (size_t)c.nfreq * c.nz * c.nxg;
   k_fac<<<grid_for(n), 256, 0, st>>>(c, q, fac);
+  note_launch();
 }
 
 void launch_wem(const DevCtx& c, const Group* groups, int ngroups, int G, float2* store, float2* bins,
@@ -877,6 +884,7 @@ void launch_wem(const DevCtx& c, const Group* groups, int ngroups, int G, float2
   size_t sm = smem_wem(c, G);
   set_smem(k_wem, sm);
   k_wem<<<ngroups, kThreads, sm, st>>>(c, groups, G, store, bins);
+  note_launch();
 }
 
 void launch_born_fwd(const DevCtx& c, const Group* groups, int ngroups, int G, const float2* dm,
@@ -884,6 +892,7 @@ void launch_born_fwd(const DevCtx& c, const Group* groups, int ngroups, int G, c
   size_t sm = smem_born_fwd(c, G);
   set_smem(k_born_fwd, sm);
   k_born_fwd<<<ngroups, kThreads, sm, st>>>(c, groups, G, dm, drm, storeA, storeB, bins);
+  note_launch();
 }
 
 void launch_born_adj(const DevCtx& c, const Group* groups, int ngroups, int G, float2* storeBG, float2* storeT,
@@ -891,6 +900,7 @@ void launch_born_adj(const DevCtx& c, const Group* groups, int ngroups, int G, f
   size_t sm = smem_born_adj(c, G);
   set_smem(k_born_adj, sm);
   k_born_adj<<<ngroups, kThreads, sm, st>>>(c, groups, G, storeBG, storeT, bins, imgR, imgS, compat);
+  note_launch();
 }
 
 void launch_onestep(const DevCtx& c, int f, int z, int adj, const float2* in, float2* out, int nrow, int add,
@@ -898,6 +908,7 @@ void launch_onestep(const DevCtx& c, int f, int z, int adj, const float2* in, fl
   size_t sm = smem_rows(c, G);
   set_smem(k_onestep, sm);
   k_onestep<<<(nrow + G - 1) / G, kThreads, sm, st>>>(c, f, z, adj, in, out, nrow, add, G);
+  note_launch();
 }
 
 void launch_scatter(const DevCtx& c, int f, int z, int adj, int exact, const float2* in, float2* out, int nrow,
@@ -906,6 +917,7 @@ void launch_scatter(const DevCtx& c, int f, int z, int adj, int exact, const flo
   set_smem(k_scatter, sm);
   int mode = adj ? (exact ? 2 : 1) : 0;
   k_scatter<<<(nrow + G - 1) / G, kThreads, sm, st>>>(c, f, z, mode, in, out, nrow, add, G);
+  note_launch();
 }
 
 void launch_oneway(const DevCtx& c, int f, int up, int adj, int recursive, const float2* in, float2* out,
@@ -913,23 +925,27 @@ void launch_oneway(const DevCtx& c, int f, int up, int adj, int recursive, const
   size_t sm = smem_rows(c, G);
   set_smem(k_oneway, sm);
   k_oneway<<<(nrow + G - 1) / G, kThreads, sm, st>>>(c, f, up, adj, recursive, in, out, nrow, add, G);
+  note_launch();
 }
 
 void launch_pad_model(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st) {
   size_t n = (size_t)M * nz * (nx + 2 * pad);
   k_pad_model<<<grid_for(n), 256, 0, st>>>(in, out, M, nz, nx, pad);
+  note_launch();
 }
 
 void launch_drefl_fwd(const DevCtx& c, int M, const float2* a0, const float2* b0, const float2* a1,
                       const float2* b1, const float2* dm0, const float2* dm1, float2* out, cudaStream_t st) {
   size_t n = (size_t)M * c.nz * c.nxg;
   k_drefl_fwd<<<grid_for(n), 256, 0, st>>>(M, c.nz, c.nxg, a0, b0, a1, b1, dm0, dm1, out);
+  note_launch();
 }
 
 void launch_reduce_images(const float2* parts, const int* slice_beg, int M, size_t plane, float2* out,
                           cudaStream_t st) {
   size_t n = (size_t)M * plane;
   k_reduce<<<grid_for(n), 256, 0, st>>>(parts, slice_beg, M, plane, out);
+  note_launch();
 }
 
 void launch_grad_assemble(const DevCtx& c, int M, const float2* a0, const float2* b0, const float2* a1,
@@ -937,6 +953,7 @@ void launch_grad_assemble(const DevCtx& c, int M, const float2* a0, const float2
                           int add, cudaStream_t st) {
   size_t n = (size_t)M * c.nz * nx;
   k_grad<<<grid_for(n), 256, 0, st>>>(M, c.nz, c.nxg, nx, c.pad, a0, b0, a1, b1, IR, IS, g0, g1, add);
+  note_launch();
 }
 
 static int trace_rows(int n) {
@@ -951,6 +968,7 @@ void launch_time_to_bins(const FftPlan& P, const float2* tw, const float* t, flo
   size_t sm = 8 * (al(P.n) + 2 * al((size_t)G * P.n));
   set_smem(k_time_to_bins, sm);
   k_time_to_bins<<<(ntr + G - 1) / G, kThreads, sm, st>>>(P, tw, t, b, ntr, nt, G);
+  note_launch();
 }
 
 void launch_bins_to_time(const FftPlan& P, const float2* tw, const float2* b, float* t, int ntr, int nt, int add,
@@ -959,16 +977,19 @@ void launch_bins_to_time(const FftPlan& P, const float2* tw, const float2* b, fl
   size_t sm = 8 * (al(P.n) + 2 * al((size_t)G * P.n));
   set_smem(k_bins_to_time, sm);
   k_bins_to_time<<<(ntr + G - 1) / G, kThreads, sm, st>>>(P, tw, b, t, ntr, nt, add, G);
+  note_launch();
 }
 
 void launch_copy_rows(const float2* src, int lds, float2* dst, int ldd, int nrows, int ncopy, int add,
                       cudaStream_t st) {
   size_t n = (size_t)nrows * ldd;
   k_copy_rows<<<grid_for(n), 256, 0, st>>>(src, lds, dst, ldd, nrows, ncopy, add);
+  note_launch();
 }
 
 void launch_scale_add(float2* y, const float2* x, size_t n, cudaStream_t st) {
   k_add<<<grid_for(n), 256, 0, st>>>(y, x, n);
+  note_launch();
 }
 
 }  // namespace wg

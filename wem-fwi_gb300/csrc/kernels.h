@@ -50,6 +50,9 @@ size_t smem_born_fwd(const DevCtx& c, int G);
 size_t smem_born_adj(const DevCtx& c, int G);
 size_t smem_rows(const DevCtx& c, int G);
 int max_smem_per_block();
+// counts the library's kernel launches (wem_launch_count)
+void note_launch();
+long long launch_count();
 
 // ---- table builders
 void launch_phase_tables(const DevCtx& c, const float2* sref /*[M][nz][nref]*/, float eps, float2* ph,

@@ -838,12 +838,15 @@ void launch_pass_w(int which, const DevCtx& c, const Group* g, int ng, const flo
   if (which == 0) {
     cudaFuncSetAttribute(kw_wem<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     kw_wem<E><<<ng, kW * 32, sm, st>>>(c, L, g, s1, bins);
+    note_launch();
   } else if (which == 1) {
     cudaFuncSetAttribute(kw_born_fwd<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     kw_born_fwd<E><<<ng, kW * 32, sm, st>>>(c, L, g, dm, drm, s1, s2, bins);
+    note_launch();
   } else {
     cudaFuncSetAttribute(kw_born_adj<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     kw_born_adj<E><<<ng, kW * 32, sm, st>>>(c, L, g, s1, s2, bins, ir, is, compat);
+    note_launch();
   }
 }
 

@@ -185,6 +185,7 @@ extern "C" int wemop_onestep_noalloc(const wem_params* p, const void* slow_row, 
   k_noalloc_setup<<<8, 256, 0, st>>>(N, nxg, p->pad, (double)p->dx, freq, p->nref,
                                      static_cast<const float2*>(slow_row), static_cast<const float2*>(sref), refidx,
                                      tw, kx, taper, omega, q);
+  wg::note_launch();
   // one depth, one frequency: the depth-step kernels index the tables at (f, z) = (0, 0)
   wg::DevCtx c{};
   c.plan = plan;

@@ -122,11 +122,13 @@ int grid_of(size_t n) {
 void launch_pad_edge(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st) {
   size_t n = (size_t)M * nz * (nx + 2 * pad);
   k_pad_edge<<<grid_of(n), 256, 0, st>>>(in, out, M, nz, nx, pad);
+  note_launch();
 }
 
 void launch_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref, cudaStream_t st) {
   size_t n = (size_t)M * nz * nref;
   k_sref<<<grid_of(n), 256, 0, st>>>(sp, sref, M, nz, nxg, nref);
+  note_launch();
 }
 
 void launch_point_tables(int M, int nz, int nxg, int nref, int ntaylor, float eps, const float2* sp,
@@ -135,6 +137,7 @@ void launch_point_tables(int M, int nz, int nxg, int nref, int ntaylor, float ep
   size_t n = (size_t)M * nz * nxg;
   k_point_tables<<<grid_of(n), 256, 0, st>>>(M, nz, nxg, nref, ntaylor + 1, (double)eps, sp, dp, sref, ref, q, rc,
                                              sc, a0, b0, a1, b1);
+  note_launch();
 }
 
 }  // namespace wg

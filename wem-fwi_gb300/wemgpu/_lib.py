@@ -29,6 +29,7 @@ _SIGS = {
     "wem_stats_enable": (_i, [_i]),
     "wem_stats_get": (_i, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)]),
     "wem_stats_reset": (_i, []),
+    "wem_launch_count": (ctypes.c_longlong, []),
     "wem_set_plain": (_i, [_i]),
     "wem_set_kernel_path": (_i, [_i]),
     "wem_create": (_i, [_pp, _v, ctypes.POINTER(_h)]),
@@ -90,6 +91,11 @@ def kernel_stats(name: str):
     ms, n = ctypes.c_double(), ctypes.c_longlong()
     call("wem_stats_get", name.encode(), ctypes.byref(ms), ctypes.byref(n))
     return ms.value, n.value
+
+
+def launch_count() -> int:
+    """Kernel launches the library has made in this process."""
+    return int(load().wem_launch_count())
 
 
 def call(name: str, *args) -> None:
