@@ -219,6 +219,10 @@ WARP_CASES = {
     "n512": dict(nx=504, pad=4, tap=0, prop="pspi", nref=3),
     "n768": dict(nx=752, pad=4, tap=4, prop="ssf", nref=1),
     "n1024": dict(nx=1016, pad=0, tap=4, prop="pspi", nref=2),
+    # tap = 0 (the reference's default): kernels built with every point on the grid
+    "n768t0": dict(nx=760, pad=4, tap=0, prop="ssf", nref=1),
+    "n384t0": dict(nx=384, pad=0, tap=0, prop="ssf", nref=1),
+    "n512t0p": dict(nx=512, pad=0, tap=0, prop="pspi", nref=1),
 }
 
 
@@ -259,7 +263,21 @@ def test_paths_wem_and_born(gpu_lib, oracle, case, kernel_path):
         assert rel_l2(a1, q1) < TOL_OP, (mode, "adj rho", rel_l2(a1, q1))
 
 
-@pytest.mark.parametrize("case", ["n256", "n768"])
+@pytest.mark.parametrize("case", ["n768t0", "n256"])
+def test_born_adjoint_many_shots(gpu_lib, oracle, case):
+    """More shots than rows per CTA: full and partial groups of one frequency."""
+    from wemgpu.core import BornOp
+    p, par, wav, s, rho = small_case(nz=12, ns=11, **WARP_CASES[case])
+    op = BornOp(p, wav, s, rho)
+    d = (np.random.default_rng(13).random((p.ns, p.nr, p.nt)) - .5).astype(np.float32)
+    a0, a1 = np.zeros_like(s), np.zeros_like(s)
+    op.adjoint(a0, a1, d)
+    q0, q1 = oracle.born_adjoint(p, wav, s, rho, d, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(a0, q0) < TOL_OP, rel_l2(a0, q0)
+    assert rel_l2(a1, q1) < TOL_OP, rel_l2(a1, q1)
+
+
+@pytest.mark.parametrize("case", ["n256", "n768", "n768t0"])
 def test_warp_path_is_deterministic(gpu_lib, case):
     from wemgpu.core import BornOp
     p, par, wav, s, rho = small_case(nz=16, ns=2, **WARP_CASES[case])

@@ -191,14 +191,14 @@ class Engine {
     return ok;
   }
 
-  int warp_G() const { return g_plain ? 1 : std::min(geo_.ns, warp_rows_per_group()); }
+  int warp_G(int which) const { return g_plain ? 1 : std::min(geo_.ns, warp_rows_per_group(ctx_, which)); }
 
   void wem_forward(const void* s2, const void* rho, void* data, int kind, int add) {
     set_background(s2, rho);
     float2* bins = zero_bins();
     const size_t plane = (size_t)p_.nz * geo_.nxg;
     const bool wp = warp_path();
-    int G = wp ? warp_G() : pick_G([&](int g) { return smem_wem(ctx_, g); });
+    int G = wp ? warp_G(0) : pick_G([&](int g) { return smem_wem(ctx_, g); });
     for_chunks(G, plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = store1_.as<float2>((size_t)rows * plane);
       if (wp) timed("k_wem", [&] { launch_pass_warp(0, ctx_, gd, ng, nullptr, nullptr, A, nullptr, bins, nullptr, nullptr, 0, 0); });
@@ -219,7 +219,7 @@ class Engine {
     launch_drefl_fwd(ctx_, M_, a0_, b0_, a1_, b1_, dm0, dm1, drm, 0);
     float2* bins = zero_bins();
     const bool wp = warp_path();
-    int G = wp ? warp_G() : pick_G([&](int g) { return smem_born_fwd(ctx_, g); });
+    int G = wp ? warp_G(1) : pick_G([&](int g) { return smem_born_fwd(ctx_, g); });
     for_chunks(G, 2 * plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = store1_.as<float2>((size_t)rows * plane);
       float2* B = store2_.as<float2>((size_t)rows * plane);
@@ -240,7 +240,7 @@ class Engine {
     cuda_check(cudaMemsetAsync(IR, 0, (size_t)M_ * plane * 8, 0), "memset");
     cuda_check(cudaMemsetAsync(IS, 0, (size_t)M_ * plane * 8, 0), "memset");
     const bool wp = warp_path();
-    int G = wp ? warp_G() : pick_G([&](int g) { return smem_born_adj(ctx_, g); });
+    int G = wp ? warp_G(2) : pick_G([&](int g) { return smem_born_adj(ctx_, g); });
     const int compat = p_.adjoint_mode == WEM_ADJ_COMPAT ? 1 : 0;
     // per row: two stored fields; per group: two partial images
     for_chunks(G, 2 * plane * 8 + (2 * plane * 8 + G - 1) / G, [&](const Group* gd, int ng, int rows) {

@@ -80,7 +80,8 @@ void launch_oneway(const DevCtx& c, int f, int up, int adj, int recursive, const
 
 // ---- warp-per-row passes (kernels_w.cu), N = 32 E with E in {8,12,16,24,32}
 bool warp_path_supported(const DevCtx& c);
-int warp_rows_per_group();
+// rows (shots) per CTA of a warp-path pass (which: 0 WEM, 1 Born forward, 2 Born adjoint)
+int warp_rows_per_group(const DevCtx& c, int which);
 size_t warp_smem_bytes(const DevCtx& c, int which);
 // which: 0 WEM, 1 Born forward, 2 Born adjoint (arguments as the launchers above)
 void launch_pass_warp(int which, const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm,

@@ -61,6 +61,7 @@ __device__ __forceinline__ void warp_copy(void* dst, const void* src, int bytes,
 
 // ------------------------------------------------------- per-depth tables
 struct Tabs {
+  bool has_fac;            // SSF split-step table present
   const float2* ph;        // [nref][N]
   const float2* fac;       // [nxg] taper * split step / N (SSF), or null
   const signed char* ref;  // [nxg] reference index
@@ -81,6 +82,7 @@ __device__ __forceinline__ Tabs global_tabs(const DevCtx& c, const Src& s, int f
   const size_t zo = ((size_t)m * c.nz + z) * c.nxg;
   const size_t plane = (size_t)c.nz * c.nxg;
   Tabs t;
+  t.has_fac = c.fac != nullptr;
   t.ph = c.ph + ((size_t)f * c.nz + z) * c.nref * c.N;
   t.fac = c.fac ? c.fac + ((size_t)f * c.nz + z) * c.nxg : nullptr;
   t.ref = c.ref + zo;
@@ -133,6 +135,22 @@ struct Ring {
     Tabs g = global_tabs(c, src, f, d);
     return L.nslots ? slot_tabs(L, slot(d), g) : g;
   }
+  // every table of the depth from its slot (the caller guarantees that the
+  // layout holds all tables it reads); pointers stay in the shared window
+  __device__ Tabs stabs(int d) const {
+    const char* p = slot(d);
+    Tabs t;
+    t.has_fac = c.fac != nullptr;
+    t.ph = reinterpret_cast<const float2*>(p + L.ph);
+    t.fac = reinterpret_cast<const float2*>(p + L.fac);
+    t.ref = reinterpret_cast<const signed char*>(p + L.ref);
+    t.rc = reinterpret_cast<const float2*>(p + L.rc);
+    t.c0 = reinterpret_cast<const float2*>(p + L.c0);
+    t.c1 = reinterpret_cast<const float2*>(p + L.c1);
+    t.dm = reinterpret_cast<const float2*>(p + L.dm);
+    t.dr = reinterpret_cast<const float2*>(p + L.dr);
+    return t;
+  }
 };
 
 struct WRow {
@@ -142,33 +160,36 @@ struct WRow {
   const float* taperN;
   const float* kx;
   int lane;
+  // FFT zero pad and grid width of the row; kernels built for tap = 0 pass
+  // the constants 0 and N, so every point is known to be on the grid
+  int tap, nxg;
 };
 
 // clamped grid index of register j: loads through it are issued without a
 // branch (so a lane's E loads are all in flight together) and the result is
 // selected with `in` afterwards
-__device__ __forceinline__ int xclamp(const DevCtx& c, int lane, int j, bool& in) {
-  const int x = lane + 32 * j - c.tap;
-  in = (unsigned)x < (unsigned)c.nxg;
+__device__ __forceinline__ int xclamp(const WRow& w, int j, bool& in) {
+  const int x = w.lane + 32 * j - w.tap;
+  in = (unsigned)x < (unsigned)w.nxg;
   return in ? x : 0;
 }
 
 template <int E>
-__device__ __forceinline__ void w_load(const DevCtx& c, int lane, const float2* row, float2 (&v)[E]) {
+__device__ __forceinline__ void w_load(const WRow& w, const float2* row, float2 (&v)[E]) {
 #pragma unroll
   for (int j = 0; j < E; ++j) {
     bool in;
-    const float2 a = row[xclamp(c, lane, j, in)];
+    const float2 a = row[xclamp(w, j, in)];
     v[j] = in ? a : make_float2(0.f, 0.f);
   }
 }
 
 template <int E>
-__device__ __forceinline__ void w_store(const DevCtx& c, int lane, float2* row, const float2 (&v)[E]) {
+__device__ __forceinline__ void w_store(const WRow& w, float2* row, const float2 (&v)[E]) {
 #pragma unroll
   for (int j = 0; j < E; ++j) {
     bool in;
-    const int x = xclamp(c, lane, j, in);
+    const int x = xclamp(w, j, in);
     if (in) row[x] = v[j];
   }
 }
@@ -179,150 +200,147 @@ __device__ __forceinline__ void w_zero(float2 (&v)[E]) {
   for (int j = 0; j < E; ++j) v[j] = make_float2(0.f, 0.f);
 }
 
-// o = P_z u  (SSF.cpp:8-32, PSPI.cpp:8-29); u and o may be the same array.
-// SSF: the split-step table is zero where a point has no reference, so the
-// reference index is only read for PSPI or several references.
+// ---------------------------------------------------------------- row ops
+// Every transform of a depth step is one "op": X <- pre(X); X <- FFT(X);
+// X <- mid(X); X <- IFFT(X); post(X).  A pass kernel runs the ops of a depth
+// in a loop that is not unrolled, so the kernel holds one forward and one
+// inverse transform per sweep whatever the number of ops, and only the state
+// rows plus the op's X are live in registers.  MR (several references) runs
+// the reference loop of SSF.cpp / PSPI.cpp around the transform pair; the
+// single-reference kernels are instantiated without it.
+
+// forward step, mid: X *= phase row of reference jr (SSF.cpp:18-23, PSPI.cpp:15-20)
 template <int E>
-__device__ void w_step_fwd(const WRow& w, const Tabs& T, const float2 (&u)[E], float2 (&o)[E]) {
-  const DevCtx& c = w.c;
-  constexpr int N = 32 * E;
-  float2 X[E];
+__device__ __forceinline__ void fwd_mid(const WRow& w, const Tabs& T, int jr, float2 (&X)[E]) {
+  const float2* pj = T.ph + (size_t)jr * 32 * E;
 #pragma unroll
-  for (int j = 0; j < E; ++j) X[j] = u[j];
-  wfft<E, false>(X, w.sb, w.tw, w.lane);
-  if (c.nref == 1) {
-#pragma unroll
-    for (int j = 0; j < E; ++j) X[j] = c_mul(X[j], T.ph[w.lane + 32 * j]);
-    wfft<E, true>(X, w.sb, w.tw, w.lane);
-    if (T.fac) {
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        bool in;
-        const float2 fx = T.fac[xclamp(c, w.lane, j, in)];
-        o[j] = in ? c_mul(X[j], fx) : make_float2(0.f, 0.f);
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        bool in;
-        const int x = xclamp(c, w.lane, j, in);
-        const float tp = w.taperN[x];
-        const int r = T.ref[x];
-        o[j] = (in && r == 0) ? c_scale(X[j], tp) : make_float2(0.f, 0.f);
-      }
-    }
-  } else {
-    w_zero<E>(o);
-    for (int jr = 0; jr < c.nref; ++jr) {
-      float2 Y[E];
-      const float2* pj = T.ph + (size_t)jr * N;
-#pragma unroll
-      for (int j = 0; j < E; ++j) Y[j] = c_mul(X[j], pj[w.lane + 32 * j]);
-      wfft<E, true>(Y, w.sb, w.tw, w.lane);
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        bool in;
-        const int x = xclamp(c, w.lane, j, in);
-        const int r = T.ref[x];
-        const float2 v = T.fac ? c_mul(Y[j], T.fac[x]) : c_scale(Y[j], w.taperN[x]);
-        if (in && r == jr) o[j] = v;
-      }
-    }
-  }
+  for (int j = 0; j < E; ++j) X[j] = c_mul(X[j], pj[w.lane + 32 * j]);
 }
 
-// o = P^H_z d  (SSF.cpp:34-60, PSPI.cpp:31-53); d and o may be the same array
-template <int E>
-__device__ void w_step_adj(const WRow& w, const Tabs& T, const float2 (&d)[E], float2 (&o)[E]) {
-  const DevCtx& c = w.c;
-  constexpr int N = 32 * E;
-  float2 A[E];
-  if (c.nref == 1) {
+// forward step, post: o = split step x taper x X / N at the points whose
+// reference is jr (SSF.cpp:24-31, PSPI.cpp:21-28).  Single reference: the
+// split-step table is zero where a point has no reference, so the index is
+// only read without it (PSPI).  MR: o keeps its value at other points and is
+// cleared at jr = 0.
+template <int E, bool MR>
+__device__ __forceinline__ void fwd_post(const WRow& w, const Tabs& T, int jr, const float2 (&X)[E], float2 (&o)[E]) {
+  const float2 zero = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int j = 0; j < E; ++j) {
-      bool in;
-      const int x = xclamp(c, w.lane, j, in);
-      if (T.fac) {
+  for (int j = 0; j < E; ++j) {
+    bool in;
+    const int x = xclamp(w, j, in);
+    if (!MR) {
+      if (T.has_fac) {
         const float2 fx = T.fac[x];
-        A[j] = in ? c_mulc(d[j], fx) : make_float2(0.f, 0.f);
+        o[j] = in ? c_mul(X[j], fx) : zero;
       } else {
         const float tp = w.taperN[x];
         const int r = T.ref[x];
-        A[j] = (in && r == 0) ? c_scale(d[j], tp) : make_float2(0.f, 0.f);
+        o[j] = (in && r == 0) ? c_scale(X[j], tp) : zero;
       }
+    } else {
+      const int r = T.ref[x];
+      const float2 v = T.has_fac ? c_mul(X[j], T.fac[x]) : c_scale(X[j], w.taperN[x]);
+      o[j] = (in && r == jr) ? v : (jr == 0 ? zero : o[j]);
     }
-    wfft<E, false>(A, w.sb, w.tw, w.lane);
-#pragma unroll
-    for (int j = 0; j < E; ++j) A[j] = c_mulc(A[j], T.ph[w.lane + 32 * j]);
-  } else {
-    float2 acc[E];
-    w_zero<E>(acc);
-    for (int jr = 0; jr < c.nref; ++jr) {
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        bool in;
-        const int x = xclamp(c, w.lane, j, in);
-        const int r = T.ref[x];
-        const float2 v = T.fac ? c_mulc(d[j], T.fac[x]) : c_scale(d[j], w.taperN[x]);
-        A[j] = (in && r == jr) ? v : make_float2(0.f, 0.f);
-      }
-      wfft<E, false>(A, w.sb, w.tw, w.lane);
-      const float2* pj = T.ph + (size_t)jr * N;
-#pragma unroll
-      for (int j = 0; j < E; ++j) acc[j] = c_add(acc[j], c_mulc(A[j], pj[w.lane + 32 * j]));
-    }
-#pragma unroll
-    for (int j = 0; j < E; ++j) A[j] = acc[j];
-  }
-  wfft<E, true>(A, w.sb, w.tw, w.lane);
-#pragma unroll
-  for (int j = 0; j < E; ++j) {
-    bool in;
-    xclamp(c, w.lane, j, in);
-    o[j] = in ? A[j] : make_float2(0.f, 0.f);
   }
 }
 
-// Taylor Born scatter (Scatter.cpp:35-111) for ntaylor <= 1 (the warp path
-// serves ntaylor 0 and 1; larger orders run on the shared-memory kernels).
-// mode 0 forward, 1 adjoint as coded (filter before scaling), 2 exact
-// adjoint.  o = Sc u (overwrite); u and o may be the same array.
+// adjoint step, pre: X = conj(split step) x taper x d / N at the points of
+// reference jr (SSF.cpp:36-45, PSPI.cpp:33-41)
+template <int E, bool MR>
+__device__ __forceinline__ void adj_pre(const WRow& w, const Tabs& T, int jr, const float2 (&d)[E], float2 (&X)[E]) {
+  const float2 zero = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    bool in;
+    const int x = xclamp(w, j, in);
+    if (!MR) {
+      if (T.has_fac) {
+        const float2 fx = T.fac[x];
+        X[j] = in ? c_mulc(d[j], fx) : zero;
+      } else {
+        const float tp = w.taperN[x];
+        const int r = T.ref[x];
+        X[j] = (in && r == 0) ? c_scale(d[j], tp) : zero;
+      }
+    } else {
+      const int r = T.ref[x];
+      const float2 v = T.has_fac ? c_mulc(d[j], T.fac[x]) : c_scale(d[j], w.taperN[x]);
+      X[j] = (in && r == jr) ? v : zero;
+    }
+  }
+}
+
+// adjoint step, mid: X *= conj(phase row jr); MR sums the references'
+// spectra in Y and returns true once X holds the sum (the inverse transform
+// runs after the last reference only)
+template <int E, bool MR>
+__device__ __forceinline__ bool adj_mid(const WRow& w, const Tabs& T, int jr, float2 (&X)[E], float2 (&Y)[MR ? E : 1]) {
+  const float2* pj = T.ph + (size_t)jr * 32 * E;
+  if constexpr (!MR) {
+#pragma unroll
+    for (int j = 0; j < E; ++j) X[j] = c_mulc(X[j], pj[w.lane + 32 * j]);
+    return true;
+  } else {
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      const float2 v = c_mulc(X[j], pj[w.lane + 32 * j]);
+      Y[j] = jr == 0 ? v : c_add(Y[j], v);
+    }
+    if (jr + 1 < w.c.nref) return false;
+#pragma unroll
+    for (int j = 0; j < E; ++j) X[j] = Y[j];
+    return true;
+  }
+}
+
+// adjoint step, post: o = X on the model grid, zero in the FFT pad
 template <int E>
-__device__ void w_scatter(const WRow& w, const Tabs& T, float om, int mode, const float2 (&u)[E],
-                          float2 (&o)[E]) {
-  const DevCtx& c = w.c;
+__device__ __forceinline__ void adj_post(const WRow& w, const float2 (&X)[E], float2 (&o)[E]) {
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    bool in;
+    xclamp(w, j, in);
+    o[j] = in ? X[j] : make_float2(0.f, 0.f);
+  }
+}
+
+// Taylor Born scatter (Scatter.cpp:35-111) for ntaylor <= 1; mode 0 forward,
+// 1 adjoint as coded (filter before scaling), 2 exact adjoint.
+// pre: the filter's input, u or conj(c_1) u (exact adjoint)
+template <int E>
+__device__ __forceinline__ void sc_pre(const WRow& w, const Tabs& T, int mode, const float2 (&u)[E], float2 (&X)[E]) {
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    if (mode == 2) {
+      bool in;
+      const float2 k1 = T.c1[xclamp(w, j, in)];
+      X[j] = in ? c_mulc(u[j], k1) : make_float2(0.f, 0.f);
+    } else {
+      X[j] = u[j];
+    }
+  }
+}
+// mid: the (k / omega)^2 filter, with the 1/N of the inverse transform
+template <int E>
+__device__ __forceinline__ void sc_mid(const WRow& w, float om, float2 (&X)[E]) {
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    const float kw = w.kx[w.lane + 32 * j] / om;
+    X[j] = c_scale(X[j], kw * kw * w.c.invN);
+  }
+}
+// post, one point: i w dz (c_0 u + c_1 filtered) with the mode's conjugations;
+// x is the filtered value (ignored when ntaylor = 0)
+__device__ __forceinline__ float2 sc_val(float2 iw, int mode, bool t1, float2 k0, float2 k1, float2 u, float2 x) {
+  float2 y = mode == 0 ? c_mul(k0, u) : c_mulc(u, k0);
+  if (t1) y = c_add(y, mode == 0 ? c_mul(k1, x) : (mode == 1 ? c_mulc(x, k1) : x));
+  return c_mul(iw, y);
+}
+__device__ __forceinline__ float2 sc_iw(const DevCtx& c, float om, int mode) {
   const float wdz = om * c.dz;
-  const float2 iw = make_float2(0.f, mode == 0 ? -wdz : wdz);
-  const bool t1 = c.ntaylor >= 1;
-  float2 X[E];
-#pragma unroll
-  for (int j = 0; j < E; ++j) {
-    bool in;
-    const int x = xclamp(c, w.lane, j, in);
-    const float2 k0 = T.c0[x];
-    const float2 k1 = t1 ? T.c1[x] : make_float2(0.f, 0.f);
-    // transform input: u, or conj(c_1) u for the exact adjoint
-    X[j] = (mode == 2 && t1) ? (in ? c_mulc(u[j], k1) : make_float2(0.f, 0.f)) : u[j];
-    o[j] = in ? c_mul(iw, mode == 0 ? c_mul(k0, u[j]) : c_mulc(u[j], k0)) : make_float2(0.f, 0.f);
-  }
-  if (!t1) return;
-  wfft<E, false>(X, w.sb, w.tw, w.lane);
-#pragma unroll
-  for (int j = 0; j < E; ++j) {
-    float kw = w.kx[w.lane + 32 * j] / om;
-    X[j] = c_scale(X[j], kw * kw * c.invN);
-  }
-  wfft<E, true>(X, w.sb, w.tw, w.lane);
-#pragma unroll
-  for (int j = 0; j < E; ++j) {
-    bool in;
-    const int x = xclamp(c, w.lane, j, in);
-    const float2 k1 = T.c1[x];
-    float2 y = X[j];
-    if (mode == 0) y = c_mul(k1, y);
-    else if (mode == 1) y = c_mulc(y, k1);
-    if (in) o[j] = c_add(o[j], c_mul(iw, y));
-  }
+  return make_float2(0.f, mode == 0 ? -wdz : wdz);
 }
 
 // add gs[g] wavelet into the row of shot s at depth z (Injection.cpp:8-19)
@@ -334,7 +352,7 @@ __device__ __forceinline__ void w_inject_src(const WRow& w, float2 (&v)[E], int 
   for (int g = -c.ngs; g <= c.ngs; ++g) {
     int x = c.sx[s] + g + c.pad;
     if (x < 0 || x >= c.nxg) continue;
-    int n = x + c.tap;
+    int n = x + w.tap;
     if ((n & 31) != w.lane) continue;
     const int jn = n >> 5;
     const float2 add = c_scale(wv, c.gs[g + c.ngs]);
@@ -352,14 +370,14 @@ __device__ __forceinline__ void w_record(const WRow& w, const float2 (&v)[E], in
   const int k0 = c.rptr[z], k1 = c.rptr[z + 1];
   if (k0 == k1) return;
 #pragma unroll
-  for (int j = 0; j < E; ++j) w.sb[swz(w.lane + 32 * j)] = v[j];
+  for (int j = 0; j < E; ++j) w.sb[swz<E>(w.lane + 32 * j)] = v[j];
   __syncwarp();
   for (int k = k0 + w.lane; k < k1; k += 32) {
     const int x0 = c.rxs[k] + c.pad;
     float2 acc = make_float2(0.f, 0.f);
     for (int g = -c.ngr; g <= c.ngr; ++g) {
       int x = x0 + g;
-      if (x >= 0 && x < c.nxg) acc = c_add(acc, c_scale(w.sb[swz(x + c.tap)], c.gr[g + c.ngr]));
+      if (x >= 0 && x < c.nxg) acc = c_add(acc, c_scale(w.sb[swz<E>(x + w.tap)], c.gr[g + c.ngr]));
     }
     float2* d = bins + ((size_t)s * c.nr + c.rid[k]) * c.nbin + bin;
     *d = c_add(*d, acc);
@@ -377,7 +395,7 @@ __device__ __forceinline__ void w_inject_rec(const WRow& w, float2 (&v)[E], int 
 #pragma unroll
   for (int j = 0; j < E; ++j) {
     bool in;
-    const int x = xclamp(c, w.lane, j, in);
+    const int x = xclamp(w, j, in);
     if (!in) continue;
     int lo = x - c.pad - c.ngr, hi = x - c.pad + c.ngr;
     int a = k0, b = k1;
@@ -395,7 +413,7 @@ __device__ __forceinline__ void w_inject_rec(const WRow& w, float2 (&v)[E], int 
 }
 
 // shared-memory carve-up common to the pass kernels:
-// [tw: N][kx: N][taper: nxg][exchange: kW x wbuf][ring][rows][image slots]
+// [tw: N][kx: N][taper: nxg][exchange: nbuf x wbuf][ring][rows][image slots]
 template <int E>
 struct Carve {
   float2* tw;
@@ -405,7 +423,7 @@ struct Carve {
   char* ring;
   char* rows;
   float2* slots;
-  __device__ Carve(const DevCtx& c, const SlotLayout& L, bool with_slots) {
+  __device__ Carve(const DevCtx& c, const SlotLayout& L, bool with_slots, int nbuf = kW) {
     extern __shared__ float4 smem4[];
     char* p = reinterpret_cast<char*>(smem4);
     auto take = [&](size_t bytes) {
@@ -416,25 +434,35 @@ struct Carve {
     tw = reinterpret_cast<float2*>(take((size_t)32 * E * 8));
     kx = reinterpret_cast<float*>(take((size_t)32 * E * 4));
     taperN = reinterpret_cast<float*>(take((size_t)c.nxg * 4));
-    sb0 = reinterpret_cast<float2*>(take((size_t)kW * wbuf_len<E>() * 8));
+    sb0 = reinterpret_cast<float2*>(take((size_t)nbuf * wbuf_len<E>() * 8));
     ring = take((size_t)L.nslots * L.bytes);
     rows = take((size_t)2 * kW * L.row_bytes);
     slots = reinterpret_cast<float2*>(take(with_slots ? (size_t)kW * c.nxg * 8 : 0));
   }
 };
 
+// twiddles in the per-stage layout of wfft.cuh (gathered from the natural
+// table W_N^t), k grid and taper
 template <int E>
 __device__ __forceinline__ void stage_static(const DevCtx& c, const Carve<E>& sm) {
-  for (int i = threadIdx.x; i < 32 * E; i += blockDim.x) {
-    sm.tw[i] = c.tw[i];
-    sm.kx[i] = c.kx[i];
+  constexpr int N = 32 * E;
+  for (int i = threadIdx.x; i < tw_entries<E>(); i += blockDim.x) {
+    int S = 1, L = WPlan<E>::r(0), off = 0;
+    while (S < WPlan<E>::n - 1 && i >= off + (WPlan<E>::r(S) - 1) * L) {
+      off += (WPlan<E>::r(S) - 1) * L;
+      L *= WPlan<E>::r(S);
+      ++S;
+    }
+    const int R = WPlan<E>::r(S), r = (i - off) / L + 1, l = (i - off) % L;
+    sm.tw[i] = c.tw[r * l * (N / (L * R))];
   }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) sm.kx[i] = c.kx[i];
   for (int i = threadIdx.x; i < c.nxg; i += blockDim.x) sm.taperN[i] = c.taperN[i];
 }
 
 // =============================================================== passes
 // nonlinear modelling (wem_prop.cpp:52-74), as k_wem in kernels.cu
-template <int E>
+template <int E, bool MR, bool NT>
 __global__ void __launch_bounds__(kW * 32, 1) kw_wem(DevCtx c, SlotLayout L, const Group* groups, float2* store,
                                                      float2* bins) {
   const Carve<E> sm(c, L, false);
@@ -442,13 +470,15 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_wem(DevCtx c, SlotLayout L, con
   stage_static<E>(c, sm);
   const Group gp = groups[blockIdx.x];
   const bool act = warp < gp.n;
-  const WRow w{c, sm.tw, sm.sb0 + warp * wbuf_len<E>(), sm.taperN, sm.kx, lane};
+  const WRow w{c, sm.tw, sm.sb0 + warp * wbuf_len<E>(), sm.taperN, sm.kx, lane, NT ? 0 : c.tap, NT ? 32 * E : c.nxg};
   const int f = gp.f, s = gp.s0 + (act ? warp : 0), bin = c.bin[f], nz = c.nz, nxg = c.nxg;
+  const int nj = MR ? c.nref : 1;
   const size_t plane = (size_t)nz * nxg;
   float2* A = store + (size_t)(gp.row0 + (act ? warp : 0)) * plane;
   const Ring ring{c, L, sm.ring, Src{nullptr, nullptr}, f};
   float2* wrow = reinterpret_cast<float2*>(sm.rows + (size_t)warp * 2 * L.row_bytes);
-  float2 W[E];
+  float2 W[E], X[E];
+  float2 Y[MR ? E : 1];
   w_zero<E>(W);
   if (act) w_inject_src<E>(w, W, s, f, 0);
   ring.issue(0);
@@ -467,12 +497,26 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_wem(DevCtx c, SlotLayout L, con
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       bool in;
-      const int x = xclamp(c, lane, j, in);
+      const int x = xclamp(w, j, in);
       const float2 r = T.rc[x];
       if (in) A[(size_t)z * nxg + x] = c_mul(r, W[j]);
     }
     if (z == nz - 1) break;
-    w_step_fwd<E>(w, T, W, W);
+    // W = P_z W
+#pragma unroll 1
+    for (int jr = 0; jr < nj; ++jr) {
+#pragma unroll
+      for (int j = 0; j < E; ++j) X[j] = W[j];
+      wfft<E, false>(X, w.sb, w.tw, lane);
+      fwd_mid<E>(w, T, jr, X);
+      wfft<E, true>(X, w.sb, w.tw, lane);
+      if constexpr (MR) fwd_post<E, true>(w, T, jr, X, Y);
+      else fwd_post<E, false>(w, T, jr, X, W);
+    }
+    if constexpr (MR) {
+#pragma unroll
+      for (int j = 0; j < E; ++j) W[j] = Y[j];
+    }
     w_inject_src<E>(w, W, s, f, z + 1);
   }
   // up sweep; each warp prefetches its stored row one depth ahead
@@ -481,7 +525,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_wem(DevCtx c, SlotLayout L, con
   auto issue_row = [&](int d) {
     if (L.row_bytes && act && d >= 0) warp_copy(wrow + (size_t)(d & 1) * nxg, A + (size_t)d * nxg, nxg * 8, lane);
   };
-  if (act) w_load<E>(c, lane, A + (size_t)(nz - 1) * nxg, W);
+  if (act) w_load<E>(w, A + (size_t)(nz - 1) * nxg, W);
   ring.issue(nz - 1);
   issue_row(nz - 2);
   cp_commit();
@@ -498,20 +542,35 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_wem(DevCtx c, SlotLayout L, con
     w_record<E>(w, W, s, bin, z, bins);
     if (z == 0) break;
     const Tabs T = ring.tabs(z);
-    w_step_fwd<E>(w, T, W, W);
+    // W = P_z W + R[z-1] down[z-1]
+#pragma unroll 1
+    for (int jr = 0; jr < nj; ++jr) {
+#pragma unroll
+      for (int j = 0; j < E; ++j) X[j] = W[j];
+      wfft<E, false>(X, w.sb, w.tw, lane);
+      fwd_mid<E>(w, T, jr, X);
+      wfft<E, true>(X, w.sb, w.tw, lane);
+      if constexpr (MR) fwd_post<E, true>(w, T, jr, X, Y);
+      else fwd_post<E, false>(w, T, jr, X, W);
+    }
+    if constexpr (MR) {
+#pragma unroll
+      for (int j = 0; j < E; ++j) W[j] = Y[j];
+    }
     const float2* a = L.row_bytes ? wrow + (size_t)((z - 1) & 1) * nxg : A + (size_t)(z - 1) * nxg;
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       bool in;
-      const float2 v = a[xclamp(c, lane, j, in)];
+      const float2 v = a[xclamp(w, j, in)];
       if (in) W[j] = c_add(W[j], v);
     }
   }
   cp_wait0();
 }
 
-// Born forward, two sweeps per row (born_prop.cpp:75-113; k_born_fwd in kernels.cu)
-template <int E>
+// Born forward, two sweeps per row (born_prop.cpp:75-113; k_born_fwd in kernels.cu).
+// Ops of a depth: 0 scatter of bg dm into sd, 1 sd = P sd, 2 bg = P bg.
+template <int E, bool MR>
 __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, SlotLayout L, const Group* groups,
                                                           const float2* dm, const float2* drm, float2* storeA,
                                                           float2* storeB, float2* bins) {
@@ -520,17 +579,93 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, SlotLayout L
   stage_static<E>(c, sm);
   const Group gp = groups[blockIdx.x];
   const bool act = warp < gp.n;
-  const WRow w{c, sm.tw, sm.sb0 + warp * wbuf_len<E>(), sm.taperN, sm.kx, lane};
+  const WRow w{c, sm.tw, sm.sb0 + warp * wbuf_len<E>(), sm.taperN, sm.kx, lane, c.tap, c.nxg};
   const int f = gp.f, s = gp.s0 + (act ? warp : 0), bin = c.bin[f], nz = c.nz, nxg = c.nxg;
   const size_t plane = (size_t)nz * nxg;
   float2* A = storeA + (size_t)(gp.row0 + (act ? warp : 0)) * plane;
   float2* B = storeB + (size_t)(gp.row0 + (act ? warp : 0)) * plane;
   const float om = c.omega[f];
+  const float2 iw = sc_iw(c, om, 0);
+  const bool t1 = c.ntaylor >= 1;
   const Ring ring{c, L, sm.ring, Src{dm, drm}, f};
-  float2 bg[E], sd[E], t[E];
+  const float2 zero = make_float2(0.f, 0.f);
+  float2 bg[E], sd[E], X[E];
+  float2 Y[MR ? E : 1];
   w_zero<E>(bg);
   w_zero<E>(sd);
   if (act) w_inject_src<E>(w, bg, s, f, 0);
+
+  // the three ops of one depth with tables T; up adds the stored rows
+  // (a: A[z-1], b: B[z-1]) after the steps, down injects the source
+  auto depth_ops = [&](const Tabs& T, int znext, const float2* a, const float2* b) {
+#pragma unroll 1
+    for (int k = 0; k < 3; ++k) {
+      const int nj = (MR && k > 0) ? c.nref : 1;
+#pragma unroll 1
+      for (int jr = 0; jr < nj; ++jr) {
+        if (k == 0) {
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            bool in;
+            const float2 q = T.dm[xclamp(w, j, in)];
+            X[j] = in ? c_mul(bg[j], q) : zero;
+          }
+        } else if (k == 1) {
+#pragma unroll
+          for (int j = 0; j < E; ++j) X[j] = sd[j];
+        } else {
+#pragma unroll
+          for (int j = 0; j < E; ++j) X[j] = bg[j];
+        }
+        if (k > 0 || t1) {
+          wfft<E, false>(X, w.sb, w.tw, lane);
+          if (k == 0) sc_mid<E>(w, om, X);
+          else fwd_mid<E>(w, T, jr, X);
+          wfft<E, true>(X, w.sb, w.tw, lane);
+        }
+        if (k == 0) {
+          // sd += Sc_z (bg dm)
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            bool in;
+            const int x = xclamp(w, j, in);
+            const float2 q = T.dm[x], k0 = T.c0[x], k1 = t1 ? T.c1[x] : zero;
+            const float2 v = sc_val(iw, 0, t1, k0, k1, c_mul(bg[j], q), X[j]);
+            if (in) sd[j] = c_add(sd[j], v);
+          }
+        } else if constexpr (MR) {
+          fwd_post<E, true>(w, T, jr, X, Y);
+        } else {
+          if (k == 1) fwd_post<E, false>(w, T, jr, X, sd);
+          else fwd_post<E, false>(w, T, jr, X, bg);
+        }
+      }
+      if constexpr (MR) {
+        if (k == 1) {
+#pragma unroll
+          for (int j = 0; j < E; ++j) sd[j] = Y[j];
+        } else if (k == 2) {
+#pragma unroll
+          for (int j = 0; j < E; ++j) bg[j] = Y[j];
+        }
+      }
+    }
+    if (a) {
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        bool in;
+        const int x = xclamp(w, j, in);
+        const float2 va = a[x], vb = b[x];
+        if (in) {
+          bg[j] = c_add(bg[j], va);
+          sd[j] = c_add(sd[j], vb);
+        }
+      }
+    } else {
+      w_inject_src<E>(w, bg, s, f, znext);
+    }
+  };
+
   ring.issue(0);
   cp_commit();
   ring.issue(1);
@@ -547,27 +682,21 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, SlotLayout L
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       bool in;
-      const int x = xclamp(c, lane, j, in);
-      const float2 r = T.rc[x], d = T.dr[x], q = T.dm[x];
-      t[j] = in ? c_mul(bg[j], q) : make_float2(0.f, 0.f);
+      const int x = xclamp(w, j, in);
+      const float2 r = T.rc[x], d = T.dr[x];
       if (in) {
         A[(size_t)z * nxg + x] = c_mul(r, bg[j]);
         B[(size_t)z * nxg + x] = c_add(c_mul(bg[j], d), c_mul(r, sd[j]));
       }
     }
     if (z == nz - 1) break;
-    w_scatter<E>(w, T, om, 0, t, t);
-#pragma unroll
-    for (int j = 0; j < E; ++j) sd[j] = c_add(sd[j], t[j]);
-    w_step_fwd<E>(w, T, sd, sd);
-    w_step_fwd<E>(w, T, bg, bg);
-    w_inject_src<E>(w, bg, s, f, z + 1);
+    depth_ops(T, z + 1, nullptr, nullptr);
   }
   cp_wait0();
   __syncthreads();
   if (act) {
-    w_load<E>(c, lane, A + (size_t)(nz - 1) * nxg, bg);
-    w_load<E>(c, lane, B + (size_t)(nz - 1) * nxg, sd);
+    w_load<E>(w, A + (size_t)(nz - 1) * nxg, bg);
+    w_load<E>(w, B + (size_t)(nz - 1) * nxg, sd);
   }
   ring.issue(nz - 1);
   cp_commit();
@@ -586,30 +715,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, SlotLayout L
       l2_prefetch(A + (size_t)(z - 2) * nxg, nxg * 8);
       l2_prefetch(B + (size_t)(z - 2) * nxg, nxg * 8);
     }
-    const Tabs T = ring.tabs(z);
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-      bool in;
-      const float2 q = T.dm[xclamp(c, lane, j, in)];
-      t[j] = in ? c_mul(bg[j], q) : make_float2(0.f, 0.f);
-    }
-    w_scatter<E>(w, T, om, 0, t, t);
-#pragma unroll
-    for (int j = 0; j < E; ++j) sd[j] = c_add(sd[j], t[j]);
-    w_step_fwd<E>(w, T, sd, sd);
-    w_step_fwd<E>(w, T, bg, bg);
-    const float2* a = A + (size_t)(z - 1) * nxg;
-    const float2* b = B + (size_t)(z - 1) * nxg;
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-      bool in;
-      const int x = xclamp(c, lane, j, in);
-      const float2 va = a[x], vb = b[x];
-      if (in) {
-        bg[j] = c_add(bg[j], va);
-        sd[j] = c_add(sd[j], vb);
-      }
-    }
+    depth_ops(ring.tabs(z), z - 1, A + (size_t)(z - 1) * nxg, B + (size_t)(z - 1) * nxg);
   }
   cp_wait0();
 }
@@ -624,8 +730,13 @@ __device__ __forceinline__ void reduce_slots(const float2* slots, int nxg, int n
   }
 }
 
-// Born adjoint, two sweeps per row (born_prop.cpp:178-216; k_born_adj in kernels.cu)
-template <int E>
+// Born adjoint, two sweeps per row (born_prop.cpp:178-216; k_born_adj in kernels.cu).
+// Down sweep, depth z: image IR[z] += conj(wu) bg, then ops bg = P_z bg and
+// wu = P^H_{z+1} wu (= T[z+1], stored).  Up sweep, iteration z = nz .. 1
+// accumulates image row z - 1: ops q = P^H_{z-1} wd (B), LinDown^H
+// conj(bg[z-1]) Sc^H_{z-1} q (C), bu = P_z bu + R[z-1] bg[z-1] (D), LinUp^H
+// conj(bu[z-1]) Sc^H_{z-1} T[z-1] (A).
+template <int E, bool MR>
 __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L, const Group* groups,
                                                           float2* storeBG, float2* storeT, const float2* bins,
                                                           float2* imgR, float2* imgS, int compat) {
@@ -636,7 +747,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
   float2* slot = sm.slots + warp * nxg;
   const Group gp = groups[blockIdx.x];
   const bool act = warp < gp.n;
-  const WRow w{c, sm.tw, sm.sb0 + warp * wbuf_len<E>(), sm.taperN, sm.kx, lane};
+  const WRow w{c, sm.tw, sm.sb0 + warp * wbuf_len<E>(), sm.taperN, sm.kx, lane, c.tap, c.nxg};
   const int f = gp.f, s = gp.s0 + (act ? warp : 0), bin = c.bin[f];
   const size_t plane = (size_t)nz * nxg;
   float2* SBG = storeBG + (size_t)(gp.row0 + (act ? warp : 0)) * plane;
@@ -645,8 +756,13 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
   float2* IS = imgS + (size_t)blockIdx.x * plane;
   const int scmode = compat ? 1 : 2;
   const float om = c.omega[f];
+  const float2 iw = sc_iw(c, om, scmode);
+  const bool t1 = c.ntaylor >= 1;
+  const int nj_step = MR ? c.nref : 1;
   const float2 zero = make_float2(0.f, 0.f);
   const Ring ring{c, L, sm.ring, Src{nullptr, nullptr}, f};
+  float2 X[E];
+  float2 Y[MR ? E : 1];
   // ---------------- down sweep: bg (Down of the source) and wu (Up^H of the data)
   float2 bg[E], wu[E];
   w_zero<E>(bg);
@@ -657,7 +773,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       bool in;
-      const int x = xclamp(c, lane, j, in);
+      const int x = xclamp(w, j, in);
       if (in) ST[x] = zero;
     }
   }
@@ -672,126 +788,453 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       bool in;
-      const int x = xclamp(c, lane, j, in);
+      const int x = xclamp(w, j, in);
       if (in) slot[x] = act ? c_mulc(wu[j], bg[j]) : zero;
     }
     cp_wait1();
     __syncthreads();
     reduce_slots(sm.slots, nxg, kW, IR + (size_t)z * nxg);
     if (!act) continue;
-    w_store<E>(c, lane, SBG + (size_t)z * nxg, bg);
+    w_store<E>(w, SBG + (size_t)z * nxg, bg);
     if (z == nz - 1) continue;
-    w_step_fwd<E>(w, ring.tabs(z), bg, bg);
-    w_inject_src<E>(w, bg, s, f, z + 1);
-    w_step_adj<E>(w, ring.tabs(z + 1), wu, wu);  // T[z+1]
-    w_store<E>(c, lane, ST + (size_t)(z + 1) * nxg, wu);
-    w_inject_rec<E>(w, wu, s, bin, z + 1, bins);
+#pragma unroll 1
+    for (int k = 0; k < 2; ++k) {
+      const Tabs T = ring.tabs(z + k);
+#pragma unroll 1
+      for (int jr = 0; jr < nj_step; ++jr) {
+        if (k == 0) {
+#pragma unroll
+          for (int j = 0; j < E; ++j) X[j] = bg[j];
+        } else {
+          adj_pre<E, MR>(w, T, jr, wu, X);
+        }
+        wfft<E, false>(X, w.sb, w.tw, lane);
+        if (k == 0) fwd_mid<E>(w, T, jr, X);
+        else if (!adj_mid<E, MR>(w, T, jr, X, Y)) continue;
+        wfft<E, true>(X, w.sb, w.tw, lane);
+        if (k == 0) {
+          if constexpr (MR) fwd_post<E, true>(w, T, jr, X, Y);
+          else fwd_post<E, false>(w, T, jr, X, bg);
+        } else {
+          adj_post<E>(w, X, wu);
+        }
+      }
+      if (k == 0) {
+        if constexpr (MR) {
+#pragma unroll
+          for (int j = 0; j < E; ++j) bg[j] = Y[j];
+        }
+        w_inject_src<E>(w, bg, s, f, z + 1);
+      } else {
+        w_store<E>(w, ST + (size_t)(z + 1) * nxg, wu);  // T[z+1]
+        w_inject_rec<E>(w, wu, s, bin, z + 1, bins);
+      }
+    }
   }
   cp_wait0();
   __syncthreads();  // the down sweep's images are out of the slots; the ring is idle
   // ---------------- up sweep: bu (Up of R bg) and wd (Down^H of rec + conj(R) wu)
-  float2 bu[E], wd[E], t[E];
+  float2 bu[E], wd[E];
   const bool keep_last = !compat || (c.ext ? (s == c.ns - 1) : (f == c.nfreq - 1));
-  ring.issue(nz - 1);
-  cp_commit();
-  ring.issue(nz - 2);
-  cp_commit();
-  if (act && lane == 0) {
-    l2_prefetch(SBG + (size_t)(nz - 2) * nxg, nxg * 8);
-    l2_prefetch(ST + (size_t)(nz - 2) * nxg, nxg * 8);
-  }
 #pragma unroll
   for (int j = 0; j < E; ++j) {
     bool in;
-    const int x = xclamp(c, lane, j, in);
+    const int x = xclamp(w, j, in);
     if (in) slot[x] = zero;
   }
-  for (int z = nz - 1; z >= 0; --z) {
+  ring.issue(nz - 1);
+  cp_commit();
+  for (int z = nz; z >= 1; --z) {
     __syncthreads();
     ring.issue(z - 2);
     cp_commit();
     cp_wait1();
     __syncthreads();
-    if (act && z == nz - 1) {
-      const float2* rc = ring.tabs(nz - 1).rc;
-      w_load<E>(c, lane, SBG + (size_t)(nz - 1) * nxg, bu);
-      w_load<E>(c, lane, ST + (size_t)(nz - 1) * nxg, t);
-      w_inject_rec<E>(w, t, s, bin, nz - 1, bins);  // wu[nz-1]
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        bool in;
-        const float2 r = rc[xclamp(c, lane, j, in)];
-        bu[j] = in ? c_mul(r, bu[j]) : zero;
-        wd[j] = in ? c_mulc(t[j], r) : zero;
+    if (act) {
+      const Tabs Tp = ring.tabs(z - 1);
+      const float2* bgp = SBG + (size_t)(z - 1) * nxg;
+      const float2* tp = ST + (size_t)(z - 1) * nxg;
+      if (lane == 0 && z >= 2) {
+        l2_prefetch(SBG + (size_t)(z - 2) * nxg, nxg * 8);
+        l2_prefetch(ST + (size_t)(z - 2) * nxg, nxg * 8);
       }
-      w_inject_rec<E>(w, wd, s, bin, nz - 1, bins);
-    }
-    // LinUp^H at depth z: conj(bu) Sc^H_z T[z]
-    if (act && z >= 1 && (z < nz - 1 || keep_last)) {
-      w_load<E>(c, lane, ST + (size_t)z * nxg, t);
-      w_scatter<E>(w, ring.tabs(z), om, scmode, t, t);
+      if (z == nz) {
+        // bu[nz-1] = R bg[nz-1]; wd[nz-1] = conj(R) (T[nz-1] + rec) + rec
+        w_load<E>(w, bgp, bu);
+        w_load<E>(w, tp, X);
+        w_inject_rec<E>(w, X, s, bin, nz - 1, bins);
 #pragma unroll
-      for (int j = 0; j < E; ++j) {
-        bool in;
-        const int x = xclamp(c, lane, j, in);
-        if (in) slot[x] = c_add(slot[x], c_mulc(t[j], bu[j]));
+        for (int j = 0; j < E; ++j) {
+          bool in;
+          const float2 r = Tp.rc[xclamp(w, j, in)];
+          bu[j] = in ? c_mul(r, bu[j]) : zero;
+          wd[j] = in ? c_mulc(X[j], r) : zero;
+        }
+        w_inject_rec<E>(w, wd, s, bin, nz - 1, bins);
+      }
+#pragma unroll 1
+      for (int k = 0; k < 4; ++k) {
+        // k: 0 B, 1 C, 2 D, 3 A
+        const bool on = k < 2 ? (z < nz) : (k == 2 ? (z < nz && z >= 2) : (z >= 2 && (z < nz || keep_last)));
+        if (!on) continue;
+        const bool step = (k == 0 || k == 2);
+        const Tabs T = k == 2 ? ring.tabs(z) : Tp;
+        const int nj = step ? nj_step : 1;
+#pragma unroll 1
+        for (int jr = 0; jr < nj; ++jr) {
+          // pre
+          if (k == 0) {
+            adj_pre<E, MR>(w, T, jr, wd, X);
+          } else if (k == 2) {
+#pragma unroll
+            for (int j = 0; j < E; ++j) X[j] = bu[j];
+          } else if (t1) {
+            if (k == 1) {
+              sc_pre<E>(w, T, scmode, wd, X);
+            } else {
+              w_load<E>(w, tp, X);
+              if (scmode == 2) sc_pre<E>(w, T, scmode, X, X);
+            }
+          }
+          if (step || t1) {
+            wfft<E, false>(X, w.sb, w.tw, lane);
+            if (k == 0) {
+              if (!adj_mid<E, MR>(w, T, jr, X, Y)) continue;
+            } else if (k == 2) {
+              fwd_mid<E>(w, T, jr, X);
+            } else {
+              sc_mid<E>(w, om, X);
+            }
+            wfft<E, true>(X, w.sb, w.tw, lane);
+          }
+          // post
+          if (k == 0) {
+            adj_post<E>(w, X, wd);  // wd holds q
+          } else if (k == 2) {
+            if constexpr (MR) fwd_post<E, true>(w, T, jr, X, Y);
+            else fwd_post<E, false>(w, T, jr, X, bu);
+          } else if (k == 1) {
+            // LinDown^H: slot = conj(bg[z-1]) Sc^H_{z-1} q
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              bool in;
+              const int x = xclamp(w, j, in);
+              const float2 k0 = T.c0[x], k1 = t1 ? T.c1[x] : zero, b = bgp[x];
+              const float2 v = sc_val(iw, scmode, t1, k0, k1, wd[j], X[j]);
+              if (in) slot[x] = c_mulc(v, b);
+            }
+          } else {
+            // LinUp^H: slot += conj(bu[z-1]) Sc^H_{z-1} T[z-1]
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              bool in;
+              const int x = xclamp(w, j, in);
+              const float2 k0 = T.c0[x], k1 = t1 ? T.c1[x] : zero, u = tp[x];
+              const float2 v = sc_val(iw, scmode, t1, k0, k1, u, X[j]);
+              if (in) slot[x] = c_add(slot[x], c_mulc(v, bu[j]));
+            }
+          }
+        }
+        if (k == 1 && z >= 2) {
+          // wd[z-1] = q + rec + conj(R[z-1]) (T[z-1] + rec)
+          w_load<E>(w, tp, X);
+          w_inject_rec<E>(w, X, s, bin, z - 1, bins);
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            bool in;
+            const float2 r = T.rc[xclamp(w, j, in)];
+            if (in) wd[j] = c_add(wd[j], c_mulc(X[j], r));
+          }
+          w_inject_rec<E>(w, wd, s, bin, z - 1, bins);
+        } else if (k == 2) {
+          // bu[z-1] = P_z bu + R[z-1] bg[z-1]
+          if constexpr (MR) {
+#pragma unroll
+            for (int j = 0; j < E; ++j) bu[j] = Y[j];
+          }
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            bool in;
+            const int x = xclamp(w, j, in);
+            const float2 r = Tp.rc[x], b = bgp[x];
+            if (in) bu[j] = c_add(bu[j], c_mul(r, b));
+          }
+        }
       }
     }
     __syncthreads();
-    reduce_slots(sm.slots, nxg, kW, IS + (size_t)z * nxg);
-    __syncthreads();
-    if (z == 0) break;
-    if (!act) continue;  // the slot of an idle warp stays zero
-    if (lane == 0 && z >= 2) {
-      l2_prefetch(SBG + (size_t)(z - 2) * nxg, nxg * 8);
-      l2_prefetch(ST + (size_t)(z - 2) * nxg, nxg * 8);
-    }
-    const Tabs Tz = ring.tabs(z), Tp = ring.tabs(z - 1);
-    // q = P^H_{z-1} wd;  LinDown^H: conj(bg[z-1]) Sc^H_{z-1} q
-    w_step_adj<E>(w, Tp, wd, wd);  // wd holds q
-    w_scatter<E>(w, Tp, om, scmode, wd, t);
-    const float2* bgp = SBG + (size_t)(z - 1) * nxg;
-    const float2* tp = ST + (size_t)(z - 1) * nxg;
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-      bool in;
-      const int x = xclamp(c, lane, j, in);
-      const float2 b = bgp[x];
-      if (in) slot[x] = c_mulc(t[j], b);
-    }
-    // wd[z-1] = q + rec + conj(R) (T[z-1] + rec)
-    w_load<E>(c, lane, tp, t);
-    w_inject_rec<E>(w, t, s, bin, z - 1, bins);
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-      bool in;
-      const float2 r = Tp.rc[xclamp(c, lane, j, in)];
-      if (in) wd[j] = c_add(wd[j], c_mulc(t[j], r));
-    }
-    w_inject_rec<E>(w, wd, s, bin, z - 1, bins);
-    // bu[z-1] = P_z bu + R[z-1] bg[z-1]
-    w_step_fwd<E>(w, Tz, bu, bu);
-#pragma unroll
-    for (int j = 0; j < E; ++j) {
-      bool in;
-      const int x = xclamp(c, lane, j, in);
-      const float2 r = Tp.rc[x], b = bgp[x];
-      if (in) bu[j] = c_add(bu[j], c_mul(r, b));
-    }
+    reduce_slots(sm.slots, nxg, kW, IS + (size_t)(z - 1) * nxg);
   }
   cp_wait0();
 }
 
-// ------------------------------------------------------ host side
-template <int E>
-size_t base_bytes(const DevCtx& c, bool slots) {
-  auto r16 = [](size_t b) { return (b + 15) & ~size_t(15); };
-  return r16((size_t)32 * E * 8) + r16((size_t)32 * E * 4) + r16((size_t)c.nxg * 4) +
-         r16((size_t)kW * wbuf_len<E>() * 8) + (slots ? r16((size_t)kW * c.nxg * 8) : 0);
+// Born adjoint with the two chains of a row on two warps (single reference).
+// Warp 2r is the source side of row r (down: bg; up: bu and LinUp^H), warp
+// 2r + 1 the receiver side (down: wu, whose steps are the stored T; up: wd
+// and LinDown^H).  Within a depth the chains meet only in the image, so each
+// warp holds one state row plus the register row of its transform, and the
+// CTA runs 16 warps.  A warp writes its image contribution into its own
+// exchange buffer after its last transform of the depth; after the depth's
+// barrier the CTA sums the buffers of its rows in row order (deterministic).
+// Two barriers per depth: the ring's copies are issued at the top of a depth
+// and waited for at its end.
+template <int E, bool NT, int R>
+__global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayout L, const Group* groups,
+                                                              float2* storeBG, float2* storeT, const float2* bins,
+                                                              float2* imgR, float2* imgS, int compat) {
+  const Carve<E> sm(c, L, false, 2 * R);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = warp >> 1;
+  const bool recv = warp & 1;
+  stage_static<E>(c, sm);
+  const int nxg = c.nxg, nz = c.nz;
+  const Group gp = groups[blockIdx.x];
+  const int nrows = gp.n;
+  const bool act = row < nrows;
+  float2* xb = sm.sb0 + warp * wbuf_len<E>();
+  const WRow w{c, sm.tw, xb, sm.taperN, sm.kx, lane, NT ? 0 : c.tap, NT ? 32 * E : c.nxg};
+  const int f = gp.f, s = gp.s0 + (act ? row : 0), bin = c.bin[f];
+  const size_t plane = (size_t)nz * nxg;
+  float2* SBG = storeBG + (size_t)(gp.row0 + (act ? row : 0)) * plane;
+  float2* ST = storeT + (size_t)(gp.row0 + (act ? row : 0)) * plane;
+  float2* IR = imgR + (size_t)blockIdx.x * plane;
+  float2* IS = imgS + (size_t)blockIdx.x * plane;
+  const int scmode = compat ? 1 : 2;
+  const float om = c.omega[f];
+  const float2 iw = sc_iw(c, om, scmode);
+  const bool t1 = c.ntaylor >= 1;
+  const float2 zero = make_float2(0.f, 0.f);
+  const Ring ring{c, L, sm.ring, Src{nullptr, nullptr}, f};
+  const float2* xb0 = sm.sb0;
+  constexpr int WB = wbuf_len<E>();
+  float2 S[E], X[E], Yd[1];
+
+  // this warp's row into its buffer (grid points)
+  auto put = [&](const float2 (&v)[E]) {
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      bool in;
+      const int x = xclamp(w, j, in);
+      if (in) xb[x] = v[j];
+    }
+  };
+  auto put_zero = [&]() {
+    for (int x = lane; x < nxg; x += 32) xb[x] = zero;
+  };
+
+  // ---------------- down sweep: bg (source side), wu (receiver side)
+  w_zero<E>(S);
+  if (act) {
+    if (!recv) {
+      w_inject_src<E>(w, S, s, f, 0);
+      w_store<E>(w, SBG, S);
+    } else {
+      w_inject_rec<E>(w, S, s, bin, 0, bins);
+      for (int x = lane; x < nxg; x += 32) ST[x] = zero;  // T[0] = 0
+    }
+    put(S);
+  }
+  ring.issue(0);
+  ring.issue(1);
+  cp_commit();
+  cp_wait0();
+  __syncthreads();
+  // IR[z] = sum over rows of wu[z] conj(bg[z])
+  auto reduce_down = [&](float2* out) {
+    for (int x = threadIdx.x; x < nxg; x += blockDim.x) {
+      float2 a = zero;
+      for (int r = 0; r < nrows; ++r) a = c_add(a, c_mulc(xb0[(2 * r + 1) * WB + x], xb0[2 * r * WB + x]));
+      out[x] = a;
+    }
+  };
+  reduce_down(IR);
+  for (int z = 0; z + 1 < nz; ++z) {
+    __syncthreads();  // the buffers are summed; slot (z + 2) % 3 is free
+    ring.issue(z + 2);
+    cp_commit();
+    if (act) {
+      // source side: bg[z+1] = P_z bg + src; receiver side: T[z+1] = P^H_{z+1} wu
+      const Tabs T = ring.stabs(recv ? z + 1 : z);
+      if (!recv) {
+#pragma unroll
+        for (int j = 0; j < E; ++j) X[j] = S[j];
+      } else {
+        adj_pre<E, false>(w, T, 0, S, X);
+      }
+      wfft<E, false>(X, w.sb, w.tw, lane);
+      if (!recv) fwd_mid<E>(w, T, 0, X);
+      else adj_mid<E, false>(w, T, 0, X, Yd);
+      wfft<E, true>(X, w.sb, w.tw, lane);
+      if (!recv) {
+        fwd_post<E, false>(w, T, 0, X, S);
+        w_inject_src<E>(w, S, s, f, z + 1);
+        w_store<E>(w, SBG + (size_t)(z + 1) * nxg, S);
+      } else {
+        adj_post<E>(w, X, S);
+        w_store<E>(w, ST + (size_t)(z + 1) * nxg, S);
+        w_inject_rec<E>(w, S, s, bin, z + 1, bins);
+      }
+      put(S);
+    }
+    cp_wait0();
+    __syncthreads();
+    reduce_down(IR + (size_t)(z + 1) * nxg);
+  }
+
+  // ---------------- up sweep, iteration z = nz .. 1 builds image row z - 1
+  // source side: bu[z-1] = P_z bu + R[z-1] bg[z-1] (op 0), LinUp^H
+  // conj(bu[z-1]) Sc^H_{z-1} T[z-1] (op 1); receiver side: q = P^H_{z-1} wd
+  // (op 0), LinDown^H conj(bg[z-1]) Sc^H_{z-1} q (op 1), then
+  // wd[z-1] = q + rec + conj(R[z-1]) (T[z-1] + rec)
+  const bool keep_last = !compat || (c.ext ? (s == c.ns - 1) : (f == c.nfreq - 1));
+  __syncthreads();  // the down sweep's buffers are summed; the ring is idle
+  ring.issue(nz - 1);
+  cp_commit();
+  cp_wait0();
+  __syncthreads();
+  auto reduce_up = [&](float2* out) {
+    for (int x = threadIdx.x; x < nxg; x += blockDim.x) {
+      float2 a = zero;
+      for (int r = 0; r < nrows; ++r) a = c_add(a, c_add(xb0[2 * r * WB + x], xb0[(2 * r + 1) * WB + x]));
+      out[x] = a;
+    }
+  };
+  for (int z = nz; z >= 1; --z) {
+    if (z < nz) __syncthreads();  // the buffers are summed; slot (z - 2) % 3 is free
+    ring.issue(z - 2);
+    cp_commit();
+    if (act) {
+      const Tabs Tp = ring.stabs(z - 1);
+      const float2* bgp = SBG + (size_t)(z - 1) * nxg;
+      const float2* tp = ST + (size_t)(z - 1) * nxg;
+      if (z == nz) {
+        if (!recv) {
+          // bu[nz-1] = R bg[nz-1]
+          w_load<E>(w, bgp, S);
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            bool in;
+            const float2 r = Tp.rc[xclamp(w, j, in)];
+            S[j] = in ? c_mul(r, S[j]) : zero;
+          }
+        } else {
+          // wd[nz-1] = conj(R) (T[nz-1] + rec) + rec
+          w_load<E>(w, tp, X);
+          w_inject_rec<E>(w, X, s, bin, nz - 1, bins);
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            bool in;
+            const float2 r = Tp.rc[xclamp(w, j, in)];
+            S[j] = in ? c_mulc(X[j], r) : zero;
+          }
+          w_inject_rec<E>(w, S, s, bin, nz - 1, bins);
+        }
+      } else if (lane == 0 && !recv && z >= 2) {
+        l2_prefetch(SBG + (size_t)(z - 2) * nxg, nxg * 8);
+        l2_prefetch(ST + (size_t)(z - 2) * nxg, nxg * 8);
+      }
+      bool wrote = false;
+#pragma unroll 1
+      for (int k = 0; k < 2; ++k) {
+        const bool on = recv ? (z < nz) : (k == 0 ? (z < nz && z >= 2) : (z >= 2 && (z < nz || keep_last)));
+        if (!on) continue;
+        const bool step = k == 0;
+        const Tabs T = (step && !recv) ? ring.stabs(z) : Tp;
+        // pre
+        if (step) {
+          if (!recv) {
+#pragma unroll
+            for (int j = 0; j < E; ++j) X[j] = S[j];
+          } else {
+            adj_pre<E, false>(w, T, 0, S, X);
+          }
+        } else if (t1) {
+          if (!recv) {
+            w_load<E>(w, tp, X);
+            if (scmode == 2) sc_pre<E>(w, T, 2, X, X);
+          } else {
+            sc_pre<E>(w, T, scmode, S, X);
+          }
+        }
+        if (step || t1) {
+          wfft<E, false>(X, w.sb, w.tw, lane);
+          if (!step) sc_mid<E>(w, om, X);
+          else if (!recv) fwd_mid<E>(w, T, 0, X);
+          else adj_mid<E, false>(w, T, 0, X, Yd);
+          wfft<E, true>(X, w.sb, w.tw, lane);
+        }
+        // post
+        if (step) {
+          if (!recv) {
+            fwd_post<E, false>(w, T, 0, X, S);
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              bool in;
+              const int x = xclamp(w, j, in);
+              const float2 r = Tp.rc[x], b = bgp[x];
+              if (in) S[j] = c_add(S[j], c_mul(r, b));
+            }
+          } else {
+            adj_post<E>(w, X, S);  // S holds q
+          }
+        } else {
+          if (recv) {
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              bool in;
+              const int x = xclamp(w, j, in);
+              const float2 k0 = T.c0[x], k1 = t1 ? T.c1[x] : zero, b = bgp[x];
+              const float2 v = sc_val(iw, scmode, t1, k0, k1, S[j], X[j]);
+              if (in) xb[x] = c_mulc(v, b);
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              bool in;
+              const int x = xclamp(w, j, in);
+              const float2 k0 = T.c0[x], k1 = t1 ? T.c1[x] : zero, u = tp[x];
+              const float2 v = sc_val(iw, scmode, t1, k0, k1, u, X[j]);
+              if (in) xb[x] = c_mulc(v, S[j]);
+            }
+          }
+          wrote = true;
+          if (recv && z >= 2) {
+            w_load<E>(w, tp, X);
+            w_inject_rec<E>(w, X, s, bin, z - 1, bins);
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              bool in;
+              const float2 r = Tp.rc[xclamp(w, j, in)];
+              if (in) S[j] = c_add(S[j], c_mulc(X[j], r));
+            }
+            w_inject_rec<E>(w, S, s, bin, z - 1, bins);
+          }
+        }
+      }
+      if (!wrote) put_zero();
+    }
+    cp_wait0();
+    __syncthreads();
+    reduce_up(IS + (size_t)(z - 1) * nxg);
+  }
 }
 
-// which: 0 WEM, 1 Born forward, 2 Born adjoint.  Lays out the ring (and the
-// per-warp rows for WEM) and drops them when the shared memory does not fit.
+// ------------------------------------------------------ host side
+// which: 0 WEM, 1 Born forward, 2 Born adjoint (one warp per row), 3 Born
+// adjoint with the two chains of a row on two warps (kw_born_adj2)
+// rows per CTA of kw_born_adj2 (two warps per row: 16 warps at 128
+// registers; 8 rows measured faster than 6 rows at 168 registers)
+constexpr int kRowsAdj2 = 8;
+
+template <int E>
+size_t base_bytes(const DevCtx& c, int which) {
+  auto r16 = [](size_t b) { return (b + 15) & ~size_t(15); };
+  const int nbuf = which == 3 ? 2 * kRowsAdj2 : kW;
+  return r16((size_t)32 * E * 8) + r16((size_t)32 * E * 4) + r16((size_t)c.nxg * 4) +
+         r16((size_t)nbuf * wbuf_len<E>() * 8) + (which == 2 ? r16((size_t)kW * c.nxg * 8) : 0);
+}
+
+// Lays out the ring (and the per-warp rows for WEM) and drops them when the
+// shared memory does not fit.
 template <int E>
 SlotLayout slot_layout(const DevCtx& c, int which, int limit) {
   SlotLayout L{};
@@ -814,8 +1257,7 @@ SlotLayout slot_layout(const DevCtx& c, int which, int limit) {
   L.bytes = off;
   L.nslots = 3;
   L.row_bytes = which == 0 ? rowb : 0;
-  const bool slots = which == 2;
-  auto total = [&]() { return base_bytes<E>(c, slots) + (size_t)L.nslots * L.bytes + (size_t)2 * kW * L.row_bytes; };
+  auto total = [&]() { return base_bytes<E>(c, which) + (size_t)L.nslots * L.bytes + (size_t)2 * kW * L.row_bytes; };
   if (total() > (size_t)limit) L.row_bytes = 0;
   if (total() > (size_t)limit) {
     L = SlotLayout{};
@@ -826,47 +1268,100 @@ SlotLayout slot_layout(const DevCtx& c, int which, int limit) {
 
 template <int E>
 size_t smem_w(const DevCtx& c, int which, const SlotLayout& L) {
-  return base_bytes<E>(c, which == 2) + (size_t)L.nslots * L.bytes + (size_t)2 * kW * L.row_bytes;
+  return base_bytes<E>(c, which) + (size_t)L.nslots * L.bytes + (size_t)2 * kW * L.row_bytes;
 }
 
+// kw_born_adj2 serves this context: one reference, and its buffers, the
+// full ring and every table of a depth fit in shared memory
 template <int E>
-void launch_pass_w(int which, const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm,
-                   float2* s1, float2* s2, float2* bins, float2* ir, float2* is, int compat, cudaStream_t st) {
-  const int limit = max_smem_per_block();
-  const SlotLayout L = slot_layout<E>(c, which, limit);
-  const size_t sm = smem_w<E>(c, which, L);
-  if (which == 0) {
-    cudaFuncSetAttribute(kw_wem<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    kw_wem<E><<<ng, kW * 32, sm, st>>>(c, L, g, s1, bins);
-    note_launch();
-  } else if (which == 1) {
-    cudaFuncSetAttribute(kw_born_fwd<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    kw_born_fwd<E><<<ng, kW * 32, sm, st>>>(c, L, g, dm, drm, s1, s2, bins);
-    note_launch();
-  } else {
-    cudaFuncSetAttribute(kw_born_adj<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    kw_born_adj<E><<<ng, kW * 32, sm, st>>>(c, L, g, s1, s2, bins, ir, is, compat);
-    note_launch();
+bool adj2_fits(const DevCtx& c) {
+  if (c.nref != 1) return false;
+  const SlotLayout L3 = slot_layout<E>(c, 3, max_smem_per_block());
+  return L3.nslots == 3 && (c.fac || L3.ref >= 0);
+}
+// W_96 twiddles of this translation unit's copy of c_w96
+inline void init_w96() {
+  static bool init = false;
+  if (init) return;
+  float2 h[96];
+  for (int k = 0; k < 96; ++k) {
+    long double a = -2.0L * 3.14159265358979323846264338327950288L * k / 96;
+    h[k] = make_float2((float)std::cos(a), (float)std::sin(a));
   }
+  cudaMemcpyToSymbol(c_w96, h, sizeof(h));
+  init = true;
 }
 
 }  // namespace
 
-// one instantiation per translation unit (kw_e*.cu)
+// one kernel family per translation unit (kw_e<E>_<pass>.cu); each unit
+// fills its own copy of the W_96 table before its first launch
 template <int E>
-void launch_pass_w_e(int which, const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm,
-                     float2* s1, float2* s2, float2* bins, float2* ir, float2* is, int compat, cudaStream_t st) {
-  static bool init = false;
-  if (!init) {
-    float2 h[96];
-    for (int k = 0; k < 96; ++k) {
-      long double a = -2.0L * 3.14159265358979323846264338327950288L * k / 96;
-      h[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+void launch_wem_w(const DevCtx& c, const Group* g, int ng, float2* store, float2* bins, cudaStream_t st) {
+  init_w96();
+  const SlotLayout L = slot_layout<E>(c, 0, max_smem_per_block());
+  const size_t sm = smem_w<E>(c, 0, L);
+  auto go = [&](auto kern) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    kern<<<ng, kW * 32, sm, st>>>(c, L, g, store, bins);
+    note_launch();
+  };
+  if (c.nref > 1) go(kw_wem<E, true, false>);
+  else if (c.tap == 0) go(kw_wem<E, false, true>);
+  else go(kw_wem<E, false, false>);
+}
+
+template <int E>
+void launch_fwd_w(const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm, float2* sA,
+                  float2* sB, float2* bins, cudaStream_t st) {
+  init_w96();
+  const SlotLayout L = slot_layout<E>(c, 1, max_smem_per_block());
+  const size_t sm = smem_w<E>(c, 1, L);
+  auto go = [&](auto kern) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    kern<<<ng, kW * 32, sm, st>>>(c, L, g, dm, drm, sA, sB, bins);
+    note_launch();
+  };
+  if (c.nref > 1) go(kw_born_fwd<E, true>);
+  else go(kw_born_fwd<E, false>);
+}
+
+template <int E>
+void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* sT, float2* bins, float2* ir,
+                  float2* is, int compat, cudaStream_t st) {
+  init_w96();
+  const int limit = max_smem_per_block();
+  if (adj2_fits<E>(c)) {
+    // the two chains of a row on two warps, when their buffers, the full
+    // ring and every table of a depth fit
+    const SlotLayout L3 = slot_layout<E>(c, 3, limit);
+    {
+      const size_t sm3 = smem_w<E>(c, 3, L3);
+      auto go = [&](auto kern) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
+        kern<<<ng, 2 * kRowsAdj2 * 32, sm3, st>>>(c, L3, g, sBG, sT, bins, ir, is, compat);
+        note_launch();
+      };
+      if (c.tap == 0) go(kw_born_adj2<E, true, kRowsAdj2>);
+      else go(kw_born_adj2<E, false, kRowsAdj2>);
+      return;
     }
-    cudaMemcpyToSymbol(c_w96, h, sizeof(h));
-    init = true;
   }
-  launch_pass_w<E>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st);
+  const SlotLayout L = slot_layout<E>(c, 2, limit);
+  const size_t sm = smem_w<E>(c, 2, L);
+  auto go = [&](auto kern) {
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    kern<<<ng, kW * 32, sm, st>>>(c, L, g, sBG, sT, bins, ir, is, compat);
+    note_launch();
+  };
+  if (c.nref > 1) go(kw_born_adj<E, true>);
+  else go(kw_born_adj<E, false>);
+}
+
+// rows per CTA the Born adjoint launcher expects
+template <int E>
+int adj_rows_w(const DevCtx& c) {
+  return adj2_fits<E>(c) ? kRowsAdj2 : kW;
 }
 
 template <int E>

@@ -1,0 +1,8 @@
+// Warp-per-row Born adjoint pass kernels for N = 32 x 16 = 512.
+#include "kernels_w.cuh"
+
+namespace wg {
+template void launch_adj_w<16>(const DevCtx&, const Group*, int, float2*, float2*, float2*, float2*, float2*,
+                                int, cudaStream_t);
+template int adj_rows_w<16>(const DevCtx&);
+}  // namespace wg

@@ -1,0 +1,7 @@
+// Warp-per-row WEM pass kernels for N = 32 x 24 = 768.
+#include "kernels_w.cuh"
+
+namespace wg {
+template void launch_wem_w<24>(const DevCtx&, const Group*, int, float2*, float2*, cudaStream_t);
+template size_t smem_w_e<24>(const DevCtx&, bool);
+}  // namespace wg

@@ -1,0 +1,8 @@
+// Warp-per-row Born adjoint pass kernels for N = 32 x 8 = 256.
+#include "kernels_w.cuh"
+
+namespace wg {
+template void launch_adj_w<8>(const DevCtx&, const Group*, int, float2*, float2*, float2*, float2*, float2*,
+                                int, cudaStream_t);
+template int adj_rows_w<8>(const DevCtx&);
+}  // namespace wg

@@ -13,7 +13,14 @@
 // In-register DFTs are unrolled mixed-radix decompositions with compile-time
 // indices; their twiddles W_R^k (R | 96) come from a 96-entry table in
 // constant memory, computed in double on the host.  Inter-stage twiddles
-// W_N^(r l N/(L R)) come from an N-entry table staged in shared memory.
+// W_N^(r l N/(L R)) come from a table in shared memory laid out per stage as
+// [r - 1][l] (stage s >= 1 holds (R_s - 1) L_s entries; all stages together
+// N - E), so the 32 lanes of a twiddle load read consecutive l.
+//
+// Shared-memory banks: the exchange buffer pads one slot every 2^k points
+// (k = 4 for E = 8, 16; k = 5 for E = 12, 24, 32), chosen by counting the
+// wavefronts of every exchange write and read of each plan; the natural-order
+// reads stay conflict-free and fold the padding into immediate offsets.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -107,21 +114,41 @@ struct WPlan<32> {
   __host__ __device__ static constexpr int r(int) { return 32; }
 };
 
-// padded index of the exchange buffer (one pad slot per 16 points keeps the
-// natural-order reads conflict-free and spreads the strided writes)
-__device__ __forceinline__ int swz(int i) { return i + (i >> 4); }
+// padded index of the exchange buffer: one pad slot per 2^k points
+template <int E>
+__host__ __device__ constexpr int swz_shift() {
+  return (E == 8 || E == 16) ? 4 : 5;
+}
+template <int E>
+__device__ __forceinline__ int swz(int i) {
+  return i + (i >> swz_shift<E>());
+}
 template <int E>
 __host__ __device__ constexpr int wbuf_len() {
-  return 32 * E + (32 * E) / 16 + 2;
+  return 32 * E + ((32 * E) >> swz_shift<E>()) + 2;
+}
+
+// offset of stage S's twiddles in the per-stage table: sum over 1 <= s < S of
+// (R_s - 1) L_s, with L_s the product of the radices before s
+template <int E>
+__host__ __device__ constexpr int tw_offset(int S) {
+  int off = 0, L = WPlan<E>::r(0);
+  for (int s = 1; s < S; ++s) {
+    off += (WPlan<E>::r(s) - 1) * L;
+    L *= WPlan<E>::r(s);
+  }
+  return off;
+}
+template <int E>
+__host__ __device__ constexpr int tw_entries() {
+  return tw_offset<E>(WPlan<E>::n);
 }
 
 template <int E, bool INV, int S, int L>
 __device__ __forceinline__ void wfft_stage(float2 (&v)[E], float2* sb, const float2* tw, int lane) {
   constexpr int R = WPlan<E>::r(S);
   constexpr int M = E / R;
-  constexpr int N = 32 * E;
   constexpr bool LAST = (S == WPlan<E>::n - 1);
-  constexpr int TWS = N / (L * R);
 #pragma unroll
   for (int m = 0; m < M; ++m) {
     const int b = lane + 32 * m;
@@ -131,7 +158,7 @@ __device__ __forceinline__ void wfft_stage(float2 (&v)[E], float2* sb, const flo
     for (int r = 0; r < R; ++r) {
       float2 x = v[m + r * M];
       if (L > 1 && r > 0) {
-        float2 w = tw[r * l * TWS];
+        float2 w = tw[tw_offset<E>(S) + (r - 1) * L + l];
         x = INV ? c_mulc(x, w) : c_mul(x, w);
       }
       a[r] = x;
@@ -143,13 +170,13 @@ __device__ __forceinline__ void wfft_stage(float2 (&v)[E], float2* sb, const flo
     } else {
       const int o = (b - l) * R + l;
 #pragma unroll
-      for (int q = 0; q < R; ++q) sb[swz(o + q * L)] = a[q];
+      for (int q = 0; q < R; ++q) sb[swz<E>(o + q * L)] = a[q];
     }
   }
   if constexpr (!LAST) {
     __syncwarp();
 #pragma unroll
-    for (int j = 0; j < E; ++j) v[j] = sb[swz(lane + 32 * j)];
+    for (int j = 0; j < E; ++j) v[j] = sb[swz<E>(lane + 32 * j)];
     __syncwarp();
     wfft_stage<E, INV, S + 1, L * R>(v, sb, tw, lane);
   }
