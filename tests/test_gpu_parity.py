@@ -277,6 +277,26 @@ def test_born_adjoint_many_shots(gpu_lib, oracle, case):
     assert rel_l2(a1, q1) < TOL_OP, rel_l2(a1, q1)
 
 
+@pytest.mark.parametrize("case", ["n256", "n768t0"])
+def test_shaped_tail(gpu_lib, oracle, case):
+    """17 shots x 66 frequencies: 198 groups of up to 8 shots, more than one
+    wave of CTAs, so the launch takes the shaped tail (the last frequencies in
+    groups of 1-2 shots)."""
+    from wemgpu.core import BornOp, WemOp
+    p, par, wav, s, rho = small_case(nz=6, ns=17, nt=1024, **WARP_CASES[case])
+    d = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    WemOp(p, wav).forward(s, rho, d)
+    o = oracle.wem_forward(p, wav, s, rho, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(d, o) < TOL_OP, ("wem", rel_l2(d, o))
+    op = BornOp(p, wav, s, rho)
+    dd = (np.random.default_rng(14).random((p.ns, p.nr, p.nt)) - .5).astype(np.float32)
+    a0, a1 = np.zeros_like(s), np.zeros_like(s)
+    op.adjoint(a0, a1, dd)
+    q0, q1 = oracle.born_adjoint(p, wav, s, rho, dd, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(a0, q0) < TOL_OP, rel_l2(a0, q0)
+    assert rel_l2(a1, q1) < TOL_OP, rel_l2(a1, q1)
+
+
 @pytest.mark.parametrize("case", ["n256", "n768", "n768t0"])
 def test_warp_path_is_deterministic(gpu_lib, case):
     from wemgpu.core import BornOp

@@ -204,7 +204,7 @@ class Engine {
       if (wp) timed("k_wem", [&] { launch_pass_warp(0, ctx_, gd, ng, nullptr, nullptr, A, nullptr, bins, nullptr, nullptr, 0, 0); });
       else timed("k_wem", [&] { launch_wem(ctx_, gd, ng, G, A, bins, 0); });
       cuda_check(cudaGetLastError(), "k_wem launch");
-    });
+    }, wp);
     emit(data, kind, add);
   }
 
@@ -226,7 +226,7 @@ class Engine {
       if (wp) timed("k_born_fwd", [&] { launch_pass_warp(1, ctx_, gd, ng, dm0, drm, A, B, bins, nullptr, nullptr, 0, 0); });
       else timed("k_born_fwd", [&] { launch_born_fwd(ctx_, gd, ng, G, dm0, drm, A, B, bins, 0); });
       cuda_check(cudaGetLastError(), "k_born_fwd launch");
-    });
+    }, wp);
     emit(data, kind, add);
   }
 
@@ -268,7 +268,7 @@ class Engine {
       launch_reduce_images(pr, dbeg, M_, plane, IR, 0);
       launch_reduce_images(ps, dbeg, M_, plane, IS, 0);
       cuda_check(cudaGetLastError(), "reduce launch");
-    });
+    }, wp);
     const size_t nm = (size_t)M_ * p_.nz * p_.nx;
     Staged o0, o1;
     o0.out(ds2, nm * 8, add != 0);
@@ -431,18 +431,59 @@ class Engine {
     return G;
   }
 
-  // groups of up to G shots of one frequency, sorted by frequency, run in
-  // chunks whose storage fits the memory budget
-  template <class F>
-  void for_chunks(int G, size_t bytes_per_row, F run) {
+  // split the ns shots of frequency f into q groups of near-equal size
+  void split_shots(std::vector<Group>& out, int f, int q) const {
+    const int ns = geo_.ns, base = ns / q, extra = ns % q;
+    for (int i = 0, s0 = 0; i < q; ++i) {
+      const int n = base + (i < extra ? 1 : 0);
+      out.push_back(Group{f, s0, n, 0});
+      s0 += n;
+    }
+  }
+
+  // Groups of one launch whose CTAs run one per SM.  With full groups of G
+  // the last wave would hold only NG mod SMs CTAs of full length; instead the
+  // frequencies that fill whole waves keep full groups and the remaining
+  // frequencies are split into smaller groups that together fill one wave,
+  // placed last in the grid, so the tail is a wave of shorter CTAs.
+  std::vector<Group> shaped_groups(int G) const {
+    int sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int ns = geo_.ns, gpf = (ns + G - 1) / G;
+    const long long ng = (long long)F_ * gpf;
     std::vector<Group> all;
-    for (int f = 0; f < F_; ++f)
-      for (int s0 = 0; s0 < geo_.ns; s0 += G) all.push_back(Group{f, s0, std::min(G, geo_.ns - s0), 0});
+    const long long waves = sms > 0 ? ng / sms : 0;
+    const int ff = waves > 0 ? (int)std::min<long long>(F_, waves * sms / gpf) : F_;
+    const int fr = F_ - ff;
+    const int q = fr > 0 ? std::min(ns, sms / fr) : 0;
+    if (fr == 0 || ng % sms == 0 || q <= gpf) {
+      for (int f = 0; f < F_; ++f)
+        for (int s0 = 0; s0 < ns; s0 += G) all.push_back(Group{f, s0, std::min(G, ns - s0), 0});
+      return all;
+    }
+    for (int f = 0; f < ff; ++f) split_shots(all, f, gpf);
+    for (int f = ff; f < F_; ++f) split_shots(all, f, q);
+    return all;
+  }
+
+  // groups of up to G shots of one frequency, sorted by frequency, run in
+  // chunks whose storage fits the memory budget; a pass that fits one launch
+  // of the warp kernels gets the shaped tail of shaped_groups
+  template <class F>
+  void for_chunks(int G, size_t bytes_per_row, F run, bool shape = false) {
     size_t freeb = 0, totalb = 0;
     cuda_check(cudaMemGetInfo(&freeb, &totalb), "cudaMemGetInfo");
     size_t budget = std::min<size_t>((size_t)(0.6 * (double)freeb), (size_t)96 << 30);
     size_t max_rows = std::max<size_t>(G, budget / std::max<size_t>(bytes_per_row, 1));
     if (g_plain) max_rows = 1;  // one row per launch
+    std::vector<Group> all;
+    if (shape && !g_plain && (size_t)F_ * geo_.ns <= max_rows) {
+      all = shaped_groups(G);
+    } else {
+      for (int f = 0; f < F_; ++f)
+        for (int s0 = 0; s0 < geo_.ns; s0 += G) all.push_back(Group{f, s0, std::min(G, geo_.ns - s0), 0});
+    }
     size_t i = 0;
     while (i < all.size()) {
       std::vector<Group> chunk;

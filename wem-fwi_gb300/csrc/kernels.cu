@@ -657,28 +657,37 @@ __global__ void __launch_bounds__(kThreads) k_oneway(DevCtx c, int f, int up, in
 // ------------------------------------------------------------- tables
 // phase_shift.ispc:2-16: a = w^2 s_re - k^2, b = w^2 (s_im - eps s_re),
 // c = |a + ib|, re = sqrt((c+a)/2), im = -sqrt((c-a)/2),
-// factor = exp(im dz) exp(-i re dz).  The square-root chain runs in double.
+// factor = exp(im dz) exp(-i re dz).
+// FP32 with the cancellation-free form of the complex square root: the part
+// whose square root is taken of c + |a| comes first, the other is |b| / (2
+// that part), so neither c - a (a > 0) nor c + a (a < 0) is formed.  One CTA
+// row per (frequency, depth, reference) table row, threads over the N points.
 __global__ void k_phase(DevCtx c, const float2* sref, float eps, float2* ph) {
-  const size_t total = (size_t)c.nfreq * c.nz * c.nref * c.N;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-    int n = (int)(i % c.N);
-    size_t t = i / c.N;
-    int j = (int)(t % c.nref);
-    t /= c.nref;
-    int z = (int)(t % c.nz);
-    int f = (int)(t / c.nz);
-    int m = c.ext ? f : 0;
-    float2 s = sref[((size_t)m * c.nz + z) * c.nref + j];
-    double w = c.omega[f], k = c.kx[n];
-    double a = w * w * (double)s.x - k * k;
-    double b = w * w * ((double)s.y - (double)eps * (double)s.x);
-    double cc = sqrt(a * a + b * b);
-    double re = sqrt(fmax((cc + a) * 0.5, 0.0));
-    double im = -sqrt(fmax((cc - a) * 0.5, 0.0));
-    float e = expf((float)(im * c.dz));
+  const int nrow = c.nfreq * c.nz * c.nref;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= c.N) return;
+  const float k = c.kx[n];
+  for (int r = blockIdx.y; r < nrow; r += gridDim.y) {
+    const int j = r % c.nref, z = (r / c.nref) % c.nz, f = r / (c.nref * c.nz);
+    const int m = c.ext ? f : 0;
+    const float2 s = sref[((size_t)m * c.nz + z) * c.nref + j];
+    const float w = c.omega[f], w2 = w * w;
+    const float a = fmaf(w2, s.x, -k * k);
+    const float b = w2 * fmaf(-eps, s.x, s.y);
+    const float cc = sqrtf(fmaf(a, a, b * b));
+    float re, im;
+    if (a >= 0.f) {
+      re = sqrtf(0.5f * (cc + a));
+      im = re > 0.f ? -fabsf(b) / (2.f * re) : 0.f;
+    } else {
+      const float q = sqrtf(0.5f * (cc - a));
+      im = -q;
+      re = fabsf(b) / (2.f * q);
+    }
+    const float e = expf(im * c.dz);
     float sn, cs;
-    sincosf((float)(re * c.dz), &sn, &cs);
-    ph[i] = make_float2(e * cs, -e * sn);
+    sincosf(re * c.dz, &sn, &cs);
+    ph[(size_t)r * c.N + n] = make_float2(e * cs, -e * sn);
   }
 }
 
@@ -868,8 +877,9 @@ size_t smem_born_adj(const DevCtx& c, int G) {
 size_t smem_rows(const DevCtx& c, int G) { return 8 * (al(c.N) + fft_bufs(c, G, true) + 2 * al((size_t)G * c.nxg)); }
 
 void launch_phase_tables(const DevCtx& c, const float2* sref, float eps, float2* ph, cudaStream_t st) {
-  size_t n = (size_t)c.nfreq * c.nz * c.nref * c.N;
-  k_phase<<<grid_for(n), 256, 0, st>>>(c, sref, eps, ph);
+  const int nrow = c.nfreq * c.nz * c.nref;
+  const dim3 grid((c.N + 255) / 256, nrow < 65535 ? nrow : 65535);
+  k_phase<<<grid, 256, 0, st>>>(c, sref, eps, ph);
   note_launch();
 }
 
