@@ -61,6 +61,13 @@ enum { WEM_ADJ_COMPAT = 0, WEM_ADJ_EXACT = 1 };
  * NEAREST is the textbook nearest-reference partition. */
 enum { WEM_REFS_ASCODED = 0, WEM_REFS_NEAREST = 1 };
 
+/* phase law of the phase shift (kernel of Phshift, a1).
+ * ISPC is the propagator's law (phase_shift.ispc:2-32): re/im of the damped
+ * square root of w^2 (s - i eps Re s) - k^2.  EXACT_KZ is the law of the
+ * older extPropagator (extPropagator/src/Phshift.cpp:41-126): forward factor
+ * exp(-i dz conj(kz)), kz = sqrt(w^2 s - k^2 + 1e-5 i), on the same k grid. */
+enum { WEM_PHASE_ISPC = 0, WEM_PHASE_EXACT_KZ = 1 };
+
 /* data representation of a call */
 enum { WEM_DATA_TIME = 0,    /* float  [ns][nr][nt]                         */
        WEM_DATA_FREQ = 1 };  /* complex [ns][nr][nbin] (nbin >= nt + tpad) */
@@ -98,6 +105,7 @@ typedef struct wem_params {
   int   adjoint_mode;  /* WEM_ADJ_COMPAT (default) | WEM_ADJ_EXACT */
   int   refs_mode;     /* WEM_REFS_ASCODED (default) | WEM_REFS_NEAREST */
   int   nbin;          /* bins of WEM_DATA_FREQ data; 0 = nt + tpad */
+  int   phase_law;     /* WEM_PHASE_ISPC (default) | WEM_PHASE_EXACT_KZ */
 } wem_params;
 
 void wem_params_default(wem_params* p);

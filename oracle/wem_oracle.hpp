@@ -303,6 +303,7 @@ template <class R>
 struct Core {
   int nxg = 0, nz = 0, N = 0, tap = 0, pad = 0, nref = 1, prop = WEM_PROP_SSF, ntaylor = 1;
   R dx = 1, dz = 1, eps = 0.04f;
+  int law = WEM_PHASE_ISPC;
   const C<R>* slow = nullptr;  // [nz][nxg], owned by the caller
   RefSampler<R> refs;
   std::vector<R> k;      // Phshift k grid, propagator/src/Phshift_cmplx.cpp:13,21-24
@@ -311,7 +312,7 @@ struct Core {
 
   Core(const wem_params& p, const C<R>* s, int nxg_, int nz_)
       : nxg(nxg_), nz(nz_), N(nxg_ + 2 * p.tap), tap(p.tap), pad(p.pad), nref(p.nref),
-        prop(p.prop), ntaylor(p.ntaylor), dx(p.dx), dz(p.dz), eps(p.eps), slow(s),
+        prop(p.prop), ntaylor(p.ntaylor), dx(p.dx), dz(p.dz), eps(p.eps), law(p.phase_law), slow(s),
         refs(s, nxg_, nz_, p.nref, p.refs_mode), fft(nxg_ + 2 * p.tap) {
     check(p.ntaylor >= 0 && p.ntaylor <= 4, "ntaylor must be in [0,4]");
     k.assign(N, R(0));
@@ -335,8 +336,16 @@ struct Work {
 };
 
 // phase_shift.ispc:2-16 (ps_fwd) / :18-32 (ps_adj): one k bin.
+// law WEM_PHASE_EXACT_KZ: extPropagator/src/Phshift.cpp:59,81, forward factor
+// exp(-i dz kz) with kz = conj(sqrt(w^2 s - k^2 + i 1e-5)) (complex s; the
+// reference's s there is real).
 template <class R>
-inline C<R> ps_factor(R w, R k, R dz, C<R> s, R eps) {
+inline C<R> ps_factor(R w, R k, R dz, C<R> s, R eps, int law = WEM_PHASE_ISPC) {
+  if (law == WEM_PHASE_EXACT_KZ) {
+    const C<R> I(0, 1);
+    C<R> kz = std::conj(std::sqrt(w * w * s - k * k + I * R(1e-5)));
+    return std::exp(-I * dz * kz);
+  }
   R a = w * w * s.real() - k * k;
   R b = w * w * (s.imag() - eps * s.real());
   R c = std::sqrt(a * a + b * b);
@@ -372,7 +381,7 @@ void onestep_fwd(const Core<R>& c, int iz, R w, const C<R>* model, C<R>* data, b
   fft_unitary(c, mp, -1, wk);
   for (int j = 0; j < c.nref; ++j) {
     C<R> sr = c.refs.sref[(size_t)iz * c.nref + j];
-    for (int ik = 0; ik < N; ++ik) wp[ik] = mp[ik] * ps_factor(w, c.k[ik], c.dz, sr, c.eps);
+    for (int ik = 0; ik < N; ++ik) wp[ik] = mp[ik] * ps_factor(w, c.k[ik], c.dz, sr, c.eps, c.law);
     fft_unitary(c, wp, +1, wk);
     for (int i = 0; i < nxg; ++i) wr[i] = wp[i + tap] * c.taper[i];
     const std::vector<int>& loc = c.refs.loc[(size_t)iz * c.nref + j];
@@ -416,7 +425,7 @@ void onestep_adj(const Core<R>& c, int iz, R w, C<R>* model, const C<R>* data, b
     std::fill(wp, wp + N, C<R>(0));
     for (int i = 0; i < nxg; ++i) wp[i + tap] = wr[i];
     fft_unitary(c, wp, -1, wk);
-    for (int ik = 0; ik < N; ++ik) mp[ik] += wp[ik] * std::conj(ps_factor(w, c.k[ik], c.dz, sr, c.eps));
+    for (int ik = 0; ik < N; ++ik) mp[ik] += wp[ik] * std::conj(ps_factor(w, c.k[ik], c.dz, sr, c.eps, c.law));
   }
   fft_unitary(c, mp, +1, wk);
   for (int i = 0; i < nxg; ++i) out[i] += mp[i + tap];

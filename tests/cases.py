@@ -32,11 +32,12 @@ def layered_model(nz, nx, seed=0, v0=1500.0, v1=3500.0, noise=0.05, sigma=4, q=1
 
 
 def small_case(prop="ssf", nref=1, nx=52, nz=24, ns=3, tap=6, pad=4, ntaylor=1, adjoint_mode="compat",
-               seed=0, nt=128, dt=0.008, fmin=6.0, fmax=14.0, ngs=2, ngr=1, eps=0.04):
+               seed=0, nt=128, dt=0.008, fmin=6.0, fmax=14.0, ngs=2, ngr=1, eps=0.04, phase_law="ispc"):
     s, rho = layered_model(nz, nx, seed)
     par = dict(ns=ns, osx=10.0 * (nx // (ns + 1)), dsx=10.0 * (nx // (ns + 1)), osz=0.0,
                nr=nx, orx=0.0, drx=10.0, orz=0.0, eps=eps, prop=prop, nref=nref, tap=tap, pad=pad,
-               fmin=fmin, fmax=fmax, ngs=ngs, ngr=ngr, ntaylor=ntaylor, adjoint_mode=adjoint_mode)
+               fmin=fmin, fmax=fmax, ngs=ngs, ngr=ngr, ntaylor=ntaylor, adjoint_mode=adjoint_mode,
+               phase_law=phase_law)
     p = make_params(par, nx=nx, nz=nz, dx=10.0, dz=10.0, nt=nt, dt=dt)
     wav = ricker(nt, dt, 10.0)
     return p, par, wav, s, rho

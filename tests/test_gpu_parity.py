@@ -321,3 +321,28 @@ def test_refsampler_history_exhausted(gpu_lib, oracle):
     WemOp(p, wav).forward(s, rho, d)
     o = oracle.wem_forward(p, wav, s, rho, kind=WEM_DATA_TIME, prec=64)
     assert rel_l2(d, o) < TOL_OP, rel_l2(d, o)
+
+
+@pytest.mark.parametrize("case", ["small", "n768t0"])
+def test_exact_kz_phase_law(gpu_lib, oracle, case):
+    """phase_law exact_kz (extPropagator/src/Phshift.cpp:41-126) through a
+    depth step, the modelling and the Born adjoint."""
+    from wemgpu.core import BornOp, RowOps, WemOp
+    kw = {} if case == "small" else dict(WARP_CASES[case])
+    p, par, wav, s, rho = small_case(nz=12, ns=2, phase_law="exact_kz", **kw)
+    sp = pad_edge(s, p.pad)
+    x = rand_c(np.random.default_rng(15), (3, sp.shape[1]))
+    for adj in (0, 1):
+        g = RowOps(p, sp).onestep(5, 9.5, adj, x)
+        o = oracle.onestep(p, sp, 5, 9.5, adj, x, prec=64)
+        assert rel_l2(g, o) < TOL_STEP, rel_l2(g, o)
+    d = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    WemOp(p, wav).forward(s, rho, d)
+    o = oracle.wem_forward(p, wav, s, rho, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(d, o) < TOL_OP, ("wem", rel_l2(d, o))
+    dd = (np.random.default_rng(16).random((p.ns, p.nr, p.nt)) - .5).astype(np.float32)
+    a0, a1 = np.zeros_like(s), np.zeros_like(s)
+    BornOp(p, wav, s, rho).adjoint(a0, a1, dd)
+    q0, q1 = oracle.born_adjoint(p, wav, s, rho, dd, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(a0, q0) < TOL_OP, rel_l2(a0, q0)
+    assert rel_l2(a1, q1) < TOL_OP, rel_l2(a1, q1)

@@ -149,3 +149,31 @@ def test_refsampler_quirks(oracle):
     for iz in (0, 10, 20):
         dist = np.abs(sp[iz].real[:, None] - sref[iz].real[None, :])
         assert (np.take_along_axis(dist, idx[iz][:, None], 1)[:, 0] <= dist.min(1) + 0).all()
+
+
+@pytest.mark.parametrize("adj", [0, 1])
+def test_exact_kz_phase_law(oracle, adj):
+    """phase_law exact_kz restates extPropagator/src/Phshift.cpp:59,81: on a
+    constant model the split step is 1 and one depth step is the plane-wave
+    factor exp(-i dz conj(sqrt(w^2 s - k^2 + 1e-5 i))) on the k grid of
+    Phshift_cmplx.cpp:13,21-24 (adjoint: its conjugate)."""
+    nx, nz, dx, dz, f = 64, 6, 10.0, 10.0, 11.0
+    s = np.full((nz, nx), 1 / 2000.0 ** 2 + 2e-10j, np.complex64)
+    par = dict(ns=1, osx=0.0, dsx=0.0, nr=1, orx=0.0, drx=dx, prop="ssf", nref=1, phase_law="exact_kz")
+    p = make_params(par, nx=nx, nz=nz, dx=dx, dz=dz, nt=64, dt=0.004)
+    x = rand_c(np.random.default_rng(5), (2, nx))
+    got = oracle.onestep(p, s, 2, f, adj, x, prec=64)
+    k = np.zeros(nx)
+    dk = 2 * np.pi / (dx * (nx - 1))
+    k[:nx // 2] = np.arange(nx // 2) * dk
+    k[nx - np.arange(1, nx // 2)] = -k[1:nx // 2]
+    w = 2 * np.pi * f
+    kz = np.conj(np.sqrt(w * w * s[2, 0].astype(np.complex128) - k * k + 1e-5j))
+    fac = np.exp(-1j * dz * kz)
+    if adj:
+        fac = np.conj(fac)
+    want = np.fft.ifft(np.fft.fft(x.astype(np.complex128), axis=-1) * fac, axis=-1)
+    assert rel_l2(got, want) < 1e-6  # complex64 output of an fp64 computation
+    p.phase_law = 0
+    ispc = oracle.onestep(p, s, 2, f, adj, x, prec=64)
+    assert rel_l2(ispc, want) > 1e-3  # the two laws differ (eps damping)

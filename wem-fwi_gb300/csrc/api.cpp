@@ -324,6 +324,7 @@ class Engine {
     ctx_.nref = p_.nref;
     ctx_.prop = p_.prop;
     ctx_.ntaylor = p_.ntaylor;
+    ctx_.phase_law = p_.phase_law;
     ctx_.nfreq = F_;
     ctx_.ext = ext_ ? 1 : 0;
     ctx_.ns = g.ns;
@@ -564,6 +565,7 @@ class RowOps {
     require(nxg >= 2 && p.nz > 1, "bad grid");
     require(p.pad >= 0 && p.tap >= 0 && p.pad != 1 && 2 * p.pad <= nxg, "bad pad/tap");
     require(p.ntaylor >= 0 && p.ntaylor <= 4, "ntaylor must be in [0,4]");
+    require(p.phase_law == WEM_PHASE_ISPC || p.phase_law == WEM_PHASE_EXACT_KZ, "phase_law must be 0 or 1");
     std::vector<float> hs = host_floats(slow, 2 * (size_t)p.nz * nxg);
     std::vector<cd> sp((size_t)p.nz * nxg), dp(sp.size(), cd(1.0, 0.0));
     for (size_t i = 0; i < sp.size(); ++i) sp[i] = cd(hs[2 * i], hs[2 * i + 1]);
@@ -581,6 +583,7 @@ class RowOps {
     c_.nref = p.nref;
     c_.prop = p.prop;
     c_.ntaylor = p.ntaylor;
+    c_.phase_law = p.phase_law;
     c_.nfreq = 1;
     c_.ext = 0;
     c_.dz = p.dz;
@@ -689,6 +692,7 @@ void wem_params_default(wem_params* p) {
   p->fmin = 1.0f;
   p->adjoint_mode = WEM_ADJ_COMPAT;
   p->refs_mode = WEM_REFS_ASCODED;
+  p->phase_law = WEM_PHASE_ISPC;
 }
 
 const char* wem_last_error(void) { return g_error.c_str(); }

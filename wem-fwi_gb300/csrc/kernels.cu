@@ -11,6 +11,7 @@
 
 #include "fft.cuh"
 #include "kernels.h"
+#include "wemgpu.h"
 
 namespace wg {
 namespace {
@@ -673,9 +674,15 @@ __global__ void k_phase(DevCtx c, const float2* sref, float eps, float2* ph) {
     const float2 s = sref[((size_t)m * c.nz + z) * c.nref + j];
     const float w = c.omega[f], w2 = w * w;
     const float a = fmaf(w2, s.x, -k * k);
-    const float b = w2 * fmaf(-eps, s.x, s.y);
+    // ISPC law: b = w^2 (s_im - eps s_re), factor exp(im dz - i re dz) with
+    // re = Re sqrt(a + i b), im = -|Im sqrt(a + i b)|.  EXACT_KZ law
+    // (extPropagator/src/Phshift.cpp:59,81): kz = sqrt(a + i (w^2 s_im + 1e-5)),
+    // factor exp(-i dz conj(kz)) = exp(-dz Im kz - i dz Re kz); Im kz >= 0
+    // for b >= 0, the principal root's sign otherwise.
+    const bool exact = c.phase_law == WEM_PHASE_EXACT_KZ;
+    const float b = exact ? fmaf(w2, s.y, 1e-5f) : w2 * fmaf(-eps, s.x, s.y);
     const float cc = sqrtf(fmaf(a, a, b * b));
-    float re, im;
+    float re, im;  // real part and non-positive imaginary part of the root
     if (a >= 0.f) {
       re = sqrtf(0.5f * (cc + a));
       im = re > 0.f ? -fabsf(b) / (2.f * re) : 0.f;
@@ -684,6 +691,7 @@ __global__ void k_phase(DevCtx c, const float2* sref, float eps, float2* ph) {
       im = -q;
       re = fabsf(b) / (2.f * q);
     }
+    if (exact && b < 0.f) im = -im;  // principal root: Im kz takes the sign of b
     const float e = expf(im * c.dz);
     float sn, cs;
     sincosf(re * c.dz, &sn, &cs);

@@ -18,6 +18,7 @@ constexpr int kThreads = 512;  // threads per CTA of every pass kernel
 struct DevCtx {
   FftPlan plan;                 // length N = nxg + 2 tap
   int N, nxg, tap, pad, nz, nref, prop, ntaylor, nfreq, ext, ns, nr, ngs, ngr, nbin;
+  int phase_law;                // WEM_PHASE_ISPC or WEM_PHASE_EXACT_KZ
   float dz, invN;
   const float2* tw;             // [N] exp(-2 pi i t/N)
   const float2* ph;             // [F][nz][nref][N] phase-shift factors (phase_shift.ispc)

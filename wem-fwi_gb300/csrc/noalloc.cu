@@ -141,7 +141,8 @@ extern "C" int wemop_onestep_noalloc(const wem_params* p, const void* slow_row, 
                                      void* out, int nrow, int add, void* stream) {
   if (!p || !slow_row || !sref || !refidx || !in || !out) return fail(WEM_EINVAL, "NULL argument");
   if (nxg < 2 || nrow < 0 || p->tap < 0 || p->pad < 0 || p->pad == 1 || 2 * p->pad > nxg || p->nref < 1 ||
-      !(p->dx > 0) || !(p->dz > 0) || (p->prop != WEM_PROP_SSF && p->prop != WEM_PROP_PSPI))
+      !(p->dx > 0) || !(p->dz > 0) || (p->prop != WEM_PROP_SSF && p->prop != WEM_PROP_PSPI) ||
+      (p->phase_law != WEM_PHASE_ISPC && p->phase_law != WEM_PHASE_EXACT_KZ))
     return fail(WEM_EINVAL, "invalid parameters for the depth step");
   const int N = nxg + 2 * p->tap;
   if (N > kMaxN || p->nref > kMaxRef)
@@ -197,6 +198,7 @@ extern "C" int wemop_onestep_noalloc(const wem_params* p, const void* slow_row, 
   c.nref = p->nref;
   c.prop = p->prop;
   c.ntaylor = p->ntaylor;
+  c.phase_law = p->phase_law;
   c.nfreq = 1;
   c.ext = 0;
   c.dz = p->dz;

@@ -104,6 +104,7 @@ Geometry make_geometry(const wem_params& p, const float* wavelet) {
   require(p.pad >= 0 && p.tap >= 0 && p.tpad >= 0, "pad/tap/tpad must be >= 0");
   require(p.pad != 1, "pad == 1 makes the taper divide by zero (Taper.h:19)");
   require(p.ntaylor >= 0 && p.ntaylor <= 4, "ntaylor must be in [0,4]");
+  require(p.phase_law == WEM_PHASE_ISPC || p.phase_law == WEM_PHASE_EXACT_KZ, "phase_law must be 0 or 1");
   require(p.ngs >= 0 && p.ngr >= 0, "ngs/ngr must be >= 0");
   require(p.prop == WEM_PROP_SSF || p.prop == WEM_PROP_PSPI, "prop must be ssf or pspi");
   Geometry g;

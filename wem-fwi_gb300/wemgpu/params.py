@@ -19,6 +19,7 @@ WEM_PROP_SSF, WEM_PROP_PSPI = 0, 1
 WEM_ADJ_COMPAT, WEM_ADJ_EXACT = 0, 1
 WEM_REFS_ASCODED, WEM_REFS_NEAREST = 0, 1
 WEM_DATA_TIME, WEM_DATA_FREQ = 0, 1
+WEM_PHASE_ISPC, WEM_PHASE_EXACT_KZ = 0, 1
 
 _fp = ctypes.POINTER(ctypes.c_float)
 
@@ -42,6 +43,7 @@ class WemParams(ctypes.Structure):
         ("eps", ctypes.c_float), ("fmin", ctypes.c_float), ("fmax", ctypes.c_float),
         ("nfreq", ctypes.c_int),
         ("adjoint_mode", ctypes.c_int), ("refs_mode", ctypes.c_int), ("nbin", ctypes.c_int),
+        ("phase_law", ctypes.c_int),
     ]
 
     def __init__(self, *a, **kw):
@@ -64,7 +66,7 @@ _DEFAULTS = dict(
     nr=0, orx=0.0, orz=0.0, drx=0.0, drz=0.0,
     prop="ssf", nref=1, tap=0, pad=0, tpad=0, ngs=0, ngr=0, ntaylor=1,
     eps=0.04, fmin=1.0, fmax=0.0, nfreq=0,
-    adjoint_mode="compat", refs_mode="ascoded", nbin=0,
+    adjoint_mode="compat", refs_mode="ascoded", nbin=0, phase_law="ispc",
 )
 
 
@@ -100,6 +102,8 @@ def make_params(par: Any, *, nx: int, nz: int, dx: float, dz: float,
     p.adjoint_mode = WEM_ADJ_EXACT if str(am).lower() == "exact" or am == WEM_ADJ_EXACT else WEM_ADJ_COMPAT
     rm = m["refs_mode"]
     p.refs_mode = WEM_REFS_NEAREST if str(rm).lower() == "nearest" or rm == WEM_REFS_NEAREST else WEM_REFS_ASCODED
+    pl = m["phase_law"]
+    p.phase_law = WEM_PHASE_EXACT_KZ if str(pl).lower() == "exact_kz" or pl == WEM_PHASE_EXACT_KZ else WEM_PHASE_ISPC
     # irregular geometry: explicit coordinate lists replace the regular grid
     for key, field, count in (("sx", "src_x", "ns"), ("sz", "src_z", "ns"),
                               ("rx", "rec_x", "nr"), ("rz", "rec_z", "nr")):
