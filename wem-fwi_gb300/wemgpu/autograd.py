@@ -1,0 +1,114 @@
+"""FWI through torch autograd.
+
+The reference builds its FWI objective from two operators:
+``NonLinearOperator(wemOp, bornOp)`` inside python-solver's
+``ProblemL2NonLinear`` (scripts/fwi.py:70-71,90,113).  The objective is
+``1/2 ||WEM(m) - d_obs||^2``, and its gradient is the Born adjoint of the
+residual at the current background (BornFull::adjoint,
+propagator/src/born_prop.cpp:178-216).
+
+``FWIGradient`` is that pair as a ``torch.autograd.Function``:
+- forward: the nonlinear modelling of ``WemOp``;
+- backward: ``BornOp.adjoint`` of the incoming data gradient, with the
+  background set to the forward's model.
+
+Both run on the CUDA library.  For any loss of the synthetic data, the
+leaves get the reference's Born-linearised gradient:
+- compat adjoint (default): the reference as coded;
+- exact adjoint: the transpose of the Born operator.
+
+For a real loss and complex leaves, torch's gradient is dL/dRe + i dL/dIm.
+That is B^H r for real time data r, which is what the Born adjoint returns.
+
+Memory: the Born adjoint stores two wavefields per (shot, frequency) row.
+The library bounds that storage by running the rows in chunks sized to free
+HBM, so no depth checkpointing is needed for the stored fields.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .core import BornOp, WemOp
+from .params import WemParams
+
+
+class FWIGradient(torch.autograd.Function):
+    """d = WEM(s2, rho); backward: (g_s2, g_rho) = Born^H(dL/dd) at (s2, rho)."""
+
+    @staticmethod
+    def forward(ctx, s2, rho, wem: WemOp, born: BornOp):
+        if not (s2.is_cuda and rho.is_cuda):
+            raise ValueError("FWIGradient works on CUDA tensors")
+        s2c, rhoc = s2.detach().contiguous(), rho.detach().contiguous()
+        d = torch.empty(wem.data_shape(0), dtype=torch.float32, device=s2.device)
+        wem.forward(s2c, rhoc, d)
+        ctx.save_for_backward(s2c, rhoc)
+        ctx.born = born
+        return d
+
+    @staticmethod
+    def backward(ctx, grad_d):
+        s2, rho = ctx.saved_tensors
+        born: BornOp = ctx.born
+        born.set_background(s2, rho)
+        g_s2, g_rho = torch.zeros_like(s2), torch.zeros_like(rho)
+        born.adjoint(g_s2, g_rho, grad_d.contiguous())
+        return g_s2, g_rho, None, None
+
+
+def modelled_data(s2, rho, wem: WemOp, born: BornOp):
+    """Synthetic data of (s2, rho) that backpropagates through the Born adjoint."""
+    return FWIGradient.apply(s2, rho, wem, born)
+
+
+class FwiObjective:
+    """The L2 FWI objective and its gradient, one call per iteration.
+
+    ``obj(s2, rho) -> (loss, g_s2, g_rho)``, with
+    loss = 1/2 ||WEM(s2, rho) - d_obs||^2 and g = Born^H(WEM(s2, rho) - d_obs).
+
+    d_obs (``[ns][nr][nt]`` float32, numpy or a CUDA tensor) is copied to the
+    device once.  Models may be numpy arrays (the call copies them in, and the
+    gradients out, through pinned buffers) or CUDA tensors (no copies).
+    """
+
+    def __init__(self, p: WemParams, wavelet, d_obs, s2_init, rho_init, device=None):
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.wem = WemOp(p, wavelet)
+        s2_init = torch.as_tensor(s2_init).to(self.device).contiguous()
+        rho_init = torch.as_tensor(rho_init).to(self.device).contiguous()
+        self.born = BornOp(p, wavelet, s2_init, rho_init)
+        self.d_obs = torch.as_tensor(d_obs).to(self.device, torch.float32).contiguous()
+        if tuple(self.d_obs.shape) != tuple(self.wem.data_shape(0)):
+            raise ValueError(f"d_obs shape {tuple(self.d_obs.shape)} != {self.wem.data_shape(0)}")
+        shape = self.wem.model_shape
+        self._dev_in = [torch.empty(shape, dtype=torch.complex64, device=self.device) for _ in range(2)]
+        self._pin_out = [torch.empty(shape, dtype=torch.complex64).pin_memory() for _ in range(2)]
+        self.h2d_bytes = 0
+        self.d2h_bytes = 0
+
+    def _to_device(self, a, i):
+        if isinstance(a, torch.Tensor) and a.is_cuda:
+            return a.contiguous(), False
+        t = torch.as_tensor(np.ascontiguousarray(a, dtype=np.complex64))
+        self._dev_in[i].copy_(t, non_blocking=t.is_pinned())
+        self.h2d_bytes = t.numel() * 8 * 2
+        return self._dev_in[i], True
+
+    def __call__(self, s2, rho):
+        s2_d, host = self._to_device(s2, 0)
+        rho_d, _ = self._to_device(rho, 1)
+        with torch.enable_grad():
+            a = s2_d.detach().requires_grad_(True)
+            b = rho_d.detach().requires_grad_(True)
+            d = modelled_data(a, b, self.wem, self.born)
+            loss = 0.5 * torch.sum((d - self.d_obs) ** 2)
+            loss.backward()
+        value = float(loss.detach())
+        if not host:
+            return value, a.grad, b.grad
+        self._pin_out[0].copy_(a.grad)
+        self._pin_out[1].copy_(b.grad)
+        self.d2h_bytes = 2 * a.grad.numel() * 8 + 4
+        return value, self._pin_out[0].numpy().copy(), self._pin_out[1].numpy().copy()
