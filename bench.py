@@ -115,10 +115,10 @@ def workload(small=False):
 
 # DRAM bytes (read + write) per (row, depth) of the pass kernels, from ncu
 # captures of the reduced case (8 shots x 21 frequencies, nz 300, N 768;
-# profiles/kw_born_adj_e24_c3_small.md): the traffic of a launch scales with
+# profiles/kw_born_adj2_e24_c3_small.md): the traffic of a launch scales with
 # the rows it carries, so a full launch is this figure x rows x depths.
 TRAFFIC_PER_ROW_DEPTH = {
-    "k_born_adj": (711913728 + 707227904) / (168 * 300),
+    "k_born_adj": (708894720 + 696811520) / (168 * 300),
 }
 
 
@@ -326,13 +326,12 @@ def cpu_sample(cfg, seconds=15.0, nthreads=0):
     from wemgpu import synthetic as S
     O.build()
     nthreads = nthreads or os.cpu_count() or 1
-    # grow the sample (frequencies first) until it takes a few seconds, then
-    # scale to the budget
-    nfk = 4
+    # grow the sample (shots, each with the workload's full frequency axis and
+    # all depths) until it takes about `seconds`
     p_full = S.params_of(cfg)
-    tmax = p_full.ot + p_full.dt * (p_full.nt + p_full.tpad - 1)
+    nsk = 1
     while True:
-        par = dict(cfg["par"], ns=1, fmax=cfg["par"]["fmin"] + (nfk - 0.5) / tmax)
+        par = dict(cfg["par"], ns=nsk)
         c = dict(cfg, par=par)
         p = S.params_of(c)
         nf = O.count_freqs(p)[0]
@@ -341,13 +340,13 @@ def cpu_sample(cfg, seconds=15.0, nthreads=0):
         O.born_adjoint(p, cfg["wavelet"], cfg["slow"], cfg["rho"], syn, kind=0, prec=32, nthreads=nthreads,
                        fchunks=max(1, nthreads))
         dt = time.perf_counter() - t0
-        if dt > 0.5 * seconds or nfk >= 96:
+        if dt > 0.5 * seconds or nsk >= p_full.ns:
             break
-        nfk = min(96, max(nfk * 2, int(nfk * seconds / max(dt, 1e-3))))
+        nsk = min(p_full.ns, max(nsk + 1, int(nsk * seconds / max(dt, 1e-3))))
     rate = row_steps(p, nf) / dt
     return {"value": rate, "unit": "depth-steps/s", "cores": nthreads, "kind": "port",
-            "sample": f"1 shot x {nf} freqs of c3 (all {p.nz} depths), WEM fwd + Born adjoint, {dt:.1f} s",
-            "s_per_iter_extrapolated": row_steps(S.params_of(cfg), 96) / rate}
+            "sample": f"{nsk} shots x {nf} freqs of c3 (all {p.nz} depths), WEM fwd + Born adjoint, {dt:.1f} s",
+            "s_per_iter_extrapolated": row_steps(p_full, nf) / rate}
 
 
 def run_reference(args, rank, world):
