@@ -5,12 +5,14 @@
 // schedule and the workspaces.  Every public call validates its arguments
 // on the host, turns every failure into a status code and never throws
 // across the boundary.
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -55,6 +57,24 @@ bool is_device_ptr(const void* p) {
     return false;
   }
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// one cuBLAS handle per device for the time <-> frequency GEMMs, created on
+// first use and kept for the life of the process
+cublasHandle_t blas_handle() {
+  static std::mutex mu;
+  static cublasHandle_t handles[64] = {};
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+  require(dev >= 0 && dev < 64, "device index out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!handles[dev] && cublasCreate(&handles[dev]) != CUBLAS_STATUS_SUCCESS)
+    throw Fail(WEM_EDEVICE, "cublasCreate failed");
+  return handles[dev];
+}
+
+void blas_check(cublasStatus_t st, const char* what) {
+  if (st != CUBLAS_STATUS_SUCCESS) throw Fail(WEM_EDEVICE, std::string(what) + ": cuBLAS status " + std::to_string((int)st));
 }
 
 // growable device buffer
@@ -287,9 +307,8 @@ class Engine {
   Geometry geo_;
   int F_ = 0, M_ = 1;
   DevCtx ctx_{};
-  FftPlan tplan_{};
   // static tables
-  Buf tw_, kx_, taper_, omega_, bin_, wave_, sx_, sz_, gs_, gr_, rptr_, rid_, rxs_, ttw_;
+  Buf tw_, kx_, taper_, omega_, bin_, wave_, sx_, sz_, gs_, gr_, rptr_, rid_, rxs_, wfwd_, winv_;
   // background tables
   Buf sref_, ref_, q_, sc_, rc_, a0b_, b0b_, a1b_, b1b_, ph_, fac_, sp_, dp_;
   float2 *a0_ = nullptr, *b0_ = nullptr, *a1_ = nullptr, *b1_ = nullptr;
@@ -331,14 +350,16 @@ class Engine {
     ctx_.nr = g.nr;
     ctx_.ngs = p_.ngs;
     ctx_.ngr = p_.ngr;
-    ctx_.nbin = g.nt_pad;
+    ctx_.nbin = F_;  // internal bins are compact: the propagated frequencies only
     ctx_.dz = p_.dz;
     ctx_.invN = 1.0f / g.N;
     ctx_.tw = upload(tw_, to_f2(tw));
     ctx_.kx = upload(kx_, kf);
     ctx_.taperN = upload(taper_, tpf);
     ctx_.omega = upload(omega_, om);
-    ctx_.bin = upload(bin_, g.bin);
+    std::vector<int> fidx(F_);
+    std::iota(fidx.begin(), fidx.end(), 0);
+    ctx_.bin = upload(bin_, fidx);
     ctx_.wave = upload(wave_, to_f2(g.wave_at));
     ctx_.sx = upload(sx_, g.sx);
     ctx_.sz = upload(sz_, g.sz);
@@ -347,9 +368,27 @@ class Engine {
     ctx_.rptr = upload(rptr_, rptr);
     ctx_.rid = upload(rid_, ord);
     ctx_.rxs = upload(rxs_, rxs);
-    tplan_ = make_plan(g.nt_pad);
-    upload(ttw_, to_f2(twiddles(g.nt_pad)));
-    bins_ = binsbuf_.as<float2>((size_t)g.ns * g.nr * g.nt_pad);
+    // FFT1_r over time (FFT1_r.cpp:74-96) restricted to the propagated bins
+    // (consecutive, PropParam.h:75-78): unitary DFT matrices in double,
+    // rounded once; the forward takes e^{-i a}, the inverse keeps Re(B e^{i a})
+    {
+      const int n = g.nt_pad, nt = p_.nt, F2 = 2 * F_;
+      std::vector<float> wf((size_t)nt * F2), wi((size_t)F2 * nt);
+      const long double pi = 3.14159265358979323846264338327950288L;
+      const double sc = 1.0 / std::sqrt((double)n);
+      for (int k = 0; k < nt; ++k)
+        for (int f = 0; f < F_; ++f) {
+          const long double a = 2 * pi * (long double)((long long)g.bin[f] * k % n) / n;
+          const float cs = (float)(std::cos(a) * sc), sn = (float)(std::sin(a) * sc);
+          wf[(size_t)k * F2 + 2 * f] = cs;
+          wf[(size_t)k * F2 + 2 * f + 1] = -sn;
+          wi[(size_t)(2 * f) * nt + k] = cs;
+          wi[(size_t)(2 * f + 1) * nt + k] = -sn;
+        }
+      upload(wfwd_, wf);
+      upload(winv_, wi);
+    }
+    bins_ = binsbuf_.as<float2>((size_t)g.ns * g.nr * F_);
   }
 
   // Background tables on the device: edge-padded model, RefSampler (on the
@@ -507,7 +546,7 @@ class Engine {
   }
 
   float2* zero_bins() {
-    cuda_check(cudaMemsetAsync(bins_, 0, (size_t)geo_.ns * geo_.nr * geo_.nt_pad * 8, 0), "memset");
+    cuda_check(cudaMemsetAsync(bins_, 0, (size_t)geo_.ns * geo_.nr * F_ * 8, 0), "memset");
     return bins_;
   }
 
@@ -520,19 +559,25 @@ class Engine {
     cuda_check(cudaStreamSynchronize(0), "pad");
   }
 
-  // internal bins [ns][nr][nt_pad] -> caller data
+  // internal bins [ns][nr][F] -> caller data: time traces by one GEMM with
+  // the inverse DFT matrix, frequency data by a window copy
   void emit(void* data, int kind, int add) {
     require(data != nullptr, "data is NULL");
     const int ntr = geo_.ns * geo_.nr;
     Staged o;
     if (kind == WEM_DATA_TIME) {
       o.out(data, (size_t)ntr * p_.nt * 4, add != 0);
-      launch_bins_to_time(tplan_, (const float2*)ttw_.p, bins_, (float*)o.dev, ntr, p_.nt, add, 0);
+      cublasHandle_t h = blas_handle();
+      blas_check(cublasSetStream(h, 0), "cublasSetStream");
+      const float one = 1.f, beta = add ? 1.f : 0.f;
+      blas_check(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, p_.nt, ntr, 2 * F_, &one, (const float*)winv_.p, p_.nt,
+                             (const float*)bins_, 2 * F_, &beta, (float*)o.dev, p_.nt),
+                 "bins to time");
+      note_launch();
     } else {
       require(kind == WEM_DATA_FREQ, "unknown data kind");
       o.out(data, (size_t)ntr * geo_.nbin * 8, add != 0);
-      launch_copy_rows(bins_, geo_.nt_pad, (float2*)o.dev, geo_.nbin, ntr, std::min(geo_.nbin, geo_.nt_pad), add,
-                       0);
+      launch_bin_window(bins_, (float2*)o.dev, ntr, geo_.nbin, F_, geo_.bin[0], 1, add, 0);
     }
     cuda_check(cudaGetLastError(), "emit launch");
     cuda_check(cudaStreamSynchronize(0), "operator");
@@ -545,12 +590,17 @@ class Engine {
     Staged s;
     if (kind == WEM_DATA_TIME) {
       s.in(data, (size_t)ntr * p_.nt * 4);
-      launch_time_to_bins(tplan_, (const float2*)ttw_.p, (const float*)s.dev, bins_, ntr, p_.nt, 0);
+      cublasHandle_t h = blas_handle();
+      blas_check(cublasSetStream(h, 0), "cublasSetStream");
+      const float one = 1.f, zero = 0.f;
+      blas_check(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, 2 * F_, ntr, p_.nt, &one, (const float*)wfwd_.p, 2 * F_,
+                             (const float*)s.dev, p_.nt, &zero, (float*)bins_, 2 * F_),
+                 "time to bins");
+      note_launch();
     } else {
       require(kind == WEM_DATA_FREQ, "unknown data kind");
       s.in(data, (size_t)ntr * geo_.nbin * 8);
-      launch_copy_rows((const float2*)s.dev, geo_.nbin, bins_, geo_.nt_pad, ntr, std::min(geo_.nbin, geo_.nt_pad),
-                       0, 0);
+      launch_bin_window((const float2*)s.dev, bins_, ntr, geo_.nbin, F_, geo_.bin[0], 0, 0, 0);
     }
     cuda_check(cudaGetLastError(), "absorb launch");
     cuda_check(cudaStreamSynchronize(0), "absorb");

@@ -699,26 +699,27 @@ __global__ void k_phase(DevCtx c, const float2* sref, float eps, float2* ph) {
   }
 }
 
-// SSF per-point factor: taper / N * exp(-i w dz q) (SplitStep.cpp:13-14)
+// SSF per-point factor: taper / N * exp(-i w dz q) (SplitStep.cpp:13-14).
+// One CTA row per (frequency, depth) table row, threads over the points.
 __global__ void k_fac(DevCtx c, const float2* q, float2* fac) {
-  const size_t total = (size_t)c.nfreq * c.nz * c.nxg;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-    int x = (int)(i % c.nxg);
-    size_t t = i / c.nxg;
-    int z = (int)(t % c.nz);
-    int f = (int)(t / c.nz);
-    int m = c.ext ? f : 0;
-    size_t qi = ((size_t)m * c.nz + z) * c.nxg + x;
-    if (c.ref[qi] < 0) {
-      fac[i] = zero2();
-      continue;
+  const int nrow = c.nfreq * c.nz;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= c.nxg) return;
+  const float tp = c.taperN[x];
+  for (int r = blockIdx.y; r < nrow; r += gridDim.y) {
+    const int z = r % c.nz, f = r / c.nz;
+    const int m = c.ext ? f : 0;
+    const size_t qi = ((size_t)m * c.nz + z) * c.nxg + x;
+    float2 out = zero2();
+    if (c.ref[qi] >= 0) {
+      const float2 qq = q[qi];
+      const double wdz = (double)c.omega[f] * c.dz;
+      const float amp = expf((float)(wdz * qq.y)) * tp;
+      float sn, cs;
+      sincosf((float)(wdz * qq.x), &sn, &cs);
+      out = make_float2(amp * cs, -amp * sn);
     }
-    float2 qq = q[qi];
-    double wdz = (double)c.omega[f] * c.dz;
-    float amp = expf((float)(wdz * qq.y)) * c.taperN[x];
-    float sn, cs;
-    sincosf((float)(wdz * qq.x), &sn, &cs);
-    fac[i] = make_float2(amp * cs, -amp * sn);
+    fac[(size_t)r * c.nxg + x] = out;
   }
 }
 
@@ -785,46 +786,25 @@ __global__ void k_grad(int M, int nz, int nxg, int nx, int pad, const float2* a0
   }
 }
 
-// FFT1_r over time (FFT1_r.cpp:74-96): unitary transforms of zero-padded traces
-__global__ void __launch_bounds__(kThreads) k_time_to_bins(FftPlan P, const float2* twg, const float* t,
-                                                           float2* b, int ntr, int nt, int G) {
-  extern __shared__ float4 smem4[];
-  Carve sm{reinterpret_cast<float2*>(smem4)};
-  const int n = P.n;
-  float2* tw = sm.take(n);
-  float2* X = sm.take((size_t)G * n);
-  float2* Y = sm.take((size_t)G * n);
-  const int r0 = blockIdx.x * G, nrow = min(G, ntr - r0);
-  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = twg[i];
-  for (int i = threadIdx.x; i < nrow * n; i += blockDim.x) {
-    int r = i / n, k = i - r * n;
-    X[i] = make_float2(k < nt ? t[(size_t)(r0 + r) * nt + k] : 0.f, 0.f);
-  }
-  __syncthreads();
-  float2* R = smem_fft(X, Y, nrow, n, P, tw, false);
-  const float s = rsqrtf((float)n);
-  for (int i = threadIdx.x; i < nrow * n; i += blockDim.x) b[(size_t)r0 * n + i] = c_scale(R[i], s);
-}
-
-__global__ void __launch_bounds__(kThreads) k_bins_to_time(FftPlan P, const float2* twg, const float2* b, float* t,
-                                                           int ntr, int nt, int add, int G) {
-  extern __shared__ float4 smem4[];
-  Carve sm{reinterpret_cast<float2*>(smem4)};
-  const int n = P.n;
-  float2* tw = sm.take(n);
-  float2* X = sm.take((size_t)G * n);
-  float2* Y = sm.take((size_t)G * n);
-  const int r0 = blockIdx.x * G, nrow = min(G, ntr - r0);
-  for (int i = threadIdx.x; i < n; i += blockDim.x) tw[i] = twg[i];
-  for (int i = threadIdx.x; i < nrow * n; i += blockDim.x) X[i] = b[(size_t)r0 * n + i];
-  __syncthreads();
-  float2* R = smem_fft(X, Y, nrow, n, P, tw, true);
-  const float s = rsqrtf((float)n);
-  for (int i = threadIdx.x; i < nrow * nt; i += blockDim.x) {
-    int r = i / nt, k = i - r * nt;
-    float v = R[r * n + k].x * s;
-    float* d = t + (size_t)(r0 + r) * nt + k;
-    *d = add ? *d + v : v;
+// Window copy between caller bins [nrows][ldu] and the compact bins
+// [nrows][nf] of the propagated frequencies (bins off .. off + nf - 1).
+// to_user: every caller bin is written (zero outside the window, or left as
+// it is with add); otherwise the compact rows take the caller's window
+// (zero where it runs past ldu).
+__global__ void k_bin_window(const float2* src, float2* dst, int nrows, int ldu, int nf, int off, int to_user,
+                             int add) {
+  const size_t total = (size_t)nrows * (to_user ? ldu : nf);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    if (to_user) {
+      const size_t r = i / ldu;
+      const int b = (int)(i - r * ldu), f = b - off;
+      const float2 v = (f >= 0 && f < nf) ? src[r * nf + f] : zero2();
+      dst[i] = add ? c_add(dst[i], v) : v;
+    } else {
+      const size_t r = i / nf;
+      const int f = (int)(i - r * nf), b = f + off;
+      dst[i] = b < ldu ? src[r * ldu + b] : zero2();
+    }
   }
 }
 
@@ -892,8 +872,9 @@ void launch_phase_tables(const DevCtx& c, const float2* sref, float eps, float2*
 }
 
 void launch_fac_tables(const DevCtx& c, const float2* q, float2* fac, cudaStream_t st) {
-  size_t n = (size_t)c.nfreq * c.nz * c.nxg;
-  k_fac<<<grid_for(n), 256, 0, st>>>(c, q, fac);
+  const int nrow = c.nfreq * c.nz;
+  const dim3 grid((c.nxg + 127) / 128, nrow < 65535 ? nrow : 65535);
+  k_fac<<<grid, 128, 0, st>>>(c, q, fac);
   note_launch();
 }
 
@@ -974,27 +955,10 @@ void launch_grad_assemble(const DevCtx& c, int M, const float2* a0, const float2
   note_launch();
 }
 
-static int trace_rows(int n) {
-  int lim = (max_smem_per_block() / 8 - n - 8) / (2 * n + 4);
-  int G = lim < 1 ? 1 : (lim > 16 ? 16 : lim);
-  return G;
-}
-
-void launch_time_to_bins(const FftPlan& P, const float2* tw, const float* t, float2* b, int ntr, int nt,
-                         cudaStream_t st) {
-  int G = trace_rows(P.n);
-  size_t sm = 8 * (al(P.n) + 2 * al((size_t)G * P.n));
-  set_smem(k_time_to_bins, sm);
-  k_time_to_bins<<<(ntr + G - 1) / G, kThreads, sm, st>>>(P, tw, t, b, ntr, nt, G);
-  note_launch();
-}
-
-void launch_bins_to_time(const FftPlan& P, const float2* tw, const float2* b, float* t, int ntr, int nt, int add,
-                         cudaStream_t st) {
-  int G = trace_rows(P.n);
-  size_t sm = 8 * (al(P.n) + 2 * al((size_t)G * P.n));
-  set_smem(k_bins_to_time, sm);
-  k_bins_to_time<<<(ntr + G - 1) / G, kThreads, sm, st>>>(P, tw, b, t, ntr, nt, add, G);
+void launch_bin_window(const float2* src, float2* dst, int nrows, int ldu, int nf, int off, int to_user, int add,
+                       cudaStream_t st) {
+  const size_t n = (size_t)nrows * (to_user ? ldu : nf);
+  k_bin_window<<<grid_for(n), 256, 0, st>>>(src, dst, nrows, ldu, nf, off, to_user, add);
   note_launch();
 }
 

@@ -107,11 +107,9 @@ void launch_grad_assemble(const DevCtx& c, int M, const float2* a0, const float2
                           const float2* b1, const float2* IR, const float2* IS, float2* g0, float2* g1, int nx,
                           int add, cudaStream_t st);
 // traces: time [ntr][nt] <-> bins [ntr][n]
-void launch_time_to_bins(const FftPlan& P, const float2* tw, const float* t, float2* b, int ntr, int nt,
-                         cudaStream_t st);
-void launch_bins_to_time(const FftPlan& P, const float2* tw, const float2* b, float* t, int ntr, int nt, int add,
-                         cudaStream_t st);
-// complex copy with row reshape: dst[r][j] (+)= src[r][j] for j < ncopy, zero beyond (unless add)
+// caller bins [nrows][ldu] <-> compact propagated bins [nrows][nf] (window at off)
+void launch_bin_window(const float2* src, float2* dst, int nrows, int ldu, int nf, int off, int to_user, int add,
+                       cudaStream_t st);
 void launch_copy_rows(const float2* src, int lds, float2* dst, int ldd, int nrows, int ncopy, int add,
                       cudaStream_t st);
 void launch_scale_add(float2* y, const float2* x, size_t n, cudaStream_t st);

@@ -15,15 +15,23 @@ template <int E>
 size_t smem_w_e(const DevCtx& c, bool slots);
 template <int E>
 int adj_rows_w(const DevCtx& c);
+template <int E>
+int wem_rows_w(const DevCtx& c);
+
+template <int E>
+static int rows_e(const DevCtx& c, int which) {
+  if (which == 0) return wem_rows_w<E>(c);
+  if (which == 2) return adj_rows_w<E>(c);
+  return 8;
+}
 
 int warp_rows_per_group(const DevCtx& c, int which) {
-  if (which != 2) return 8;
   switch (c.N / 32) {
-    case 8: return adj_rows_w<8>(c);
-    case 12: return adj_rows_w<12>(c);
-    case 16: return adj_rows_w<16>(c);
-    case 24: return adj_rows_w<24>(c);
-    case 32: return adj_rows_w<32>(c);
+    case 8: return rows_e<8>(c, which);
+    case 12: return rows_e<12>(c, which);
+    case 16: return rows_e<16>(c, which);
+    case 24: return rows_e<24>(c, which);
+    case 32: return rows_e<32>(c, which);
     default: return 8;
   }
 }

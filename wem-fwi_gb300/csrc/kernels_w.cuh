@@ -436,7 +436,7 @@ struct Carve {
     taperN = reinterpret_cast<float*>(take((size_t)c.nxg * 4));
     sb0 = reinterpret_cast<float2*>(take((size_t)nbuf * wbuf_len<E>() * 8));
     ring = take((size_t)L.nslots * L.bytes);
-    rows = take((size_t)2 * kW * L.row_bytes);
+    rows = take((size_t)2 * nbuf * L.row_bytes);
     slots = reinterpret_cast<float2*>(take(with_slots ? (size_t)kW * c.nxg * 8 : 0));
   }
 };
@@ -462,10 +462,10 @@ __device__ __forceinline__ void stage_static(const DevCtx& c, const Carve<E>& sm
 
 // =============================================================== passes
 // nonlinear modelling (wem_prop.cpp:52-74), as k_wem in kernels.cu
-template <int E, bool MR, bool NT>
-__global__ void __launch_bounds__(kW * 32, 1) kw_wem(DevCtx c, SlotLayout L, const Group* groups, float2* store,
-                                                     float2* bins) {
-  const Carve<E> sm(c, L, false);
+template <int E, bool MR, bool NT, int R>
+__global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, const Group* groups, float2* store,
+                                                    float2* bins) {
+  const Carve<E> sm(c, L, false, R);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   stage_static<E>(c, sm);
   const Group gp = groups[blockIdx.x];
@@ -1224,11 +1224,19 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
 // rows per CTA of kw_born_adj2 (two warps per row: 16 warps at 128
 // registers; 8 rows measured faster than 6 rows at 168 registers)
 constexpr int kRowsAdj2 = 8;
+// rows per CTA of the single-reference WEM kernel when its buffers fit
+// (16 warps at 128 registers)
+constexpr int kRowsWem = 16;
+
+// which: 4 is WEM with kRowsWem rows per CTA; exchange buffers per CTA
+inline int nbuf_of(int which) { return which == 3 ? 2 * kRowsAdj2 : (which == 4 ? kRowsWem : kW); }
+// the tables a pass reads: as WEM (0), Born forward (1) or Born adjoint (2)
+inline int tables_of(int which) { return which == 4 ? 0 : (which == 3 ? 2 : which); }
 
 template <int E>
 size_t base_bytes(const DevCtx& c, int which) {
   auto r16 = [](size_t b) { return (b + 15) & ~size_t(15); };
-  const int nbuf = which == 3 ? 2 * kRowsAdj2 : kW;
+  const int nbuf = nbuf_of(which);
   return r16((size_t)32 * E * 8) + r16((size_t)32 * E * 4) + r16((size_t)c.nxg * 4) +
          r16((size_t)nbuf * wbuf_len<E>() * 8) + (which == 2 ? r16((size_t)kW * c.nxg * 8) : 0);
 }
@@ -1236,7 +1244,8 @@ size_t base_bytes(const DevCtx& c, int which) {
 // Lays out the ring (and the per-warp rows for WEM) and drops them when the
 // shared memory does not fit.
 template <int E>
-SlotLayout slot_layout(const DevCtx& c, int which, int limit) {
+SlotLayout slot_layout(const DevCtx& c, int pass, int limit) {
+  const int which = tables_of(pass);
   SlotLayout L{};
   int off = 0;
   auto put = [&](int bytes) {
@@ -1257,7 +1266,9 @@ SlotLayout slot_layout(const DevCtx& c, int which, int limit) {
   L.bytes = off;
   L.nslots = 3;
   L.row_bytes = which == 0 ? rowb : 0;
-  auto total = [&]() { return base_bytes<E>(c, which) + (size_t)L.nslots * L.bytes + (size_t)2 * kW * L.row_bytes; };
+  auto total = [&]() {
+    return base_bytes<E>(c, pass) + (size_t)L.nslots * L.bytes + (size_t)2 * nbuf_of(pass) * L.row_bytes;
+  };
   if (total() > (size_t)limit) L.row_bytes = 0;
   if (total() > (size_t)limit) {
     L = SlotLayout{};
@@ -1268,7 +1279,15 @@ SlotLayout slot_layout(const DevCtx& c, int which, int limit) {
 
 template <int E>
 size_t smem_w(const DevCtx& c, int which, const SlotLayout& L) {
-  return base_bytes<E>(c, which) + (size_t)L.nslots * L.bytes + (size_t)2 * kW * L.row_bytes;
+  return base_bytes<E>(c, which) + (size_t)L.nslots * L.bytes + (size_t)2 * nbuf_of(which) * L.row_bytes;
+}
+
+// the 16-row WEM kernel serves this context: one reference, and its buffers
+// and the full ring fit in shared memory
+template <int E>
+bool wem16_fits(const DevCtx& c) {
+  if (c.nref != 1) return false;
+  return slot_layout<E>(c, 4, max_smem_per_block()).nslots == 3;
 }
 
 // kw_born_adj2 serves this context: one reference, and its buffers, the
@@ -1299,16 +1318,26 @@ inline void init_w96() {
 template <int E>
 void launch_wem_w(const DevCtx& c, const Group* g, int ng, float2* store, float2* bins, cudaStream_t st) {
   init_w96();
-  const SlotLayout L = slot_layout<E>(c, 0, max_smem_per_block());
-  const size_t sm = smem_w<E>(c, 0, L);
+  const int pass = wem16_fits<E>(c) ? 4 : 0;
+  const SlotLayout L = slot_layout<E>(c, pass, max_smem_per_block());
+  const size_t sm = smem_w<E>(c, pass, L);
+  const int threads = (pass == 4 ? kRowsWem : kW) * 32;
   auto go = [&](auto kern) {
     cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    kern<<<ng, kW * 32, sm, st>>>(c, L, g, store, bins);
+    kern<<<ng, threads, sm, st>>>(c, L, g, store, bins);
     note_launch();
   };
-  if (c.nref > 1) go(kw_wem<E, true, false>);
-  else if (c.tap == 0) go(kw_wem<E, false, true>);
-  else go(kw_wem<E, false, false>);
+  if (c.nref > 1) go(kw_wem<E, true, false, kW>);
+  else if (pass == 4 && c.tap == 0) go(kw_wem<E, false, true, kRowsWem>);
+  else if (pass == 4) go(kw_wem<E, false, false, kRowsWem>);
+  else if (c.tap == 0) go(kw_wem<E, false, true, kW>);
+  else go(kw_wem<E, false, false, kW>);
+}
+
+// rows per CTA the WEM launcher expects
+template <int E>
+int wem_rows_w(const DevCtx& c) {
+  return wem16_fits<E>(c) ? kRowsWem : kW;
 }
 
 template <int E>

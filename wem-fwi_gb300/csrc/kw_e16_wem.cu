@@ -4,4 +4,5 @@
 namespace wg {
 template void launch_wem_w<16>(const DevCtx&, const Group*, int, float2*, float2*, cudaStream_t);
 template size_t smem_w_e<16>(const DevCtx&, bool);
+template int wem_rows_w<16>(const DevCtx&);
 }  // namespace wg
