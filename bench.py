@@ -137,7 +137,10 @@ def algorithmic_bytes(kernel, p, nfreq, G):
     if kernel == "k_wem":
         return rows * p.nz * 16 * nxg + 2 * tables
     if kernel == "k_born_adj":
-        return rows * p.nz * 32 * nxg + groups * p.nz * 16 * nxg + 4 * tables
+        # stored bg and T (and, with tap 0, the as-coded scatter adjoint and one
+        # Taylor term, the filtered spectra of T) written once and read once
+        fields = 3 if (p.tap == 0 and p.adjoint_mode == 0 and p.ntaylor == 1 and p.nref == 1) else 2
+        return rows * p.nz * 16 * fields * nxg + groups * p.nz * 16 * nxg + 4 * tables
     if kernel == "k_born_fwd":
         return rows * p.nz * 32 * nxg + 2 * tables
     return None

@@ -221,7 +221,7 @@ class Engine {
     int G = wp ? warp_G(0) : pick_G([&](int g) { return smem_wem(ctx_, g); });
     for_chunks(G, plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = store1_.as<float2>((size_t)rows * plane);
-      if (wp) timed("k_wem", [&] { launch_pass_warp(0, ctx_, gd, ng, nullptr, nullptr, A, nullptr, bins, nullptr, nullptr, 0, 0); });
+      if (wp) timed("k_wem", [&] { launch_pass_warp(0, ctx_, gd, ng, nullptr, nullptr, A, nullptr, nullptr, bins, nullptr, nullptr, 0, 0); });
       else timed("k_wem", [&] { launch_wem(ctx_, gd, ng, G, A, bins, 0); });
       cuda_check(cudaGetLastError(), "k_wem launch");
     }, wp);
@@ -243,7 +243,7 @@ class Engine {
     for_chunks(G, 2 * plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = store1_.as<float2>((size_t)rows * plane);
       float2* B = store2_.as<float2>((size_t)rows * plane);
-      if (wp) timed("k_born_fwd", [&] { launch_pass_warp(1, ctx_, gd, ng, dm0, drm, A, B, bins, nullptr, nullptr, 0, 0); });
+      if (wp) timed("k_born_fwd", [&] { launch_pass_warp(1, ctx_, gd, ng, dm0, drm, A, B, nullptr, bins, nullptr, nullptr, 0, 0); });
       else timed("k_born_fwd", [&] { launch_born_fwd(ctx_, gd, ng, G, dm0, drm, A, B, bins, 0); });
       cuda_check(cudaGetLastError(), "k_born_fwd launch");
     }, wp);
@@ -262,13 +262,16 @@ class Engine {
     const bool wp = warp_path();
     int G = wp ? warp_G(2) : pick_G([&](int g) { return smem_born_adj(ctx_, g); });
     const int compat = p_.adjoint_mode == WEM_ADJ_COMPAT ? 1 : 0;
-    // per row: two stored fields; per group: two partial images
-    for_chunks(G, 2 * plane * 8 + (2 * plane * 8 + G - 1) / G, [&](const Group* gd, int ng, int rows) {
+    const bool reuse = wp && !g_plain && warp_adj_reuse(ctx_, compat);
+    const int nfield = reuse ? 3 : 2;
+    // per row: two stored fields (three with spectral reuse); per group: two partial images
+    for_chunks(G, nfield * plane * 8 + (2 * plane * 8 + G - 1) / G, [&](const Group* gd, int ng, int rows) {
       float2* BG = store1_.as<float2>((size_t)rows * plane);
       float2* T = store2_.as<float2>((size_t)rows * plane);
+      float2* SG = reuse ? store3_.as<float2>((size_t)rows * plane) : nullptr;
       float2* pr = part1_.as<float2>((size_t)ng * plane);
       float2* ps = part2_.as<float2>((size_t)ng * plane);
-      if (wp) timed("k_born_adj", [&] { launch_pass_warp(2, ctx_, gd, ng, nullptr, nullptr, BG, T, bins_, pr, ps, compat, 0); });
+      if (wp) timed("k_born_adj", [&] { launch_pass_warp(2, ctx_, gd, ng, nullptr, nullptr, BG, T, SG, bins_, pr, ps, compat, 0); });
       else timed("k_born_adj", [&] { launch_born_adj(ctx_, gd, ng, G, BG, T, bins_, pr, ps, compat, 0); });
       cuda_check(cudaGetLastError(), "k_born_adj launch");
       // chunk-local group ranges of each model slice
@@ -313,7 +316,7 @@ class Engine {
   Buf sref_, ref_, q_, sc_, rc_, a0b_, b0b_, a1b_, b1b_, ph_, fac_, sp_, dp_;
   float2 *a0_ = nullptr, *b0_ = nullptr, *a1_ = nullptr, *b1_ = nullptr;
   // workspaces
-  Buf binsbuf_, groups_, store1_, store2_, part1_, part2_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
+  Buf binsbuf_, groups_, store1_, store2_, store3_, part1_, part2_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
   float2* bins_ = nullptr;
 
   void build_static() {

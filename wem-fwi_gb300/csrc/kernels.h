@@ -86,7 +86,11 @@ int warp_rows_per_group(const DevCtx& c, int which);
 size_t warp_smem_bytes(const DevCtx& c, int which);
 // which: 0 WEM, 1 Born forward, 2 Born adjoint (arguments as the launchers above)
 void launch_pass_warp(int which, const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm,
-                      float2* s1, float2* s2, float2* bins, float2* ir, float2* is, int compat, cudaStream_t st);
+                      float2* s1, float2* s2, float2* s3, float2* bins, float2* ir, float2* is, int compat,
+                      cudaStream_t st);
+// the Born adjoint's warp kernel reuses step spectra in its scatters and
+// then needs s3: [rows][nz][nxg] filtered spectra of the stored T
+bool warp_adj_reuse(const DevCtx& c, int compat);
 
 // ---- background tables on the device (tables.cu)
 void launch_pad_edge(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st);

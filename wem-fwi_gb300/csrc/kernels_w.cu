@@ -9,8 +9,10 @@ template <int E>
 void launch_fwd_w(const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm, float2* sA,
                   float2* sB, float2* bins, cudaStream_t st);
 template <int E>
-void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* sT, float2* bins, float2* ir,
-                  float2* is, int compat, cudaStream_t st);
+void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* sT, float2* sG, float2* bins,
+                  float2* ir, float2* is, int compat, cudaStream_t st);
+template <int E>
+bool adj_reuse_w(const DevCtx& c, int compat);
 template <int E>
 size_t smem_w_e(const DevCtx& c, bool slots);
 template <int E>
@@ -55,21 +57,34 @@ size_t warp_smem_bytes(const DevCtx& c, int which) {
 
 template <int E>
 static void launch_e(int which, const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm,
-                     float2* s1, float2* s2, float2* bins, float2* ir, float2* is, int compat, cudaStream_t st) {
+                     float2* s1, float2* s2, float2* s3, float2* bins, float2* ir, float2* is, int compat,
+                     cudaStream_t st) {
   if (which == 0) launch_wem_w<E>(c, g, ng, s1, bins, st);
   else if (which == 1) launch_fwd_w<E>(c, g, ng, dm, drm, s1, s2, bins, st);
-  else launch_adj_w<E>(c, g, ng, s1, s2, bins, ir, is, compat, st);
+  else launch_adj_w<E>(c, g, ng, s1, s2, s3, bins, ir, is, compat, st);
 }
 
 void launch_pass_warp(int which, const DevCtx& c, const Group* g, int ng, const float2* dm, const float2* drm,
-                      float2* s1, float2* s2, float2* bins, float2* ir, float2* is, int compat, cudaStream_t st) {
+                      float2* s1, float2* s2, float2* s3, float2* bins, float2* ir, float2* is, int compat,
+                      cudaStream_t st) {
   switch (c.N / 32) {
-    case 8: launch_e<8>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st); break;
-    case 12: launch_e<12>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st); break;
-    case 16: launch_e<16>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st); break;
-    case 24: launch_e<24>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st); break;
-    case 32: launch_e<32>(which, c, g, ng, dm, drm, s1, s2, bins, ir, is, compat, st); break;
+    case 8: launch_e<8>(which, c, g, ng, dm, drm, s1, s2, s3, bins, ir, is, compat, st); break;
+    case 12: launch_e<12>(which, c, g, ng, dm, drm, s1, s2, s3, bins, ir, is, compat, st); break;
+    case 16: launch_e<16>(which, c, g, ng, dm, drm, s1, s2, s3, bins, ir, is, compat, st); break;
+    case 24: launch_e<24>(which, c, g, ng, dm, drm, s1, s2, s3, bins, ir, is, compat, st); break;
+    case 32: launch_e<32>(which, c, g, ng, dm, drm, s1, s2, s3, bins, ir, is, compat, st); break;
     default: break;
+  }
+}
+
+bool warp_adj_reuse(const DevCtx& c, int compat) {
+  switch (c.N / 32) {
+    case 8: return adj_reuse_w<8>(c, compat);
+    case 12: return adj_reuse_w<12>(c, compat);
+    case 16: return adj_reuse_w<16>(c, compat);
+    case 24: return adj_reuse_w<24>(c, compat);
+    case 32: return adj_reuse_w<32>(c, compat);
+    default: return false;
   }
 }
 

@@ -333,6 +333,17 @@ __device__ __forceinline__ void sc_mid(const WRow& w, float om, float2 (&X)[E]) 
 }
 // post, one point: i w dz (c_0 u + c_1 filtered) with the mode's conjugations;
 // x is the filtered value (ignored when ntaylor = 0)
+// (k / omega)^2 X: the filtered spectrum of a row whose transform is X / N
+// away (the inverse transform and the filter's forward one cancel when no
+// point is masked between them)
+template <int E>
+__device__ __forceinline__ void sc_spec(const WRow& w, float om, const float2 (&X)[E], float2 (&Y)[E]) {
+#pragma unroll
+  for (int j = 0; j < E; ++j) {
+    const float kw = w.kx[w.lane + 32 * j] / om;
+    Y[j] = c_scale(X[j], kw * kw);
+  }
+}
 __device__ __forceinline__ float2 sc_val(float2 iw, int mode, bool t1, float2 k0, float2 k1, float2 u, float2 x) {
   float2 y = mode == 0 ? c_mul(k0, u) : c_mulc(u, k0);
   if (t1) y = c_add(y, mode == 0 ? c_mul(k1, x) : (mode == 1 ? c_mulc(x, k1) : x));
@@ -980,8 +991,9 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
 // and waited for at its end.
 template <int E, bool NT, int R>
 __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayout L, const Group* groups,
-                                                              float2* storeBG, float2* storeT, const float2* bins,
-                                                              float2* imgR, float2* imgS, int compat) {
+                                                              float2* storeBG, float2* storeT, float2* storeG,
+                                                              const float2* bins, float2* imgR, float2* imgS,
+                                                              int compat) {
   const Carve<E> sm(c, L, false, 2 * R);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = warp >> 1;
   const bool recv = warp & 1;
@@ -1002,6 +1014,13 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
   const float om = c.omega[f];
   const float2 iw = sc_iw(c, om, scmode);
   const bool t1 = c.ntaylor >= 1;
+  // Spectral reuse (tap 0, as-coded scatter adjoint, one Taylor term): no
+  // point is masked between a step's inverse transform and the scatter's
+  // forward one, so the scatter filters the step's spectrum directly.  The
+  // receiver side keeps it in registers; for LinUp^H the down sweep stores
+  // the filtered spectrum of T (storeG) next to T.
+  const bool reuse = NT && compat && t1 && storeG != nullptr;
+  float2* SG = reuse ? storeG + (size_t)(gp.row0 + (act ? row : 0)) * plane : nullptr;
   const float2 zero = make_float2(0.f, 0.f);
   const Ring ring{c, L, sm.ring, Src{nullptr, nullptr}, f};
   const float2* xb0 = sm.sb0;
@@ -1061,8 +1080,20 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
         adj_pre<E, false>(w, T, 0, S, X);
       }
       wfft<E, false>(X, w.sb, w.tw, lane);
-      if (!recv) fwd_mid<E>(w, T, 0, X);
-      else adj_mid<E, false>(w, T, 0, X, Yd);
+      if (!recv) {
+        fwd_mid<E>(w, T, 0, X);
+      } else {
+        adj_mid<E, false>(w, T, 0, X, Yd);
+        if (reuse) {
+          // filtered spectrum of T[z+1], every point (tap 0: N = nxg)
+          float2* g = SG + (size_t)(z + 1) * nxg;
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            const float kw = w.kx[lane + 32 * j] / om;
+            g[lane + 32 * j] = c_scale(X[j], kw * kw);
+          }
+        }
+      }
       wfft<E, true>(X, w.sb, w.tw, lane);
       if (!recv) {
         fwd_post<E, false>(w, T, 0, X, S);
@@ -1131,6 +1162,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
       } else if (lane == 0 && !recv && z >= 2) {
         l2_prefetch(SBG + (size_t)(z - 2) * nxg, nxg * 8);
         l2_prefetch(ST + (size_t)(z - 2) * nxg, nxg * 8);
+        if (reuse) l2_prefetch(SG + (size_t)(z - 2) * nxg, nxg * 8);
       }
       bool wrote = false;
 #pragma unroll 1
@@ -1147,6 +1179,18 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
           } else {
             adj_pre<E, false>(w, T, 0, S, X);
           }
+        } else if (reuse) {
+          if (!recv) {
+            w_load<E>(w, SG + (size_t)(z - 1) * nxg, X);  // filtered spectrum of T[z-1]
+          } else {
+            // X holds q, S the filtered spectrum of q (see the step's post)
+#pragma unroll
+            for (int j = 0; j < E; ++j) {
+              const float2 t = X[j];
+              X[j] = S[j];
+              S[j] = t;
+            }
+          }
         } else if (t1) {
           if (!recv) {
             w_load<E>(w, tp, X);
@@ -1156,10 +1200,17 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
           }
         }
         if (step || t1) {
-          wfft<E, false>(X, w.sb, w.tw, lane);
-          if (!step) sc_mid<E>(w, om, X);
-          else if (!recv) fwd_mid<E>(w, T, 0, X);
-          else adj_mid<E, false>(w, T, 0, X, Yd);
+          if (step || !reuse) {
+            wfft<E, false>(X, w.sb, w.tw, lane);
+            if (!step) {
+              sc_mid<E>(w, om, X);
+            } else if (!recv) {
+              fwd_mid<E>(w, T, 0, X);
+            } else {
+              adj_mid<E, false>(w, T, 0, X, Yd);
+              if (reuse) sc_spec<E>(w, om, X, S);  // wd is spent
+            }
+          }
           wfft<E, true>(X, w.sb, w.tw, lane);
         }
         // post
@@ -1173,9 +1224,9 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
               const float2 r = Tp.rc[x], b = bgp[x];
               if (in) S[j] = c_add(S[j], c_mul(r, b));
             }
-          } else {
+          } else if (!reuse) {
             adj_post<E>(w, X, S);  // S holds q
-          }
+          }  // with reuse X holds q (tap 0: no point to mask)
         } else {
           if (recv) {
 #pragma unroll
@@ -1356,8 +1407,8 @@ void launch_fwd_w(const DevCtx& c, const Group* g, int ng, const float2* dm, con
 }
 
 template <int E>
-void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* sT, float2* bins, float2* ir,
-                  float2* is, int compat, cudaStream_t st) {
+void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* sT, float2* sG, float2* bins,
+                  float2* ir, float2* is, int compat, cudaStream_t st) {
   init_w96();
   const int limit = max_smem_per_block();
   if (adj2_fits<E>(c)) {
@@ -1368,7 +1419,7 @@ void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* 
       const size_t sm3 = smem_w<E>(c, 3, L3);
       auto go = [&](auto kern) {
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
-        kern<<<ng, 2 * kRowsAdj2 * 32, sm3, st>>>(c, L3, g, sBG, sT, bins, ir, is, compat);
+        kern<<<ng, 2 * kRowsAdj2 * 32, sm3, st>>>(c, L3, g, sBG, sT, sG, bins, ir, is, compat);
         note_launch();
       };
       if (c.tap == 0) go(kw_born_adj2<E, true, kRowsAdj2>);
@@ -1391,6 +1442,12 @@ void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* 
 template <int E>
 int adj_rows_w(const DevCtx& c) {
   return adj2_fits<E>(c) ? kRowsAdj2 : kW;
+}
+// the Born adjoint reuses step spectra in its scatters (and then needs the
+// third stored field of filtered spectra)
+template <int E>
+bool adj_reuse_w(const DevCtx& c, int compat) {
+  return adj2_fits<E>(c) && c.tap == 0 && compat && c.ntaylor == 1;
 }
 
 template <int E>

@@ -3,6 +3,7 @@
 
 namespace wg {
 template void launch_adj_w<32>(const DevCtx&, const Group*, int, float2*, float2*, float2*, float2*, float2*,
-                                int, cudaStream_t);
+                                float2*, int, cudaStream_t);
+template bool adj_reuse_w<32>(const DevCtx&, int);
 template int adj_rows_w<32>(const DevCtx&);
 }  // namespace wg
