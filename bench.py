@@ -150,7 +150,7 @@ def run_gpu(args, rank, world):
     import torch
     import wemgpu
     from wemgpu import _lib, synthetic as S
-    from wemgpu.core import BornOp, WemOp
+    from wemgpu.core import BornOp, FwiOp, WemOp
 
     wemgpu.build()
     lib = _lib.load()
@@ -168,14 +168,13 @@ def run_gpu(args, rank, world):
     born = BornOp(p, wav, s0, rho)
     d_obs = torch.zeros((p.ns, p.nr, p.nt), dtype=torch.float32, device=dev)
     wem.forward(s_true, rho, d_obs)
-    d_syn = torch.zeros_like(d_obs)
     g0, g1 = torch.zeros_like(s0), torch.zeros_like(s0)
+    # one gradient step: modelling, residual and loss, Born adjoint of the
+    # residual (the library's fused call, inputs resident on the device)
+    fwi = FwiOp(p, wav)
 
     def step():
-        wem.forward(s0, rho, d_syn)
-        res = d_syn - d_obs
-        born.set_background(s0, rho)
-        born.adjoint(g0, g1, res)
+        fwi.gradient(s0, rho, d_obs, g0, g1)
         if world > 1:
             torch.distributed.all_reduce(g0)
         return g0
@@ -226,7 +225,7 @@ def run_gpu(args, rank, world):
     from wemgpu.autograd import FwiObjective
     s0_pin = torch.from_numpy(cfg["slow"]).pin_memory()
     rho_pin = torch.from_numpy(cfg["rho"]).pin_memory()
-    obj = FwiObjective(p, wav, d_obs, s0, rho)
+    obj = FwiObjective(p, wav, d_obs)
     obj(s0_pin.numpy(), rho_pin.numpy())
     torch.cuda.synchronize()
     t0 = time.perf_counter()

@@ -173,6 +173,22 @@ int born_forward(born_handle* h, const void* dslow2, const void* drho,
 int born_adjoint(born_handle* h, void* dslow2, void* drho,
                  const void* data, int data_kind, int add);
 
+/* ------------------------------------------ FWI objective and gradient
+ * No single reference counterpart: one call for what scripts/fwi.py:70-71,90
+ * composes from NonLinearOperator(wemOp, bornOp) and the solver's L2
+ * residual (python-solver ProblemL2NonLinear):
+ *   loss = 1/2 ||WEM(s2, rho) - d_obs||^2
+ *   (g_slow2, g_rho) = Born^H(WEM(s2, rho) - d_obs) at the background (s2, rho)
+ * with the parameters' adjoint_mode (compat: the reference's gradient as
+ * coded).  d_obs: float [ns][nr][nt] time traces.  Host or device pointers.
+ * The residual and the loss stay on the device, and the tables of the
+ * background are built once for both passes. */
+typedef struct fwi_handle fwi_handle;
+int fwi_create(const wem_params* p, const float* wavelet, fwi_handle** out);
+void fwi_destroy(fwi_handle* h);
+int fwi_gradient(fwi_handle* h, const void* slow2, const void* rho, const void* d_obs,
+                 void* g_slow2, void* g_rho, double* loss);
+
 /* ------------------------------------- frequency-extended operators (ext*) */
 typedef struct extwem_handle extwem_handle;
 typedef struct extborn_handle extborn_handle;

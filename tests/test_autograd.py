@@ -28,7 +28,7 @@ def test_objective_is_born_adjoint_of_residual(gpu_lib, mode):
     from wemgpu.autograd import FwiObjective
     from wemgpu.core import BornOp, WemOp
     p, wav, s, rho, d_obs, torch = _setup(mode)
-    obj = FwiObjective(p, wav, d_obs, s, rho)
+    obj = FwiObjective(p, wav, d_obs)
     loss, g0, g1 = obj(s, rho)  # numpy in, numpy out
     d = np.zeros_like(d_obs)
     WemOp(p, wav).forward(s, rho, d)
@@ -42,6 +42,26 @@ def test_objective_is_born_adjoint_of_residual(gpu_lib, mode):
     l2, t0, t1 = obj(torch.from_numpy(s).to(dev), torch.from_numpy(rho).to(dev))
     assert l2 == pytest.approx(loss, rel=1e-6)
     assert rel_l2(t0.cpu().numpy(), g0) < 1e-6 and rel_l2(t1.cpu().numpy(), g1) < 1e-6
+
+
+@pytest.mark.parametrize("case", ["n768t0", "n256"])
+def test_fwi_gradient_matches_plain_launches(gpu_lib, case):
+    """fwi_gradient with all rows in one launch per pass (grouped, shaped
+    tail) against the same call forced onto one row per launch."""
+    from wemgpu import _lib
+    from wemgpu.core import FwiOp
+    p, wav, s, rho, d_obs, torch = _setup("compat", case)
+    op = FwiOp(p, wav)
+    a0, a1 = np.zeros_like(s), np.zeros_like(s)
+    la = op.gradient(s, rho, d_obs, a0, a1)
+    _lib.call("wem_set_plain", 1)
+    try:
+        b0, b1 = np.zeros_like(s), np.zeros_like(s)
+        lb = op.gradient(s, rho, d_obs, b0, b1)
+    finally:
+        _lib.call("wem_set_plain", 0)
+    assert la == pytest.approx(lb, rel=1e-5)
+    assert rel_l2(a0, b0) < 1e-5 and rel_l2(a1, b1) < 1e-5
 
 
 def test_backward_is_the_transpose_of_born(gpu_lib):

@@ -215,17 +215,43 @@ class Engine {
 
   void wem_forward(const void* s2, const void* rho, void* data, int kind, int add) {
     set_background(s2, rho);
-    float2* bins = zero_bins();
+    zero_bins();
+    wem_pass();
+    emit(data, kind, add);
+  }
+
+  // modelling of the current background into the internal bins
+  void wem_pass() {
     const size_t plane = (size_t)p_.nz * geo_.nxg;
     const bool wp = warp_path();
     int G = wp ? warp_G(0) : pick_G([&](int g) { return smem_wem(ctx_, g); });
     for_chunks(G, plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = store1_.as<float2>((size_t)rows * plane);
-      if (wp) timed("k_wem", [&] { launch_pass_warp(0, ctx_, gd, ng, nullptr, nullptr, A, nullptr, nullptr, bins, nullptr, nullptr, 0, 0); });
-      else timed("k_wem", [&] { launch_wem(ctx_, gd, ng, G, A, bins, 0); });
+      if (wp) timed("k_wem", [&] { launch_pass_warp(0, ctx_, gd, ng, nullptr, nullptr, A, nullptr, nullptr, bins_, nullptr, nullptr, 0, 0); });
+      else timed("k_wem", [&] { launch_wem(ctx_, gd, ng, G, A, bins_, 0); });
       cuda_check(cudaGetLastError(), "k_wem launch");
     }, wp);
-    emit(data, kind, add);
+  }
+
+  // FWI objective and gradient in one call: modelling, residual and loss on
+  // the device, Born adjoint of the residual at the same background (its
+  // tables built once for both passes)
+  double fwi_gradient(const void* s2, const void* rho, const void* dobs, void* g_s2, void* g_rho) {
+    require(s2 && rho && dobs && g_s2 && g_rho, "NULL argument");
+    set_background(s2, rho);
+    zero_bins();
+    wem_pass();
+    // residual r = WEM(m) - d_obs in time, loss = 1/2 |r|^2, r back to bins
+    const size_t nd = (size_t)geo_.ns * geo_.nr * p_.nt;
+    float* syn = dsyn_.as<float>(nd);
+    bins_to_time(syn, 0);
+    Staged obs;
+    obs.in(dobs, nd * 4);
+    const double loss = residual_loss(syn, (const float*)obs.dev, nd);
+    time_to_bins(syn);
+    adj_pass();
+    grad_out(g_s2, g_rho, 0);
+    return loss;
   }
 
   void born_forward(const void* ds2, const void* drho, void* data, int kind, int add) {
@@ -253,8 +279,14 @@ class Engine {
   void born_adjoint(void* ds2, void* drho, const void* data, int kind, int add) {
     require(have_bg_, "background not set");
     require(ds2 && drho && data, "NULL argument");
-    const size_t plane = (size_t)p_.nz * geo_.nxg;
     absorb(data, kind);
+    adj_pass();
+    grad_out(ds2, drho, add);
+  }
+
+  // Born adjoint of the internal bins into the images IR, IS
+  void adj_pass() {
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
     float2* IR = ir_.as<float2>((size_t)M_ * plane);
     float2* IS = is_.as<float2>((size_t)M_ * plane);
     cuda_check(cudaMemsetAsync(IR, 0, (size_t)M_ * plane * 8, 0), "memset");
@@ -276,14 +308,12 @@ class Engine {
       cuda_check(cudaGetLastError(), "k_born_adj launch");
       // chunk-local group ranges of each model slice
       std::vector<int> beg(M_ + 1, 0);
-      std::vector<Group> hg(ng);
-      cuda_check(cudaMemcpy(hg.data(), gd, ng * sizeof(Group), cudaMemcpyDeviceToHost), "D2H groups");
       if (M_ == 1) {
         beg[1] = ng;
       } else {
         int g = 0;
         for (int m = 0; m <= M_; ++m) {
-          while (g < ng && hg[g].f < m) ++g;
+          while (g < ng && chunk_[g].f < m) ++g;
           beg[m] = g;
         }
       }
@@ -292,7 +322,14 @@ class Engine {
       launch_reduce_images(ps, dbeg, M_, plane, IS, 0);
       cuda_check(cudaGetLastError(), "reduce launch");
     }, wp);
+  }
+
+  // images -> gradient [M][nz][nx] x 2 (dR^H of IR plus IS, unpadded)
+  void grad_out(void* ds2, void* drho, int add) {
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
     const size_t nm = (size_t)M_ * p_.nz * p_.nx;
+    float2* IR = ir_.as<float2>((size_t)M_ * plane);
+    float2* IS = is_.as<float2>((size_t)M_ * plane);
     Staged o0, o1;
     o0.out(ds2, nm * 8, add != 0);
     o1.out(drho, nm * 8, add != 0);
@@ -316,7 +353,8 @@ class Engine {
   Buf sref_, ref_, q_, sc_, rc_, a0b_, b0b_, a1b_, b1b_, ph_, fac_, sp_, dp_;
   float2 *a0_ = nullptr, *b0_ = nullptr, *a1_ = nullptr, *b1_ = nullptr;
   // workspaces
-  Buf binsbuf_, groups_, store1_, store2_, store3_, part1_, part2_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
+  std::vector<Group> chunk_;  // host copy of the groups of the current launch
+  Buf binsbuf_, groups_, store1_, store2_, store3_, dsyn_, lossbuf_, part1_, part2_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
   float2* bins_ = nullptr;
 
   void build_static() {
@@ -513,12 +551,17 @@ class Engine {
   // groups of up to G shots of one frequency, sorted by frequency, run in
   // chunks whose storage fits the memory budget; a pass that fits one launch
   // of the warp kernels gets the shaped tail of shaped_groups
-  template <class F>
-  void for_chunks(int G, size_t bytes_per_row, F run, bool shape = false) {
+  // rows whose storage fits the memory budget (60 % of free HBM, at most 96 GB)
+  size_t max_rows_of(size_t bytes_per_row, int G) const {
     size_t freeb = 0, totalb = 0;
     cuda_check(cudaMemGetInfo(&freeb, &totalb), "cudaMemGetInfo");
     size_t budget = std::min<size_t>((size_t)(0.6 * (double)freeb), (size_t)96 << 30);
-    size_t max_rows = std::max<size_t>(G, budget / std::max<size_t>(bytes_per_row, 1));
+    return std::max<size_t>(G, budget / std::max<size_t>(bytes_per_row, 1));
+  }
+
+  template <class F>
+  void for_chunks(int G, size_t bytes_per_row, F run, bool shape = false) {
+    size_t max_rows = max_rows_of(bytes_per_row, G);
     if (g_plain) max_rows = 1;  // one row per launch
     std::vector<Group> all;
     if (shape && !g_plain && (size_t)F_ * geo_.ns <= max_rows) {
@@ -544,6 +587,7 @@ class Engine {
         chunk.push_back(g);
       }
       Group* gd = upload(groups_, chunk);
+      chunk_ = chunk;
       run(gd, (int)chunk.size(), rows);
     }
   }
@@ -562,21 +606,54 @@ class Engine {
     cuda_check(cudaStreamSynchronize(0), "pad");
   }
 
-  // internal bins [ns][nr][F] -> caller data: time traces by one GEMM with
-  // the inverse DFT matrix, frequency data by a window copy
+  // internal bins [ns][nr][F] -> time traces [ns][nr][nt] on the device: one
+  // GEMM with the inverse DFT matrix of the propagated bins
+  void bins_to_time(float* t, int add) {
+    const int ntr = geo_.ns * geo_.nr;
+    cublasHandle_t h = blas_handle();
+    blas_check(cublasSetStream(h, 0), "cublasSetStream");
+    const float one = 1.f, beta = add ? 1.f : 0.f;
+    blas_check(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, p_.nt, ntr, 2 * F_, &one, (const float*)winv_.p, p_.nt,
+                           (const float*)bins_, 2 * F_, &beta, t, p_.nt),
+               "bins to time");
+    note_launch();
+  }
+
+  // time traces on the device -> internal bins
+  void time_to_bins(const float* t) {
+    const int ntr = geo_.ns * geo_.nr;
+    cublasHandle_t h = blas_handle();
+    blas_check(cublasSetStream(h, 0), "cublasSetStream");
+    const float one = 1.f, zero = 0.f;
+    blas_check(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, 2 * F_, ntr, p_.nt, &one, (const float*)wfwd_.p, 2 * F_, t,
+                           p_.nt, &zero, (float*)bins_, 2 * F_),
+               "time to bins");
+    note_launch();
+  }
+
+  // syn <- syn - obs; returns 1/2 |syn - obs|^2 (per-block partial sums in
+  // double, added in block order on the host)
+  double residual_loss(float* syn, const float* obs, size_t n) {
+    const int nblk = residual_blocks();
+    double* part = lossbuf_.as<double>(nblk);
+    launch_residual(syn, obs, n, part, nblk, 0);
+    cuda_check(cudaGetLastError(), "residual launch");
+    std::vector<double> h(nblk);
+    cuda_check(cudaMemcpy(h.data(), part, nblk * sizeof(double), cudaMemcpyDeviceToHost), "D2H loss");
+    double sum = 0;
+    for (double v : h) sum += v;
+    return 0.5 * sum;
+  }
+
+  // internal bins -> caller data: time traces by one GEMM, frequency data by
+  // a window copy
   void emit(void* data, int kind, int add) {
     require(data != nullptr, "data is NULL");
     const int ntr = geo_.ns * geo_.nr;
     Staged o;
     if (kind == WEM_DATA_TIME) {
       o.out(data, (size_t)ntr * p_.nt * 4, add != 0);
-      cublasHandle_t h = blas_handle();
-      blas_check(cublasSetStream(h, 0), "cublasSetStream");
-      const float one = 1.f, beta = add ? 1.f : 0.f;
-      blas_check(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, p_.nt, ntr, 2 * F_, &one, (const float*)winv_.p, p_.nt,
-                             (const float*)bins_, 2 * F_, &beta, (float*)o.dev, p_.nt),
-                 "bins to time");
-      note_launch();
+      bins_to_time((float*)o.dev, add);
     } else {
       require(kind == WEM_DATA_FREQ, "unknown data kind");
       o.out(data, (size_t)ntr * geo_.nbin * 8, add != 0);
@@ -593,13 +670,7 @@ class Engine {
     Staged s;
     if (kind == WEM_DATA_TIME) {
       s.in(data, (size_t)ntr * p_.nt * 4);
-      cublasHandle_t h = blas_handle();
-      blas_check(cublasSetStream(h, 0), "cublasSetStream");
-      const float one = 1.f, zero = 0.f;
-      blas_check(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, 2 * F_, ntr, p_.nt, &one, (const float*)wfwd_.p, 2 * F_,
-                             (const float*)s.dev, p_.nt, &zero, (float*)bins_, 2 * F_),
-                 "time to bins");
-      note_launch();
+      time_to_bins((const float*)s.dev);
     } else {
       require(kind == WEM_DATA_FREQ, "unknown data kind");
       s.in(data, (size_t)ntr * geo_.nbin * 8);
@@ -731,6 +802,7 @@ struct wem_handle { std::unique_ptr<Engine> e; };
 struct born_handle { std::unique_ptr<Engine> e; };
 struct extwem_handle { std::unique_ptr<Engine> e; };
 struct extborn_handle { std::unique_ptr<Engine> e; };
+struct fwi_handle { std::unique_ptr<Engine> e; };
 struct wemop_handle { std::unique_ptr<RowOps> r; };
 
 extern "C" {
@@ -838,6 +910,23 @@ void extwem_destroy(extwem_handle* h) { delete h; }
 int extwem_forward(extwem_handle* h, const void* s2, const void* rho, void* data, int kind, int add) {
   return guard([&] { require(h != nullptr, "NULL handle"); h->e->wem_forward(s2, rho, data, kind, add); });
 }
+int fwi_create(const wem_params* p, const float* wavelet, fwi_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<fwi_handle>();
+    h->e = std::make_unique<Engine>(*p, wavelet, false, true);
+    *out = h.release();
+  });
+}
+void fwi_destroy(fwi_handle* h) { delete h; }
+int fwi_gradient(fwi_handle* h, const void* s2, const void* rho, const void* d_obs, void* g_s2, void* g_rho,
+                 double* loss) {
+  return guard([&] {
+    require(h != nullptr && loss != nullptr, "NULL argument");
+    *loss = h->e->fwi_gradient(s2, rho, d_obs, g_s2, g_rho);
+  });
+}
+
 int extborn_create(const wem_params* p, const float* wavelet, const void* s2, const void* rho,
                    extborn_handle** out) {
   return guard([&] {

@@ -111,6 +111,9 @@ void launch_grad_assemble(const DevCtx& c, int M, const float2* a0, const float2
                           const float2* b1, const float2* IR, const float2* IS, float2* g0, float2* g1, int nx,
                           int add, cudaStream_t st);
 // traces: time [ntr][nt] <-> bins [ntr][n]
+// syn <- syn - obs; part[nblk] per-CTA sums of the squares (double)
+int residual_blocks();
+void launch_residual(float* syn, const float* obs, size_t n, double* part, int nblk, cudaStream_t st);
 // caller bins [nrows][ldu] <-> compact propagated bins [nrows][nf] (window at off)
 void launch_bin_window(const float2* src, float2* dst, int nrows, int ldu, int nf, int off, int to_user, int add,
                        cudaStream_t st);

@@ -18,7 +18,7 @@ def __getattr__(name):
     if name in ("WEM", "Born", "extWEM", "extBorn", "Propagator"):
         from . import ops
         return getattr(ops, name)
-    if name in ("WemOp", "BornOp", "ExtWemOp", "ExtBornOp", "RowOps"):
+    if name in ("WemOp", "BornOp", "ExtWemOp", "ExtBornOp", "RowOps", "FwiOp"):
         from . import core
         return getattr(core, name)
     raise AttributeError(name)

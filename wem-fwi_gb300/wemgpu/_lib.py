@@ -49,6 +49,9 @@ _SIGS = {
     "extborn_set_background": (_i, [_h, _v, _v]),
     "extborn_forward": (_i, [_h, _v, _v, _v, _i, _i]),
     "extborn_adjoint": (_i, [_h, _v, _v, _v, _i, _i]),
+    "fwi_create": (_i, [_pp, _v, ctypes.POINTER(_h)]),
+    "fwi_destroy": (None, [_h]),
+    "fwi_gradient": (_i, [_h, _v, _v, _v, _v, _v, ctypes.POINTER(ctypes.c_double)]),
     "wemop_create": (_i, [_pp, _v, _i, ctypes.POINTER(_h)]),
     "wemop_destroy": (None, [_h]),
     "wemop_onestep": (_i, [_h, _i, _f, _i, _v, _v, _i, _i]),

@@ -20,16 +20,16 @@ leaves get the reference's Born-linearised gradient:
 For a real loss and complex leaves, torch's gradient is dL/dRe + i dL/dIm.
 That is B^H r for real time data r, which is what the Born adjoint returns.
 
-Memory: the Born adjoint stores two wavefields per (shot, frequency) row.
-The library bounds that storage by running the rows in chunks sized to free
-HBM, so no depth checkpointing is needed for the stored fields.
+Memory: the Born adjoint stores two or three wavefields per (shot,
+frequency) row.  The library bounds that storage by running the rows in
+chunks sized to free HBM, so no depth checkpointing is needed.
 """
 from __future__ import annotations
 
 import numpy as np
 import torch
 
-from .core import BornOp, WemOp
+from .core import BornOp, FwiOp, WemOp
 from .params import WemParams
 
 
@@ -66,23 +66,23 @@ class FwiObjective:
     """The L2 FWI objective and its gradient, one call per iteration.
 
     ``obj(s2, rho) -> (loss, g_s2, g_rho)``, with
-    loss = 1/2 ||WEM(s2, rho) - d_obs||^2 and g = Born^H(WEM(s2, rho) - d_obs).
+    loss = 1/2 ||WEM(s2, rho) - d_obs||^2 and g = Born^H(WEM(s2, rho) - d_obs),
+    computed by one library call (``FwiOp``, ``fwi_gradient``): the residual
+    and loss stay on the device and the background tables are built once.
 
     d_obs (``[ns][nr][nt]`` float32, numpy or a CUDA tensor) is copied to the
     device once.  Models may be numpy arrays (the call copies them in, and the
-    gradients out, through pinned buffers) or CUDA tensors (no copies).
+    gradients out, through pinned buffers) or CUDA tensors (no copies; the
+    gradients are returned as new CUDA tensors).
     """
 
-    def __init__(self, p: WemParams, wavelet, d_obs, s2_init, rho_init, device=None):
+    def __init__(self, p: WemParams, wavelet, d_obs, device=None):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
-        self.wem = WemOp(p, wavelet)
-        s2_init = torch.as_tensor(s2_init).to(self.device).contiguous()
-        rho_init = torch.as_tensor(rho_init).to(self.device).contiguous()
-        self.born = BornOp(p, wavelet, s2_init, rho_init)
+        self.op = FwiOp(p, wavelet)
         self.d_obs = torch.as_tensor(d_obs).to(self.device, torch.float32).contiguous()
-        if tuple(self.d_obs.shape) != tuple(self.wem.data_shape(0)):
-            raise ValueError(f"d_obs shape {tuple(self.d_obs.shape)} != {self.wem.data_shape(0)}")
-        shape = self.wem.model_shape
+        if tuple(self.d_obs.shape) != tuple(self.op.data_shape(0)):
+            raise ValueError(f"d_obs shape {tuple(self.d_obs.shape)} != {self.op.data_shape(0)}")
+        shape = self.op.model_shape
         self._dev_in = [torch.empty(shape, dtype=torch.complex64, device=self.device) for _ in range(2)]
         self._pin_out = [torch.empty(shape, dtype=torch.complex64).pin_memory() for _ in range(2)]
         self.h2d_bytes = 0
@@ -99,16 +99,12 @@ class FwiObjective:
     def __call__(self, s2, rho):
         s2_d, host = self._to_device(s2, 0)
         rho_d, _ = self._to_device(rho, 1)
-        with torch.enable_grad():
-            a = s2_d.detach().requires_grad_(True)
-            b = rho_d.detach().requires_grad_(True)
-            d = modelled_data(a, b, self.wem, self.born)
-            loss = 0.5 * torch.sum((d - self.d_obs) ** 2)
-            loss.backward()
-        value = float(loss.detach())
+        g0 = torch.empty_like(s2_d)
+        g1 = torch.empty_like(rho_d)
+        loss = self.op.gradient(s2_d, rho_d, self.d_obs, g0, g1)
         if not host:
-            return value, a.grad, b.grad
-        self._pin_out[0].copy_(a.grad)
-        self._pin_out[1].copy_(b.grad)
-        self.d2h_bytes = 2 * a.grad.numel() * 8 + 4
-        return value, self._pin_out[0].numpy().copy(), self._pin_out[1].numpy().copy()
+            return loss, g0, g1
+        self._pin_out[0].copy_(g0)
+        self._pin_out[1].copy_(g1)
+        self.d2h_bytes = 2 * g0.numel() * 8 + 8
+        return loss, self._pin_out[0].numpy().copy(), self._pin_out[1].numpy().copy()

@@ -140,6 +140,28 @@ class BornOp(_Base):
         return ds2, drho
 
 
+class FwiOp(_Base):
+    """FWI objective and gradient in one call (fwi_gradient): the loss
+    1/2 ||WEM(m) - d_obs||^2 and the Born adjoint of the residual at m, as
+    scripts/fwi.py:70-71,90 composes them from WEM and Born."""
+
+    _destroy = "fwi_destroy"
+
+    def __init__(self, p: WemParams, wavelet):
+        super().__init__(p, wavelet)
+        _lib.call("fwi_create", ctypes.byref(self.p), self.wavelet.ctypes.data_as(ctypes.c_void_p),
+                  ctypes.byref(self.h))
+
+    def gradient(self, s2, rho, d_obs, g_s2, g_rho) -> float:
+        loss = ctypes.c_double()
+        _lib.call("fwi_gradient", self.h, ptr(s2, np.complex64, self.model_shape, "slowness"),
+                  ptr(rho, np.complex64, self.model_shape, "density"),
+                  ptr(d_obs, np.float32, self.data_shape(WEM_DATA_TIME), "d_obs"),
+                  ptr(g_s2, np.complex64, self.model_shape, "g_slowness", True),
+                  ptr(g_rho, np.complex64, self.model_shape, "g_density", True), ctypes.byref(loss))
+        return loss.value
+
+
 class ExtWemOp(WemOp):
     """Frequency-extended modelling (extWEM, propagator/src/extWEM.cpp:9-70)."""
 
