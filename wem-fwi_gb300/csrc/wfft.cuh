@@ -18,9 +18,10 @@
 // N - E), so the 32 lanes of a twiddle load read consecutive l.
 //
 // Shared-memory banks: the exchange buffer pads one slot every 2^k points
-// (k = 4 for E = 8, 16; k = 5 for E = 12, 24, 32), chosen by counting the
+// (k = 4 for E = 8, 16; k = 5 for E = 12, 32), chosen by counting the
 // wavefronts of every exchange write and read of each plan; the natural-order
 // reads stay conflict-free and fold the padding into immediate offsets.
+// E = 24 uses rows of 24 points padded by one (rows_layout).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -123,9 +124,22 @@ template <int E>
 __device__ __forceinline__ int swz(int i) {
   return i + (i >> swz_shift<E>());
 }
+// E = 24 lays the exchange out as rows of E points padded by one slot
+// instead: every exchange address is then a per-butterfly base plus
+// compile-time offsets, and the stage-0 writes (stride E + 1) are free of
+// bank conflicts
+template <int E>
+__host__ __device__ constexpr bool rows_layout() {
+  return E == 24;
+}
+template <int E>
+__device__ __forceinline__ int xaddr(int i) {
+  if constexpr (rows_layout<E>()) return (i / E) * (E + 1) + i % E;
+  else return swz<E>(i);
+}
 template <int E>
 __host__ __device__ constexpr int wbuf_len() {
-  return 32 * E + ((32 * E) >> swz_shift<E>()) + 2;
+  return (rows_layout<E>() ? 32 * (E + 1) : 32 * E + ((32 * E) >> swz_shift<E>())) + 2;
 }
 
 // offset of stage S's twiddles in the per-stage table: sum over 1 <= s < S of
@@ -167,6 +181,13 @@ __device__ __forceinline__ void wfft_stage(float2 (&v)[E], float2* sb, const flo
     if constexpr (LAST) {
 #pragma unroll
       for (int q = 0; q < R; ++q) v[m + q * M] = a[q];
+    } else if constexpr (rows_layout<E>()) {
+      // positions o + q L of one row (L = 1) or of rows L / E apart
+      static_assert(L == 1 || L % E == 0, "row layout needs L = 1 or a multiple of E");
+      constexpr int STEP = (L == 1) ? 1 : (L / E) * (E + 1);
+      const int a0 = xaddr<E>((b - l) * R + l);
+#pragma unroll
+      for (int q = 0; q < R; ++q) sb[a0 + q * STEP] = a[q];
     } else {
       const int o = (b - l) * R + l;
 #pragma unroll
@@ -175,8 +196,22 @@ __device__ __forceinline__ void wfft_stage(float2 (&v)[E], float2* sb, const flo
   }
   if constexpr (!LAST) {
     __syncwarp();
+    if constexpr (rows_layout<E>()) {
+      // natural order, read per butterfly of the next stage: positions
+      // lane + 32 m + r 32 M2 lie 32 M2 / E rows apart
+      constexpr int R2 = WPlan<E>::r(S + 1), M2 = E / R2;
+      static_assert((32 * M2) % E == 0, "row layout needs 32 E / R2 to be a multiple of E");
+      constexpr int RSTEP = (32 * M2 / E) * (E + 1);
 #pragma unroll
-    for (int j = 0; j < E; ++j) v[j] = sb[swz<E>(lane + 32 * j)];
+      for (int m = 0; m < M2; ++m) {
+        const int base = xaddr<E>(lane + 32 * m);
+#pragma unroll
+        for (int r = 0; r < R2; ++r) v[m + r * M2] = sb[base + r * RSTEP];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < E; ++j) v[j] = sb[swz<E>(lane + 32 * j)];
+    }
     __syncwarp();
     wfft_stage<E, INV, S + 1, L * R>(v, sb, tw, lane);
   }
