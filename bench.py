@@ -118,7 +118,7 @@ def workload(small=False):
 # profiles/kw_born_adj2_e24_c3_small.md): the traffic of a launch scales with
 # the rows it carries, so a full launch is this figure x rows x depths.
 TRAFFIC_PER_ROW_DEPTH = {
-    "k_born_adj": (708894720 + 696811520) / (168 * 300),
+    "k_born_adj": (1014829999 + 1006327999) / (168 * 300),
 }
 
 
