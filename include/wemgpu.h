@@ -173,6 +173,33 @@ int born_forward(born_handle* h, const void* dslow2, const void* drho,
 int born_adjoint(born_handle* h, void* dslow2, void* drho,
                  const void* data, int data_kind, int add);
 
+/* ---------------------------------- frequency-extended Born variants
+ * BornRefl: replaces pyWEM.BornRefl (pyWEM.cpp:83-97; BornRefl.cpp,
+ * ext_born_refl.cpp:8-105).  model: complex [nfreq][nz][nx] reflectivity
+ * per frequency; forward records Up(bg m_f), adjoint gives the image
+ * sum over shots of conj(bg) Up^H(data) per frequency.
+ * BornTomo: replaces pyWEM.BornTomo (pyWEM.cpp:101-115; BornTomo.cpp,
+ * ext_born_tomo.cpp:9-119).  model: complex [nz][nx] slowness^2
+ * perturbation; the down- and up-scattering terms of BornFull with the
+ * reflectivity set by borntomo_set_refl ([nfreq][nz][nx]) in place of R.
+ * Backgrounds are slowness^2 only (the reference takes no density). */
+typedef struct bornrefl_handle bornrefl_handle;
+int bornrefl_create(const wem_params* p, const float* wavelet, const void* bg_slow2, bornrefl_handle** out);
+void bornrefl_destroy(bornrefl_handle* h);
+/* replaces BornRefl::setBgSlow (BornRefl.h:25-29) */
+int bornrefl_set_background(bornrefl_handle* h, const void* bg_slow2);
+int bornrefl_forward(bornrefl_handle* h, const void* model, void* data, int data_kind, int add);
+int bornrefl_adjoint(bornrefl_handle* h, void* model, const void* data, int data_kind, int add);
+
+typedef struct borntomo_handle borntomo_handle;
+int borntomo_create(const wem_params* p, const float* wavelet, const void* bg_slow2, borntomo_handle** out);
+void borntomo_destroy(borntomo_handle* h);
+/* replaces BornTomo::setBgSlow / setBgRefl (BornTomo.h:36-43) */
+int borntomo_set_background(borntomo_handle* h, const void* bg_slow2);
+int borntomo_set_refl(borntomo_handle* h, const void* refl);
+int borntomo_forward(borntomo_handle* h, const void* dslow2, void* data, int data_kind, int add);
+int borntomo_adjoint(borntomo_handle* h, void* dslow2, const void* data, int data_kind, int add);
+
 /* ------------------------------------------ FWI objective and gradient
  * No single reference counterpart: one call for what scripts/fwi.py:70-71,90
  * composes from NonLinearOperator(wemOp, bornOp) and the solver's L2

@@ -146,6 +146,39 @@ def extborn_adjoint(p, wavelet, bs2, brho, data, kind=WEM_DATA_FREQ, add=False, 
     return ds2, drho
 
 
+def bornrefl_forward(p, wavelet, bs2, model, kind=WEM_DATA_TIME, data=None, add=False, prec=32, nthreads=0):
+    """BornRefl (ext_born_refl.cpp:8-57): model [nfreq][nz][nx] reflectivity per frequency."""
+    out = _data_out(p, kind, data)
+    _call("oracle_bornrefl_forward", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(bs2)), _ptr(_c64(model)), _ptr(out), kind, int(add), prec, nthreads)
+    return out
+
+
+def bornrefl_adjoint(p, wavelet, bs2, data, kind=WEM_DATA_TIME, add=False, prec=32, nthreads=0):
+    nf = count_freqs(p)[0]
+    model = np.zeros((nf, p.nz, p.nx), np.complex64)
+    d = np.ascontiguousarray(data, np.float32 if kind == WEM_DATA_TIME else np.complex64)
+    _call("oracle_bornrefl_adjoint", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(bs2)), _ptr(model), _ptr(d), kind, int(add), prec, nthreads)
+    return model
+
+
+def borntomo_forward(p, wavelet, bs2, refl, dm, kind=WEM_DATA_TIME, data=None, add=False, prec=32, nthreads=0):
+    """BornTomo (ext_born_tomo.cpp:9-57): dm [nz][nx], refl [nfreq][nz][nx]."""
+    out = _data_out(p, kind, data)
+    _call("oracle_borntomo_forward", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(bs2)), _ptr(_c64(refl)), _ptr(_c64(dm)), _ptr(out), kind, int(add), prec, nthreads)
+    return out
+
+
+def borntomo_adjoint(p, wavelet, bs2, refl, data, kind=WEM_DATA_TIME, add=False, prec=32, nthreads=0):
+    dm = np.zeros((p.nz, p.nx), np.complex64)
+    d = np.ascontiguousarray(data, np.float32 if kind == WEM_DATA_TIME else np.complex64)
+    _call("oracle_borntomo_adjoint", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(bs2)), _ptr(_c64(refl)), _ptr(dm), _ptr(d), kind, int(add), prec, nthreads)
+    return dm
+
+
 def onestep(p, slow_padded, iz, freq, adj, x, out=None, add=False, prec=32):
     x = _c64(x)
     nxg = slow_padded.shape[-1]

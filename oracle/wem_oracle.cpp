@@ -482,6 +482,193 @@ void extborn_adjoint(const wem_params& p, const float* wavelet, const float* bs2
   store(drho, m1.data(), nm * nf, add);
 }
 
+// ------------------------------------------- BornRefl / BornTomo (f3)
+// One complex field [slices][nz][nx] padded to [slices][nz][nxg].
+template <class R>
+std::vector<C<R>> pad_field(const wem_params& p, const float* a, int slices, bool extend) {
+  const int nxg = p.nx + 2 * p.pad;
+  const size_t n = (size_t)p.nx * p.nz, ng = (size_t)nxg * p.nz;
+  std::vector<C<R>> out(ng * slices);
+  for (int k = 0; k < slices; ++k) {
+    std::vector<C<R>> v = load<R>(a + 2 * n * k, n);
+    pad_x(v.data(), out.data() + ng * k, p.nz, p.nx, p.pad, extend);
+  }
+  return out;
+}
+
+// BornRefl::fwd_propagate (ext_born_refl.cpp:8-57): per (frequency, shot)
+// bg = Down(src); sc = bg m_f (IC::forward); Up in place; record.
+template <class R>
+void bornrefl_forward(const wem_params& p, const float* wavelet, const float* bs2, const float* model, void* data,
+                      int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
+  std::vector<C<R>> sp = pad_field<R>(p, bs2, 1, true);
+  std::vector<C<R>> m = pad_field<R>(p, model, nf, false);
+  Core<R> core(p, sp.data(), nx, nz);
+  DataF<R> D = new_dataf(P);
+  const size_t ng = (size_t)nx * nz;
+  parallel_for(nf, nthreads, [&](int f, int) {
+    const int bin = P.F.bin[f];
+    R w = Core<R>::omega(P.F.freq[f]);
+    Inject<R> rec = P.rec_inj();
+    std::vector<C<R>> vals(rec.ix.size()), bg(ng), sc(ng);
+    Work<R> wk(core.N, nx);
+    for (int is = 0; is < p.ns; ++is) {
+      std::fill(bg.begin(), bg.end(), C<R>(0));
+      C<R> wv = P.wave_f[bin];
+      P.src_inj(is).spread(bg.data(), nx, &wv);
+      down_fwd(core, w, bg.data(), bg.data(), true, wk);
+      for (size_t i = 0; i < ng; ++i) sc[i] = bg[i] * m[ng * f + i];
+      up_fwd(core, w, sc.data(), sc.data(), true, wk);
+      for (size_t i = 0; i < vals.size(); ++i) vals[i] = *D.at(is, (int)i, bin);
+      rec.gather(sc.data(), nx, vals.data());
+      for (size_t i = 0; i < vals.size(); ++i) *D.at(is, (int)i, bin) = vals[i];
+    }
+  });
+  emit_data(P, D, data, kind, add, nthreads);
+}
+
+// BornRefl::adj_propagate (ext_born_refl.cpp:60-105): image_f += conj(bg) Up^H(rec)
+template <class R>
+void bornrefl_adjoint(const wem_params& p, const float* wavelet, const float* bs2, float* model, const void* data,
+                      int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
+  std::vector<C<R>> sp = pad_field<R>(p, bs2, 1, true);
+  Core<R> core(p, sp.data(), nx, nz);
+  DataF<R> D = absorb_data(P, data, kind, nthreads);
+  const size_t ng = (size_t)nx * nz, nm = (size_t)p.nx * nz;
+  std::vector<C<R>> out(nm * nf);
+  parallel_for(nf, nthreads, [&](int f, int) {
+    const int bin = P.F.bin[f];
+    R w = Core<R>::omega(P.F.freq[f]);
+    Inject<R> rec = P.rec_inj();
+    std::vector<C<R>> vals(rec.ix.size()), bg(ng), sc(ng), img(ng, C<R>(0));
+    Work<R> wk(core.N, nx);
+    for (int is = 0; is < p.ns; ++is) {
+      std::fill(bg.begin(), bg.end(), C<R>(0));
+      C<R> wv = P.wave_f[bin];
+      P.src_inj(is).spread(bg.data(), nx, &wv);
+      down_fwd(core, w, bg.data(), bg.data(), true, wk);
+      std::fill(sc.begin(), sc.end(), C<R>(0));
+      for (size_t i = 0; i < vals.size(); ++i) vals[i] = *D.at(is, (int)i, bin);
+      rec.spread(sc.data(), nx, vals.data());
+      up_adj(core, w, sc.data(), sc.data(), true, wk);
+      for (size_t i = 0; i < ng; ++i) img[i] += std::conj(bg[i]) * sc[i];
+    }
+    for (int iz = 0; iz < nz; ++iz)
+      for (int ix = 0; ix < p.nx; ++ix) out[nm * f + (size_t)iz * p.nx + ix] = img[(size_t)iz * nx + ix + p.pad];
+  });
+  store(model, out.data(), nm * nf, add);
+}
+
+// BornTomo::fwd_propagate (ext_born_tomo.cpp:9-57): Born_down (LinDown,
+// Down, reflectivity, Up, record; Born_down.cpp:14-27) and Born_up on the
+// up background Up(refl_f bg) (Born_up.cpp:14-22)
+template <class R>
+void borntomo_forward(const wem_params& p, const float* wavelet, const float* bs2, const float* refl,
+                      const float* dm, void* data, int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
+  std::vector<C<R>> sp = pad_field<R>(p, bs2, 1, true);
+  std::vector<C<R>> rf = pad_field<R>(p, refl, nf, true);
+  std::vector<C<R>> g = pad_field<R>(p, dm, 1, false);
+  Core<R> core(p, sp.data(), nx, nz);
+  DataF<R> D = new_dataf(P);
+  const size_t ng = (size_t)nx * nz;
+  parallel_for(nf, nthreads, [&](int f, int) {
+    const int bin = P.F.bin[f];
+    R w = Core<R>::omega(P.F.freq[f]);
+    Inject<R> rec = P.rec_inj();
+    std::vector<C<R>> vals(rec.ix.size()), bg(ng), sc(ng);
+    const C<R>* r = rf.data() + ng * f;
+    Work<R> wk(core.N, nx);
+    auto record = [&](int is) {
+      for (size_t i = 0; i < vals.size(); ++i) vals[i] = *D.at(is, (int)i, bin);
+      rec.gather(sc.data(), nx, vals.data());
+      for (size_t i = 0; i < vals.size(); ++i) *D.at(is, (int)i, bin) = vals[i];
+    };
+    for (int is = 0; is < p.ns; ++is) {
+      std::fill(bg.begin(), bg.end(), C<R>(0));
+      C<R> wv = P.wave_f[bin];
+      P.src_inj(is).spread(bg.data(), nx, &wv);
+      down_fwd(core, w, bg.data(), bg.data(), true, wk);
+      lindown_fwd(core, w, bg.data(), g.data(), sc.data(), false, wk);
+      down_fwd(core, w, sc.data(), sc.data(), true, wk);
+      for (size_t i = 0; i < ng; ++i) sc[i] = r[i] * sc[i];
+      up_fwd(core, w, sc.data(), sc.data(), true, wk);
+      record(is);
+      for (size_t i = 0; i < ng; ++i) bg[i] = r[i] * bg[i];
+      up_fwd(core, w, bg.data(), bg.data(), true, wk);
+      linup_fwd(core, w, bg.data(), g.data(), sc.data(), false, wk);
+      up_fwd(core, w, sc.data(), sc.data(), true, wk);
+      record(is);
+    }
+  });
+  emit_data(P, D, data, kind, add, nthreads);
+}
+
+// BornTomo::adj_propagate (ext_born_tomo.cpp:62-119).  All (frequency, shot)
+// terms add into one model.  As coded, every LinDown^H zeroes that model's
+// last depth row (LinOneWay.cpp:64-65): in the reference's order (frequencies,
+// then shots) the row ends with the LinUp^H term of the last (f, s) alone, so
+// the as-coded mode runs the terms in that order in one task.
+template <class R>
+void borntomo_adjoint(const wem_params& p, const float* wavelet, const float* bs2, const float* refl, float* dm,
+                      const void* data, int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
+  const bool exact = p.adjoint_mode == WEM_ADJ_EXACT;
+  std::vector<C<R>> sp = pad_field<R>(p, bs2, 1, true);
+  std::vector<C<R>> rf = pad_field<R>(p, refl, nf, true);
+  Core<R> core(p, sp.data(), nx, nz);
+  DataF<R> D = absorb_data(P, data, kind, nthreads);
+  const size_t ng = (size_t)nx * nz, nm = (size_t)p.nx * nz;
+  const int ntask = exact ? nf : 1;
+  std::vector<std::vector<C<R>>> part(ntask, std::vector<C<R>>(ng, C<R>(0)));
+  parallel_for(ntask, nthreads, [&](int t, int) {
+    const int fb = exact ? t : 0, fe = exact ? t + 1 : nf;
+    Inject<R> rec = P.rec_inj();
+    std::vector<C<R>> vals(rec.ix.size()), bg(ng), sc(ng);
+    std::vector<C<R>>& M = part[t];
+    Work<R> wk(core.N, nx);
+    for (int f = fb; f < fe; ++f) {
+      const int bin = P.F.bin[f];
+      R w = Core<R>::omega(P.F.freq[f]);
+      const C<R>* r = rf.data() + ng * f;
+      auto inject_data = [&](int is) {
+        std::fill(sc.begin(), sc.end(), C<R>(0));
+        for (size_t i = 0; i < vals.size(); ++i) vals[i] = *D.at(is, (int)i, bin);
+        rec.spread(sc.data(), nx, vals.data());
+      };
+      for (int is = 0; is < p.ns; ++is) {
+        std::fill(bg.begin(), bg.end(), C<R>(0));
+        C<R> wv = P.wave_f[bin];
+        P.src_inj(is).spread(bg.data(), nx, &wv);
+        down_fwd(core, w, bg.data(), bg.data(), true, wk);
+        // Born_down::adjoint (Born_down.cpp:29-41)
+        inject_data(is);
+        up_adj(core, w, sc.data(), sc.data(), true, wk);
+        for (size_t i = 0; i < ng; ++i) sc[i] = std::conj(r[i]) * sc[i];
+        down_adj(core, w, sc.data(), sc.data(), true, wk);
+        lindown_adj(core, w, bg.data(), M.data(), sc.data(), true, exact, wk);
+        // up background, then Born_up::adjoint (Born_up.cpp:24-31)
+        for (size_t i = 0; i < ng; ++i) bg[i] = r[i] * bg[i];
+        up_fwd(core, w, bg.data(), bg.data(), true, wk);
+        inject_data(is);
+        up_adj(core, w, sc.data(), sc.data(), true, wk);
+        linup_adj(core, w, bg.data(), M.data(), sc.data(), true, exact, wk);
+      }
+    }
+  });
+  std::vector<C<R>> out(nm, C<R>(0));
+  for (int t = 0; t < ntask; ++t)
+    for (int iz = 0; iz < nz; ++iz)
+      for (int ix = 0; ix < p.nx; ++ix) out[(size_t)iz * p.nx + ix] += part[t][(size_t)iz * nx + ix + p.pad];
+  store(dm, out.data(), nm, add);
+}
+
 // ---------------------------------------------------- row-level operators
 template <class R>
 struct RowOp {
@@ -583,6 +770,35 @@ int oracle_extborn_forward(const wem_params* p, const float* wavelet, const floa
   return run_guarded([&] {
     if (prec == 64) extborn_forward<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
     else extborn_forward<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+  });
+}
+
+int oracle_bornrefl_forward(const wem_params* p, const float* wavelet, const float* bs2, const float* model,
+                            void* data, int kind, int add, int prec, int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) bornrefl_forward<double>(*p, wavelet, bs2, model, data, kind, add, nthreads);
+    else bornrefl_forward<float>(*p, wavelet, bs2, model, data, kind, add, nthreads);
+  });
+}
+int oracle_bornrefl_adjoint(const wem_params* p, const float* wavelet, const float* bs2, float* model,
+                            const void* data, int kind, int add, int prec, int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) bornrefl_adjoint<double>(*p, wavelet, bs2, model, data, kind, add, nthreads);
+    else bornrefl_adjoint<float>(*p, wavelet, bs2, model, data, kind, add, nthreads);
+  });
+}
+int oracle_borntomo_forward(const wem_params* p, const float* wavelet, const float* bs2, const float* refl,
+                            const float* dm, void* data, int kind, int add, int prec, int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) borntomo_forward<double>(*p, wavelet, bs2, refl, dm, data, kind, add, nthreads);
+    else borntomo_forward<float>(*p, wavelet, bs2, refl, dm, data, kind, add, nthreads);
+  });
+}
+int oracle_borntomo_adjoint(const wem_params* p, const float* wavelet, const float* bs2, const float* refl,
+                            float* dm, const void* data, int kind, int add, int prec, int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) borntomo_adjoint<double>(*p, wavelet, bs2, refl, dm, data, kind, add, nthreads);
+    else borntomo_adjoint<float>(*p, wavelet, bs2, refl, dm, data, kind, add, nthreads);
   });
 }
 

@@ -346,3 +346,38 @@ def test_exact_kz_phase_law(gpu_lib, oracle, case):
     q0, q1 = oracle.born_adjoint(p, wav, s, rho, dd, kind=WEM_DATA_TIME, prec=64)
     assert rel_l2(a0, q0) < TOL_OP, rel_l2(a0, q0)
     assert rel_l2(a1, q1) < TOL_OP, rel_l2(a1, q1)
+
+
+@pytest.mark.parametrize("case", ["small", "n256", "n768t0"])
+@pytest.mark.parametrize("mode", ["compat", "exact"])
+def test_bornrefl_borntomo(gpu_lib, oracle, case, mode):
+    """BornRefl / BornTomo (ext_born_refl.cpp, ext_born_tomo.cpp) on the Born
+    passes against the oracle."""
+    from wemgpu.core import BornReflOp, BornTomoOp
+    kw = {} if case == "small" else dict(WARP_CASES[case])
+    p, par, wav, s, rho = small_case(nz=12, ns=3, adjoint_mode=mode, **kw)
+    nf = oracle.count_freqs(p)[0]
+    rng = np.random.default_rng(41)
+    m = rand_c(rng, (nf, p.nz, p.nx)) * 0.1
+    d = (rng.random((p.ns, p.nr, p.nt)) - .5).astype(np.float32)
+    op = BornReflOp(p, wav, s)
+    g = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    op.forward(m, g)
+    o = oracle.bornrefl_forward(p, wav, s, m, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(g, o) < TOL_OP, ("refl fwd", rel_l2(g, o))
+    a = np.zeros((nf, p.nz, p.nx), np.complex64)
+    op.adjoint(a, d)
+    q = oracle.bornrefl_adjoint(p, wav, s, d, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(a, q) < TOL_OP, ("refl adj", rel_l2(a, q))
+    refl = (rand_c(rng, (nf, p.nz, p.nx)) * 0.2).astype(np.complex64)
+    dm = (rand_c(rng, (p.nz, p.nx)) * 1e-8).astype(np.complex64)
+    op = BornTomoOp(p, wav, s)
+    op.set_refl(refl)
+    g = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    op.forward(dm, g)
+    o = oracle.borntomo_forward(p, wav, s, refl, dm, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(g, o) < TOL_OP, ("tomo fwd", rel_l2(g, o))
+    a = np.zeros((p.nz, p.nx), np.complex64)
+    op.adjoint(a, d)
+    q = oracle.borntomo_adjoint(p, wav, s, refl, d, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(a, q) < TOL_OP, ("tomo adj", rel_l2(a, q))

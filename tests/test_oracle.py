@@ -177,3 +177,35 @@ def test_exact_kz_phase_law(oracle, adj):
     p.phase_law = 0
     ispc = oracle.onestep(p, s, 2, f, adj, x, prec=64)
     assert rel_l2(ispc, want) > 1e-3  # the two laws differ (eps damping)
+
+
+@pytest.mark.parametrize("mode", ["compat", "exact"])
+def test_bornrefl_dot(oracle, mode):
+    """BornRefl (ext_born_refl.cpp:8-105): Up and Up^H are exact transposes,
+    so forward and adjoint pass the dot test in either adjoint mode."""
+    p, par, wav, s, rho = small_case(nz=12, ns=2, adjoint_mode=mode)
+    nf = oracle.count_freqs(p)[0]
+    rng = np.random.default_rng(31)
+    m = rand_c(rng, (nf, p.nz, p.nx))
+    d = (rng.random((p.ns, p.nr, p.nt)) - .5).astype(np.float32)
+    Fm = oracle.bornrefl_forward(p, wav, s, m, kind=WEM_DATA_TIME, prec=64)
+    Fd = oracle.bornrefl_adjoint(p, wav, s, d, kind=WEM_DATA_TIME, prec=64)
+    lhs = float(np.sum(Fm.astype(np.float64) * d))
+    rhs = float(np.sum((np.conj(Fd.astype(np.complex128)) * m).real))
+    assert abs(lhs / rhs - 1) < 1e-5, (lhs, rhs)
+
+
+def test_borntomo_dot_exact(oracle):
+    """BornTomo (ext_born_tomo.cpp:9-119) with the exact scatter adjoint is
+    the transpose of its forward."""
+    p, par, wav, s, rho = small_case(nz=12, ns=2, adjoint_mode="exact")
+    nf = oracle.count_freqs(p)[0]
+    rng = np.random.default_rng(32)
+    refl = (rand_c(rng, (nf, p.nz, p.nx)) * 0.2).astype(np.complex64)
+    dm = (rand_c(rng, (p.nz, p.nx)) * 1e-8).astype(np.complex64)
+    d = (rng.random((p.ns, p.nr, p.nt)) - .5).astype(np.float32)
+    Fm = oracle.borntomo_forward(p, wav, s, refl, dm, kind=WEM_DATA_TIME, prec=64)
+    Fd = oracle.borntomo_adjoint(p, wav, s, refl, d, kind=WEM_DATA_TIME, prec=64)
+    lhs = float(np.sum(Fm.astype(np.float64) * d))
+    rhs = float(np.sum((np.conj(Fd.astype(np.complex128)) * dm).real))
+    assert abs(lhs / rhs - 1) < 1e-5, (lhs, rhs)

@@ -186,17 +186,26 @@ std::vector<float> host_floats(const void* p, size_t nfloat) {
 
 class Engine {
  public:
-  Engine(const wem_params& p, const float* wavelet, bool ext, bool born) : p_(p), ext_(ext), born_(born) {
+  // kind: 0 BornFull / WEM, 1 BornRefl, 2 BornTomo (propagator/src/ext_born_refl.cpp,
+  // ext_born_tomo.cpp); the variants run on the Born passes with the
+  // switches of DevCtx
+  Engine(const wem_params& p, const float* wavelet, bool ext, bool born, int kind = 0)
+      : p_(p), ext_(ext), born_(born), kind_(kind) {
     require(wavelet != nullptr, "wavelet is NULL");
     geo_ = make_geometry(p, wavelet);
     F_ = geo_.nfreq();
     M_ = ext ? F_ : 1;
+    M_img_ = (ext || kind == 1) ? F_ : 1;
     int dev = 0;
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     build_static();
+    ctx_.ext_model = kind == 1 ? 1 : 0;
+    ctx_.no_fwd_record = kind == 2 ? 1 : 0;
+    ctx_.last_rule = kind == 2 ? 1 : 0;
   }
 
   int nfreq() const { return F_; }
+  const wem_params& params() const { return p_; }
 
   void set_background(const void* s2, const void* rho) {
     require(s2 && rho, "background model is NULL");
@@ -259,21 +268,101 @@ class Engine {
     const size_t plane = (size_t)p_.nz * geo_.nxg;
     float2* dm0 = dm0_.as<float2>((size_t)M_ * plane);
     float2* dm1 = dm1_.as<float2>((size_t)M_ * plane);
-    pad_perturbation(ds2, dm0);
-    pad_perturbation(drho, dm1);
+    pad_perturbation(ds2, dm0, M_);
+    pad_perturbation(drho, dm1, M_);
     float2* drm = drm_.as<float2>((size_t)M_ * plane);
     launch_drefl_fwd(ctx_, M_, a0_, b0_, a1_, b1_, dm0, dm1, drm, 0);
-    float2* bins = zero_bins();
+    zero_bins();
+    born_fwd_pass(dm0, drm);
+    emit(data, kind, add);
+  }
+
+  // Born forward of the slowness perturbation rows dm0 and the reflectivity
+  // perturbation rows drm into the internal bins
+  void born_fwd_pass(const float2* dm0, const float2* drm) {
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
     const bool wp = warp_path();
     int G = wp ? warp_G(1) : pick_G([&](int g) { return smem_born_fwd(ctx_, g); });
     for_chunks(G, 2 * plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = store1_.as<float2>((size_t)rows * plane);
       float2* B = store2_.as<float2>((size_t)rows * plane);
-      if (wp) timed("k_born_fwd", [&] { launch_pass_warp(1, ctx_, gd, ng, dm0, drm, A, B, nullptr, bins, nullptr, nullptr, 0, 0); });
-      else timed("k_born_fwd", [&] { launch_born_fwd(ctx_, gd, ng, G, dm0, drm, A, B, bins, 0); });
+      if (wp) timed("k_born_fwd", [&] { launch_pass_warp(1, ctx_, gd, ng, dm0, drm, A, B, nullptr, bins_, nullptr, nullptr, 0, 0); });
+      else timed("k_born_fwd", [&] { launch_born_fwd(ctx_, gd, ng, G, dm0, drm, A, B, bins_, 0); });
       cuda_check(cudaGetLastError(), "k_born_fwd launch");
     }, wp);
+  }
+
+  // ------------------------------------------------ BornRefl, BornTomo
+  // BornRefl (ext_born_refl.cpp:8-105): the model is a reflectivity per
+  // frequency [F][nz][nx]; forward records Up(bg m_f), adjoint gives
+  // sum_s conj(bg) Up^H(rec) per frequency.  On the Born passes: no slowness
+  // perturbation, the model in place of dR(dm), the reflectivity image out.
+  void refl_forward(const void* model, void* data, int kind, int add) {
+    require(have_bg_, "background not set");
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
+    float2* drm = drm_.as<float2>((size_t)F_ * plane);
+    pad_perturbation(model, drm, F_);
+    float2* dm0 = dm0_.as<float2>((size_t)F_ * plane);
+    cuda_check(cudaMemsetAsync(dm0, 0, (size_t)F_ * plane * 8, 0), "memset");
+    zero_bins();
+    born_fwd_pass(dm0, drm);
     emit(data, kind, add);
+  }
+  void refl_adjoint(void* model, const void* data, int kind, int add) {
+    require(have_bg_, "background not set");
+    require(model && data, "NULL argument");
+    absorb(data, kind);
+    adj_pass();
+    image_out(ir_, model, add);
+  }
+
+  // BornTomo (ext_born_tomo.cpp:9-119): the model is a slowness perturbation
+  // [nz][nx]; the down- and up-scattering terms of BornFull with the given
+  // reflectivity per frequency in place of R, without the forward-scattering
+  // record and the reflectivity perturbation.
+  void tomo_set_refl(const void* refl) {
+    require(refl != nullptr, "reflectivity is NULL");
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
+    Staged s;
+    s.in(refl, (size_t)F_ * p_.nz * p_.nx * 8);
+    float2* rcf = rcf_.as<float2>((size_t)F_ * plane);
+    launch_pad_edge((const float2*)s.dev, rcf, F_, p_.nz, p_.nx, p_.pad, 0);
+    cuda_check(cudaGetLastError(), "pad launch");
+    cuda_check(cudaStreamSynchronize(0), "set_refl");
+    ctx_.rcf = rcf;
+  }
+  void tomo_forward(const void* dm, void* data, int kind, int add) {
+    require(have_bg_, "background not set");
+    require(ctx_.rcf != nullptr, "reflectivity not set");
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
+    float2* dm0 = dm0_.as<float2>(plane);
+    pad_perturbation(dm, dm0, 1);
+    float2* drm = drm_.as<float2>(plane);
+    cuda_check(cudaMemsetAsync(drm, 0, plane * 8, 0), "memset");
+    zero_bins();
+    born_fwd_pass(dm0, drm);
+    emit(data, kind, add);
+  }
+  void tomo_adjoint(void* dm, const void* data, int kind, int add) {
+    require(have_bg_, "background not set");
+    require(ctx_.rcf != nullptr, "reflectivity not set");
+    require(dm && data, "NULL argument");
+    absorb(data, kind);
+    adj_pass();
+    image_out(is_, dm, add);
+  }
+
+  // an image [M_img][nz][nxg] unpadded into the caller's [M_img][nz][nx]
+  void image_out(Buf& img, void* out, int add) {
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
+    const size_t nm = (size_t)M_img_ * p_.nz * p_.nx;
+    float2* I = img.as<float2>((size_t)M_img_ * plane);
+    Staged o;
+    o.out(out, nm * 8, add != 0);
+    launch_copy_rows(I + p_.pad, geo_.nxg, (float2*)o.dev, p_.nx, M_img_ * p_.nz, p_.nx, add, 0);
+    cuda_check(cudaGetLastError(), "image launch");
+    cuda_check(cudaStreamSynchronize(0), "image");
+    o.finish(out);
   }
 
   void born_adjoint(void* ds2, void* drho, const void* data, int kind, int add) {
@@ -287,10 +376,10 @@ class Engine {
   // Born adjoint of the internal bins into the images IR, IS
   void adj_pass() {
     const size_t plane = (size_t)p_.nz * geo_.nxg;
-    float2* IR = ir_.as<float2>((size_t)M_ * plane);
-    float2* IS = is_.as<float2>((size_t)M_ * plane);
-    cuda_check(cudaMemsetAsync(IR, 0, (size_t)M_ * plane * 8, 0), "memset");
-    cuda_check(cudaMemsetAsync(IS, 0, (size_t)M_ * plane * 8, 0), "memset");
+    float2* IR = ir_.as<float2>((size_t)M_img_ * plane);
+    float2* IS = is_.as<float2>((size_t)M_img_ * plane);
+    cuda_check(cudaMemsetAsync(IR, 0, (size_t)M_img_ * plane * 8, 0), "memset");
+    cuda_check(cudaMemsetAsync(IS, 0, (size_t)M_img_ * plane * 8, 0), "memset");
     const bool wp = warp_path();
     int G = wp ? warp_G(2) : pick_G([&](int g) { return smem_born_adj(ctx_, g); });
     const int compat = p_.adjoint_mode == WEM_ADJ_COMPAT ? 1 : 0;
@@ -306,20 +395,20 @@ class Engine {
       if (wp) timed("k_born_adj", [&] { launch_pass_warp(2, ctx_, gd, ng, nullptr, nullptr, BG, T, SG, bins_, pr, ps, compat, 0); });
       else timed("k_born_adj", [&] { launch_born_adj(ctx_, gd, ng, G, BG, T, bins_, pr, ps, compat, 0); });
       cuda_check(cudaGetLastError(), "k_born_adj launch");
-      // chunk-local group ranges of each model slice
-      std::vector<int> beg(M_ + 1, 0);
-      if (M_ == 1) {
+      // chunk-local group ranges of each image slice
+      std::vector<int> beg(M_img_ + 1, 0);
+      if (M_img_ == 1) {
         beg[1] = ng;
       } else {
         int g = 0;
-        for (int m = 0; m <= M_; ++m) {
+        for (int m = 0; m <= M_img_; ++m) {
           while (g < ng && chunk_[g].f < m) ++g;
           beg[m] = g;
         }
       }
       int* dbeg = upload(begbuf_, beg);
-      launch_reduce_images(pr, dbeg, M_, plane, IR, 0);
-      launch_reduce_images(ps, dbeg, M_, plane, IS, 0);
+      launch_reduce_images(pr, dbeg, M_img_, plane, IR, 0);
+      launch_reduce_images(ps, dbeg, M_img_, plane, IS, 0);
       cuda_check(cudaGetLastError(), "reduce launch");
     }, wp);
   }
@@ -343,6 +432,8 @@ class Engine {
  private:
   wem_params p_;
   bool ext_, born_;
+  int kind_ = 0;
+  int M_img_ = 1;  // image slices: per frequency for the extended operators and BornRefl
   bool have_bg_ = false;
   Geometry geo_;
   int F_ = 0, M_ = 1;
@@ -354,7 +445,7 @@ class Engine {
   float2 *a0_ = nullptr, *b0_ = nullptr, *a1_ = nullptr, *b1_ = nullptr;
   // workspaces
   std::vector<Group> chunk_;  // host copy of the groups of the current launch
-  Buf binsbuf_, groups_, store1_, store2_, store3_, dsyn_, lossbuf_, part1_, part2_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
+  Buf rcf_, binsbuf_, groups_, store1_, store2_, store3_, dsyn_, lossbuf_, part1_, part2_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
   float2* bins_ = nullptr;
 
   void build_static() {
@@ -597,11 +688,11 @@ class Engine {
     return bins_;
   }
 
-  void pad_perturbation(const void* m, float2* out) {
+  void pad_perturbation(const void* m, float2* out, int slices) {
     require(m != nullptr, "perturbation is NULL");
     Staged s;
-    s.in(m, (size_t)M_ * p_.nz * p_.nx * 8);
-    launch_pad_model((const float2*)s.dev, out, M_, p_.nz, p_.nx, p_.pad, 0);
+    s.in(m, (size_t)slices * p_.nz * p_.nx * 8);
+    launch_pad_model((const float2*)s.dev, out, slices, p_.nz, p_.nx, p_.pad, 0);
     cuda_check(cudaGetLastError(), "pad launch");
     cuda_check(cudaStreamSynchronize(0), "pad");
   }
@@ -803,6 +894,8 @@ struct born_handle { std::unique_ptr<Engine> e; };
 struct extwem_handle { std::unique_ptr<Engine> e; };
 struct extborn_handle { std::unique_ptr<Engine> e; };
 struct fwi_handle { std::unique_ptr<Engine> e; };
+struct bornrefl_handle { std::unique_ptr<Engine> e; };
+struct borntomo_handle { std::unique_ptr<Engine> e; };
 struct wemop_handle { std::unique_ptr<RowOps> r; };
 
 extern "C" {
@@ -910,6 +1003,57 @@ void extwem_destroy(extwem_handle* h) { delete h; }
 int extwem_forward(extwem_handle* h, const void* s2, const void* rho, void* data, int kind, int add) {
   return guard([&] { require(h != nullptr, "NULL handle"); h->e->wem_forward(s2, rho, data, kind, add); });
 }
+// background of the variants: slowness^2 with unit density (the reference's
+// BornRefl / BornTomo take no density; it only enters the tables they replace)
+static void set_bg_unit_rho(Engine& e, const wem_params& p, const void* s2) {
+  std::vector<float> ones((size_t)2 * p.nz * p.nx, 0.f);
+  for (size_t i = 0; i < ones.size(); i += 2) ones[i] = 1.f;
+  e.set_background(s2, ones.data());
+}
+
+int bornrefl_create(const wem_params* p, const float* wavelet, const void* s2, bornrefl_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<bornrefl_handle>();
+    h->e = std::make_unique<Engine>(*p, wavelet, false, true, 1);
+    set_bg_unit_rho(*h->e, *p, s2);
+    *out = h.release();
+  });
+}
+void bornrefl_destroy(bornrefl_handle* h) { delete h; }
+int bornrefl_set_background(bornrefl_handle* h, const void* s2) {
+  return guard([&] { require(h != nullptr, "NULL handle"); set_bg_unit_rho(*h->e, h->e->params(), s2); });
+}
+int bornrefl_forward(bornrefl_handle* h, const void* model, void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->refl_forward(model, data, kind, add); });
+}
+int bornrefl_adjoint(bornrefl_handle* h, void* model, const void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->refl_adjoint(model, data, kind, add); });
+}
+
+int borntomo_create(const wem_params* p, const float* wavelet, const void* s2, borntomo_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<borntomo_handle>();
+    h->e = std::make_unique<Engine>(*p, wavelet, false, true, 2);
+    set_bg_unit_rho(*h->e, *p, s2);
+    *out = h.release();
+  });
+}
+void borntomo_destroy(borntomo_handle* h) { delete h; }
+int borntomo_set_background(borntomo_handle* h, const void* s2) {
+  return guard([&] { require(h != nullptr, "NULL handle"); set_bg_unit_rho(*h->e, h->e->params(), s2); });
+}
+int borntomo_set_refl(borntomo_handle* h, const void* refl) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->tomo_set_refl(refl); });
+}
+int borntomo_forward(borntomo_handle* h, const void* dm, void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->tomo_forward(dm, data, kind, add); });
+}
+int borntomo_adjoint(borntomo_handle* h, void* dm, const void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->tomo_adjoint(dm, data, kind, add); });
+}
+
 int fwi_create(const wem_params* p, const float* wavelet, fwi_handle** out) {
   return guard([&] {
     require(p && out, "NULL argument");

@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(kThreads) k_wem(DevCtx c, const Group* groups,
   __syncthreads();
   for (int z = 0; z < nz; ++z) {
     record(c, W, nxg, nrow, s0, bin, z, bins);
-    const float2* rc = c.rc + ((size_t)m * nz + z) * nxg;
+    const float2* rc = rc_row(c, f, z);
     for (int i = threadIdx.x; i < nrow * nxg; i += blockDim.x) {
       int r = i / nxg, x = i - r * nxg;
       A[r * plane + (size_t)z * nxg + x] = c_mul(rc[x], W[i]);
@@ -350,10 +350,10 @@ __global__ void __launch_bounds__(kThreads) k_born_fwd(DevCtx c, const Group* gr
   for (int z = 0; z < nz; ++z) {
     float2* bg = P;
     float2* sd = P + half;
-    record(c, sd, nxg, nrow, s0, bin, z, bins);
-    const float2* rc = c.rc + ((size_t)m * nz + z) * nxg;
-    const float2* dr = drm + ((size_t)m * nz + z) * nxg;
-    const float2* dmz = dm + ((size_t)m * nz + z) * nxg;
+    if (!c.no_fwd_record) record(c, sd, nxg, nrow, s0, bin, z, bins);
+    const float2* rc = rc_row(c, f, z);
+    const float2* dr = drm + pert_off(c, f, z);
+    const float2* dmz = dm + pert_off(c, f, z);
     for (int i = threadIdx.x; i < nrow * nxg; i += blockDim.x) {
       int r = i / nxg, x = i - r * nxg;
       size_t o = r * plane + (size_t)z * nxg + x;
@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(kThreads) k_born_adj(DevCtx c, const Group* gr
   float2* Q2 = S3;
   float2* T1 = S4;
   auto source_S = [&](int z) {  // WD = conj(R[z]) (T[z] + rec[z]) + rec[z] + WD_in (in Q1)
-    const float2* rc = c.rc + ((size_t)m * nz + z) * nxg;
+    const float2* rc = rc_row(c, f, z);
     for (int i = threadIdx.x; i < nrow * nxg; i += blockDim.x) {
       int r = i / nxg, x = i - r * nxg;
       T1[i] = ST[r * plane + (size_t)z * nxg + x];
@@ -495,11 +495,11 @@ __global__ void __launch_bounds__(kThreads) k_born_adj(DevCtx c, const Group* gr
       WD[i] = c_add(Q1[i], c_mulc(T1[i], rc[x]));
     }
     __syncthreads();
-    inject_rec(c, WD, nxg, nrow, s0, bin, z, bins);
+    if (!c.no_fwd_record) inject_rec(c, WD, nxg, nrow, s0, bin, z, bins);  // adjoint of the forward-scattering record
     __syncthreads();
   };
   {
-    const float2* rc = c.rc + ((size_t)m * nz + nz - 1) * nxg;
+    const float2* rc = rc_row(c, f, nz - 1);
     for (int i = threadIdx.x; i < nrow * nxg; i += blockDim.x) {
       int r = i / nxg, x = i - r * nxg;
       BU[i] = c_mul(rc[x], SBG[r * plane + (size_t)(nz - 1) * nxg + x]);
@@ -517,8 +517,7 @@ __global__ void __launch_bounds__(kThreads) k_born_adj(DevCtx c, const Group* gr
       for (int x = threadIdx.x; x < nxg; x += blockDim.x) {
         float2 a = ACC[x];
         for (int r = 0; r < nrow; ++r) {
-          bool keep = !(compat && z == nz - 1) ||
-                      (c.ext ? (s0 + r == c.ns - 1) : (f == c.nfreq - 1));
+          bool keep = z != nz - 1 || keep_last_row(c, compat, f, s0 + r);
           if (keep) a = c_add(a, c_mulc(T1[r * nxg + x], BU[r * nxg + x]));
         }
         ACC[x] = a;
@@ -540,7 +539,7 @@ __global__ void __launch_bounds__(kThreads) k_born_adj(DevCtx c, const Group* gr
     source_S(z - 1);  // WD = q + S[z-1]
     // bu[z-1] = P_z bu[z] + R[z-1] bg[z-1]
     step_fwd(c, tw, f, z, BU, nxg, Q2, nxg, nrow, X, Y, Z, false);
-    const float2* rc = c.rc + ((size_t)m * nz + z - 1) * nxg;
+    const float2* rc = rc_row(c, f, z - 1);
     for (int i = threadIdx.x; i < nrow * nxg; i += blockDim.x) {
       int r = i / nxg, x = i - r * nxg;
       BU[i] = c_add(Q2[i], c_mul(rc[x], SBG[r * plane + (size_t)(z - 1) * nxg + x]));

@@ -19,6 +19,12 @@ struct DevCtx {
   FftPlan plan;                 // length N = nxg + 2 tap
   int N, nxg, tap, pad, nz, nref, prop, ntaylor, nfreq, ext, ns, nr, ngs, ngr, nbin;
   int phase_law;                // WEM_PHASE_ISPC or WEM_PHASE_EXACT_KZ
+  // Born variants (BornRefl, BornTomo of propagator/src/ext_born_refl.cpp,
+  // ext_born_tomo.cpp) on the Born passes:
+  int ext_model;                // perturbation rows and images per frequency, tables shared
+  const float2* rcf;            // [F][nz][nxg] per-frequency reflectivity replacing rc, or null
+  int no_fwd_record;            // the forward-scattered (down) field is not recorded
+  int last_rule;                // compat last depth row: 0 per shot (BornFull), 1 only the last (f, s)
   float dz, invN;
   const float2* tw;             // [N] exp(-2 pi i t/N)
   const float2* ph;             // [F][nz][nref][N] phase-shift factors (phase_shift.ispc)
@@ -54,6 +60,24 @@ int max_smem_per_block();
 // counts the library's kernel launches (wem_launch_count)
 void note_launch();
 long long launch_count();
+
+#ifdef __CUDACC__
+// reflection row of depth z for frequency f
+__device__ __forceinline__ const float2* rc_row(const DevCtx& c, int f, int z) {
+  return c.rcf ? c.rcf + ((size_t)f * c.nz + z) * c.nxg : c.rc + ((size_t)(c.ext ? f : 0) * c.nz + z) * c.nxg;
+}
+// offset of the perturbation row (dm, dR(dm)) of depth z for frequency f
+__device__ __forceinline__ size_t pert_off(const DevCtx& c, int f, int z) {
+  return ((size_t)((c.ext || c.ext_model) ? f : 0) * c.nz + z) * c.nxg;
+}
+// the as-coded Born adjoint keeps, in the last depth row, the LinUp^H term of
+// one row only (LinOneWay.cpp:64-65 zeroes that row on every LinDown^H call)
+__device__ __forceinline__ bool keep_last_row(const DevCtx& c, int compat, int f, int s) {
+  if (!compat) return true;
+  if (c.last_rule == 1) return f == c.nfreq - 1 && s == c.ns - 1;
+  return c.ext ? (s == c.ns - 1) : (f == c.nfreq - 1);
+}
+#endif
 
 // ---- table builders
 void launch_phase_tables(const DevCtx& c, const float2* sref /*[M][nz][nref]*/, float eps, float2* ph,

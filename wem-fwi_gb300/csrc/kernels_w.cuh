@@ -86,11 +86,11 @@ __device__ __forceinline__ Tabs global_tabs(const DevCtx& c, const Src& s, int f
   t.ph = c.ph + ((size_t)f * c.nz + z) * c.nref * c.N;
   t.fac = c.fac ? c.fac + ((size_t)f * c.nz + z) * c.nxg : nullptr;
   t.ref = c.ref + zo;
-  t.rc = c.rc + zo;
+  t.rc = rc_row(c, f, z);
   t.c0 = c.sc ? c.sc + (size_t)m * (c.ntaylor + 1) * plane + (size_t)z * c.nxg : nullptr;
   t.c1 = (c.sc && c.ntaylor >= 1) ? t.c0 + plane : nullptr;
-  t.dm = s.dm ? s.dm + zo : nullptr;
-  t.dr = s.drm ? s.drm + zo : nullptr;
+  t.dm = s.dm ? s.dm + pert_off(c, f, z) : nullptr;
+  t.dr = s.drm ? s.drm + pert_off(c, f, z) : nullptr;
   return t;
 }
 
@@ -689,7 +689,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, SlotLayout L
     __syncthreads();
     if (!act) continue;
     const Tabs T = ring.tabs(z);
-    w_record<E>(w, sd, s, bin, z, bins);
+    if (!c.no_fwd_record) w_record<E>(w, sd, s, bin, z, bins);
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       bool in;
@@ -846,7 +846,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
   __syncthreads();  // the down sweep's images are out of the slots; the ring is idle
   // ---------------- up sweep: bu (Up of R bg) and wd (Down^H of rec + conj(R) wu)
   float2 bu[E], wd[E];
-  const bool keep_last = !compat || (c.ext ? (s == c.ns - 1) : (f == c.nfreq - 1));
+  const bool keep_last = keep_last_row(c, compat, f, s);
 #pragma unroll
   for (int j = 0; j < E; ++j) {
     bool in;
@@ -881,7 +881,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
           bu[j] = in ? c_mul(r, bu[j]) : zero;
           wd[j] = in ? c_mulc(X[j], r) : zero;
         }
-        w_inject_rec<E>(w, wd, s, bin, nz - 1, bins);
+        if (!c.no_fwd_record) w_inject_rec<E>(w, wd, s, bin, nz - 1, bins);
       }
 #pragma unroll 1
       for (int k = 0; k < 4; ++k) {
@@ -956,7 +956,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
             const float2 r = T.rc[xclamp(w, j, in)];
             if (in) wd[j] = c_add(wd[j], c_mulc(X[j], r));
           }
-          w_inject_rec<E>(w, wd, s, bin, z - 1, bins);
+          if (!c.no_fwd_record) w_inject_rec<E>(w, wd, s, bin, z - 1, bins);
         } else if (k == 2) {
           // bu[z-1] = P_z bu + R[z-1] bg[z-1]
           if constexpr (MR) {
@@ -1116,7 +1116,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
   // conj(bu[z-1]) Sc^H_{z-1} T[z-1] (op 1); receiver side: q = P^H_{z-1} wd
   // (op 0), LinDown^H conj(bg[z-1]) Sc^H_{z-1} q (op 1), then
   // wd[z-1] = q + rec + conj(R[z-1]) (T[z-1] + rec)
-  const bool keep_last = !compat || (c.ext ? (s == c.ns - 1) : (f == c.nfreq - 1));
+  const bool keep_last = keep_last_row(c, compat, f, s);
   __syncthreads();  // the down sweep's buffers are summed; the ring is idle
   ring.issue(nz - 1);
   cp_commit();
@@ -1157,7 +1157,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
             const float2 r = Tp.rc[xclamp(w, j, in)];
             S[j] = in ? c_mulc(X[j], r) : zero;
           }
-          w_inject_rec<E>(w, S, s, bin, nz - 1, bins);
+          if (!c.no_fwd_record) w_inject_rec<E>(w, S, s, bin, nz - 1, bins);
         }
       } else if (lane == 0 && !recv && z >= 2) {
         l2_prefetch(SBG + (size_t)(z - 2) * nxg, nxg * 8);
@@ -1257,7 +1257,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
               const float2 r = Tp.rc[xclamp(w, j, in)];
               if (in) S[j] = c_add(S[j], c_mulc(X[j], r));
             }
-            w_inject_rec<E>(w, S, s, bin, z - 1, bins);
+            if (!c.no_fwd_record) w_inject_rec<E>(w, S, s, bin, z - 1, bins);
           }
         }
       }

@@ -15,10 +15,10 @@ from .vector import Axis, Hypercube, SuperVector, Vector, getSepVector, superVec
 
 def __getattr__(name):
     # operator classes load the CUDA library on first use
-    if name in ("WEM", "Born", "extWEM", "extBorn", "Propagator"):
+    if name in ("WEM", "Born", "extWEM", "extBorn", "BornRefl", "BornTomo", "Propagator"):
         from . import ops
         return getattr(ops, name)
-    if name in ("WemOp", "BornOp", "ExtWemOp", "ExtBornOp", "RowOps", "FwiOp"):
+    if name in ("WemOp", "BornOp", "ExtWemOp", "ExtBornOp", "BornReflOp", "BornTomoOp", "RowOps", "FwiOp"):
         from . import core
         return getattr(core, name)
     raise AttributeError(name)

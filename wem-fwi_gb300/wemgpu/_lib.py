@@ -49,6 +49,17 @@ _SIGS = {
     "extborn_set_background": (_i, [_h, _v, _v]),
     "extborn_forward": (_i, [_h, _v, _v, _v, _i, _i]),
     "extborn_adjoint": (_i, [_h, _v, _v, _v, _i, _i]),
+    "bornrefl_create": (_i, [_pp, _v, _v, ctypes.POINTER(_h)]),
+    "bornrefl_destroy": (None, [_h]),
+    "bornrefl_set_background": (_i, [_h, _v]),
+    "bornrefl_forward": (_i, [_h, _v, _v, _i, _i]),
+    "bornrefl_adjoint": (_i, [_h, _v, _v, _i, _i]),
+    "borntomo_create": (_i, [_pp, _v, _v, ctypes.POINTER(_h)]),
+    "borntomo_destroy": (None, [_h]),
+    "borntomo_set_background": (_i, [_h, _v]),
+    "borntomo_set_refl": (_i, [_h, _v]),
+    "borntomo_forward": (_i, [_h, _v, _v, _i, _i]),
+    "borntomo_adjoint": (_i, [_h, _v, _v, _i, _i]),
     "fwi_create": (_i, [_pp, _v, ctypes.POINTER(_h)]),
     "fwi_destroy": (None, [_h]),
     "fwi_gradient": (_i, [_h, _v, _v, _v, _v, _v, ctypes.POINTER(ctypes.c_double)]),

@@ -162,6 +162,72 @@ class FwiOp(_Base):
         return loss.value
 
 
+class BornReflOp(_Base):
+    """Frequency-extended reflectivity Born (BornRefl,
+    propagator/src/ext_born_refl.cpp:8-105): model [nfreq][nz][nx] is a
+    reflectivity per frequency; forward records Up(bg m_f), adjoint gives the
+    per-frequency image sum_s conj(bg) Up^H(data)."""
+
+    _destroy = "bornrefl_destroy"
+
+    def __init__(self, p: WemParams, wavelet, bg_s2):
+        super().__init__(p, wavelet)
+        _lib.call("bornrefl_create", ctypes.byref(self.p), self.wavelet.ctypes.data_as(ctypes.c_void_p),
+                  ptr(bg_s2, np.complex64, (self.p.nz, self.p.nx), "slowness"), ctypes.byref(self.h))
+
+    @property
+    def model_shape(self):
+        return (self.nfreq(), self.p.nz, self.p.nx)
+
+    def set_background(self, s2):
+        _lib.call("bornrefl_set_background", self.h, ptr(s2, np.complex64, (self.p.nz, self.p.nx), "slowness"))
+
+    def forward(self, model, data, add=False):
+        d, kind = self._data_ptr(data, True)
+        _lib.call("bornrefl_forward", self.h, ptr(model, np.complex64, self.model_shape, "model"), d, kind,
+                  int(bool(add)))
+        return data
+
+    def adjoint(self, model, data, add=False):
+        d, kind = self._data_ptr(data, False)
+        _lib.call("bornrefl_adjoint", self.h, ptr(model, np.complex64, self.model_shape, "model", True), d, kind,
+                  int(bool(add)))
+        return model
+
+
+class BornTomoOp(_Base):
+    """Frequency-extended tomographic Born (BornTomo,
+    propagator/src/ext_born_tomo.cpp:9-119): model [nz][nx] is a slowness^2
+    perturbation; the down- and up-scattering terms with the reflectivity per
+    frequency of ``set_refl`` ([nfreq][nz][nx]) in place of R."""
+
+    _destroy = "borntomo_destroy"
+
+    def __init__(self, p: WemParams, wavelet, bg_s2):
+        super().__init__(p, wavelet)
+        _lib.call("borntomo_create", ctypes.byref(self.p), self.wavelet.ctypes.data_as(ctypes.c_void_p),
+                  ptr(bg_s2, np.complex64, self.model_shape, "slowness"), ctypes.byref(self.h))
+
+    def set_background(self, s2):
+        _lib.call("borntomo_set_background", self.h, ptr(s2, np.complex64, self.model_shape, "slowness"))
+
+    def set_refl(self, refl):
+        _lib.call("borntomo_set_refl", self.h,
+                  ptr(refl, np.complex64, (self.nfreq(), self.p.nz, self.p.nx), "reflectivity"))
+
+    def forward(self, model, data, add=False):
+        d, kind = self._data_ptr(data, True)
+        _lib.call("borntomo_forward", self.h, ptr(model, np.complex64, self.model_shape, "model"), d, kind,
+                  int(bool(add)))
+        return data
+
+    def adjoint(self, model, data, add=False):
+        d, kind = self._data_ptr(data, False)
+        _lib.call("borntomo_adjoint", self.h, ptr(model, np.complex64, self.model_shape, "model", True), d, kind,
+                  int(bool(add)))
+        return model
+
+
 class ExtWemOp(WemOp):
     """Frequency-extended modelling (extWEM, propagator/src/extWEM.cpp:9-70)."""
 

@@ -191,3 +191,48 @@ class extBorn(Propagator):
     def adjoint(self, add, model, data):
         m = _vecs(model)
         self.cppMode.adjoint(m[0].getNdArray(), m[1].getNdArray(), data.getNdArray(), add)
+
+
+class BornRefl(Propagator):
+    """Frequency-extended reflectivity Born (WEM.py:85-115; BornRefl,
+    ext_born_refl.cpp:8-105).  model: reflectivity per frequency (a vector
+    of shape [nfreq][nz][nx]); slowness: the background slowness^2."""
+
+    def __init__(self, model, slowness, data, wave, par):
+        self.wave, self.par, self.domain, self.range = wave, par, model, data
+        self.params = _grid_params(par, slowness.getHyper(), wave, data)
+        self.cppMode = core.BornReflOp(self.params, wave.getNdArray(), slowness.getNdArray())
+
+    def set_background(self, slow):
+        self.cppMode.set_background(slow.getNdArray())
+
+    def forward(self, add, model, data):
+        self.cppMode.forward(model.getNdArray(), data.getNdArray(), add)
+
+    def adjoint(self, add, model, data):
+        self.cppMode.adjoint(model.getNdArray(), data.getNdArray(), add)
+
+
+class BornTomo(Propagator):
+    """Frequency-extended tomographic Born (WEM.py:117-134; BornTomo,
+    ext_born_tomo.cpp:9-119).  As in pyWEM.BornTomo(wave, slow, par), the
+    constructor's model vector is the background slowness^2; forward and
+    adjoint take a slowness^2 perturbation; setBgRefl sets the reflectivity
+    per frequency ([nfreq][nz][nx])."""
+
+    def __init__(self, model, data, wave, par):
+        self.wave, self.par, self.domain, self.range = wave, par, model, data
+        self.params = _grid_params(par, model.getHyper(), wave, data)
+        self.cppMode = core.BornTomoOp(self.params, wave.getNdArray(), model.getNdArray())
+
+    def setBgRefl(self, refl):
+        self.cppMode.set_refl(refl.getNdArray())
+
+    def set_background(self, slow):
+        self.cppMode.set_background(slow.getNdArray())
+
+    def forward(self, add, model, data):
+        self.cppMode.forward(model.getNdArray(), data.getNdArray(), add)
+
+    def adjoint(self, add, model, data):
+        self.cppMode.adjoint(model.getNdArray(), data.getNdArray(), add)
