@@ -122,6 +122,15 @@ TRAFFIC_PER_ROW_DEPTH = {
 }
 
 
+def config_of(p, nf, world, small):
+    """The workload block of both arms' JSON lines."""
+    return {"workload": "c3 FWI gradient: WEM fwd + residual + Born adjoint (compat)",
+            "nx": p.nx, "nz": p.nz, "dx": p.dx, "shots": p.ns * world, "freqs": nf, "fft_n": p.nx + 2 * p.pad,
+            "prop": "ssf", "depth_steps_per_iter": row_steps(p, nf) * world,
+            "l2": "inputs larger than L2 (stored wavefields ~11 GB per pass)",
+            "small": bool(small)}
+
+
 def row_steps(p, nfreq):
     return (PASSES_WEM + PASSES_BORN_ADJ) * p.ns * nfreq * (p.nz - 1)
 
@@ -296,11 +305,7 @@ def run_gpu(args, rank, world):
         "metric": METRIC, "value": value, "unit": "depth-steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded c3 model, see wemgpu/synthetic.py)",
-        "config": {"workload": "c3 FWI gradient: WEM fwd + residual + Born adjoint (compat)",
-                   "nx": p.nx, "nz": p.nz, "dx": p.dx, "shots": p.ns * world, "freqs": nf, "fft_n": p.nx,
-                   "prop": "ssf", "depth_steps_per_iter": steps_per_iter,
-                   "l2": "inputs larger than L2 (stored wavefields ~11 GB per pass)",
-                   "small": bool(args.small)},
+        "config": config_of(p, nf, world, args.small),
         "s_per_iter": s_per_iter,
         "e2e": {"value": steps_per_iter / e2e_s, "unit": "depth-steps/s", "s_per_iter": e2e_s,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
@@ -362,10 +367,16 @@ def run_reference(args, rank, world):
         if i >= args.warmup:
             res.append(r["value"])
     v = float(np.median(res))
+    from oracle import oracle as O
+    from wemgpu import synthetic as S
+    p = S.params_of(cfg)
+    nf = O.count_freqs(p)[0]
+    per_iter = row_steps(p, nf) / v
     line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "depth-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded c3 model)",
-            "config": {"workload": "c3 FWI gradient: WEM fwd + residual + Born adjoint (compat)"},
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * 1e3, "s_per_iter": per_iter,
+            "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded c3 model, see wemgpu/synthetic.py)",
+            "config": config_of(p, nf, 1, args.small),
             "cpu_baseline": {"value": v, "unit": "depth-steps/s", "cores": r["cores"], "kind": "port",
                              "sample": r["sample"]},
             "e2e": {"value": v, "unit": "depth-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
