@@ -273,7 +273,7 @@ __global__ void __launch_bounds__(kThreads) k_wem(DevCtx c, const Group* groups,
   float2* W = sm.take((size_t)G * nxg);
   float2* V = sm.take((size_t)G * nxg);
   const Group gp = groups[blockIdx.x];
-  const int nrow = gp.n, f = gp.f, s0 = gp.s0, bin = c.bin[f], m = c.ext ? f : 0;
+  const int nrow = gp.n, f = gp.f, s0 = gp.s0, bin = c.bin[f];
   const size_t plane = (size_t)nz * nxg;
   float2* A = store + (size_t)gp.row0 * plane;
   load_tw(c, tw);
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(kThreads) k_born_fwd(DevCtx c, const Group* gr
   float2* T1 = sm.take((size_t)G * nxg);
   float2* T2 = sm.take((size_t)G * nxg);
   const Group gp = groups[blockIdx.x];
-  const int nrow = gp.n, f = gp.f, s0 = gp.s0, bin = c.bin[f], m = c.ext ? f : 0;
+  const int nrow = gp.n, f = gp.f, s0 = gp.s0, bin = c.bin[f];
   const size_t plane = (size_t)nz * nxg;
   const size_t half = (size_t)nrow * nxg;
   float2* A = storeA + (size_t)gp.row0 * plane;
@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(kThreads) k_born_fwd(DevCtx c, const Group* gr
     float2* su = P + half;
     record(c, su, nxg, nrow, s0, bin, z, bins);
     if (z == 0) break;
-    const float2* dmz = dm + ((size_t)m * nz + z) * nxg;
+    const float2* dmz = dm + pert_off(c, f, z);
     for (int i = threadIdx.x; i < nrow * nxg; i += blockDim.x) T1[i] = c_mul(bu[i], dmz[i % nxg]);
     __syncthreads();
     scatter_rows(c, tw, f, z, 0, T1, nxg, T2, nxg, nrow, X, Y, Z, false);
@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(kThreads) k_born_adj(DevCtx c, const Group* gr
   float2* S4 = sm.take((size_t)G * nxg);
   float2* ACC = sm.take(nxg);
   const Group gp = groups[blockIdx.x];
-  const int nrow = gp.n, f = gp.f, s0 = gp.s0, bin = c.bin[f], m = c.ext ? f : 0;
+  const int nrow = gp.n, f = gp.f, s0 = gp.s0, bin = c.bin[f];
   const size_t plane = (size_t)nz * nxg;
   float2* SBG = storeBG + (size_t)gp.row0 * plane;
   float2* ST = storeT + (size_t)gp.row0 * plane;
