@@ -989,6 +989,15 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
 // barrier the CTA sums the buffers of its rows in row order (deterministic).
 // Two barriers per depth: the ring's copies are issued at the top of a depth
 // and waited for at its end.
+// an int the compiler cannot see through: values derived from it after this
+// point are recomputed there instead of being kept live across the code
+// before it
+__device__ __forceinline__ int launder(int v) {
+  int r;
+  asm volatile("mov.b32 %0, %1;" : "=r"(r) : "r"(v));
+  return r;
+}
+
 template <int E, bool NT, int R>
 __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayout L, const Group* groups,
                                                               float2* storeBG, float2* storeT, float2* storeG,
@@ -1213,15 +1222,19 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
           }
           wfft<E, true>(X, w.sb, w.tw, lane);
         }
-        // post
+        // post: the depth's tables and rows again from a laundered depth
+        const int zl = launder(z);
+        const Tabs Tq = ring.stabs(zl - 1);
+        const float2* bgq = SBG + (size_t)(zl - 1) * nxg;
+        const float2* tq = ST + (size_t)(zl - 1) * nxg;
         if (step) {
           if (!recv) {
-            fwd_post<E, false>(w, T, 0, X, S);
+            fwd_post<E, false>(w, ring.stabs(zl), 0, X, S);
 #pragma unroll
             for (int j = 0; j < E; ++j) {
               bool in;
               const int x = xclamp(w, j, in);
-              const float2 r = Tp.rc[x], b = bgp[x];
+              const float2 r = Tq.rc[x], b = bgq[x];
               if (in) S[j] = c_add(S[j], c_mul(r, b));
             }
           } else if (!reuse) {
@@ -1233,7 +1246,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
             for (int j = 0; j < E; ++j) {
               bool in;
               const int x = xclamp(w, j, in);
-              const float2 k0 = T.c0[x], k1 = t1 ? T.c1[x] : zero, b = bgp[x];
+              const float2 k0 = Tq.c0[x], k1 = t1 ? Tq.c1[x] : zero, b = bgq[x];
               const float2 v = sc_val(iw, scmode, t1, k0, k1, S[j], X[j]);
               if (in) xb[x] = c_mulc(v, b);
             }
@@ -1242,19 +1255,19 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
             for (int j = 0; j < E; ++j) {
               bool in;
               const int x = xclamp(w, j, in);
-              const float2 k0 = T.c0[x], k1 = t1 ? T.c1[x] : zero, u = tp[x];
+              const float2 k0 = Tq.c0[x], k1 = t1 ? Tq.c1[x] : zero, u = tq[x];
               const float2 v = sc_val(iw, scmode, t1, k0, k1, u, X[j]);
               if (in) xb[x] = c_mulc(v, S[j]);
             }
           }
           wrote = true;
           if (recv && z >= 2) {
-            w_load<E>(w, tp, X);
+            w_load<E>(w, tq, X);
             w_inject_rec<E>(w, X, s, bin, z - 1, bins);
 #pragma unroll
             for (int j = 0; j < E; ++j) {
               bool in;
-              const float2 r = Tp.rc[xclamp(w, j, in)];
+              const float2 r = Tq.rc[xclamp(w, j, in)];
               if (in) S[j] = c_add(S[j], c_mulc(X[j], r));
             }
             if (!c.no_fwd_record) w_inject_rec<E>(w, S, s, bin, z - 1, bins);
