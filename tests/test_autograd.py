@@ -87,3 +87,23 @@ def test_backward_is_the_transpose_of_born(gpu_lib):
     rhs = float(np.sum((np.conj(a.grad.cpu().numpy().astype(np.complex128)) * ds).real)
                 + np.sum((np.conj(b.grad.cpu().numpy().astype(np.complex128)) * dr).real))
     assert abs(lhs / rhs - 1) < 1e-4, (lhs, rhs)
+
+
+def test_objective_pspi_shared_memory_path(gpu_lib):
+    """fwi_gradient off the warp kernels (N = 72, PSPI with two references)
+    equals the Born adjoint of its residual."""
+    import torch
+    from cases import small_case
+    from wemgpu.core import BornOp, FwiOp, WemOp
+    p, par, wav, s, rho = small_case(nz=12, ns=2, prop="pspi", nref=2)
+    d_obs = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    WemOp(p, wav).forward((s * 1.02).astype(np.complex64), rho, d_obs)
+    g0, g1 = np.zeros_like(s), np.zeros_like(s)
+    loss = FwiOp(p, wav).gradient(s, rho, d_obs, g0, g1)
+    d = np.zeros_like(d_obs)
+    WemOp(p, wav).forward(s, rho, d)
+    res = d - d_obs
+    assert loss == pytest.approx(0.5 * float(np.sum(res.astype(np.float64) ** 2)), rel=1e-4)
+    a0, a1 = np.zeros_like(s), np.zeros_like(s)
+    BornOp(p, wav, s, rho).adjoint(a0, a1, res)
+    assert rel_l2(g0, a0) < 1e-6 and rel_l2(g1, a1) < 1e-6

@@ -381,3 +381,59 @@ def test_bornrefl_borntomo(gpu_lib, oracle, case, mode):
     op.adjoint(a, d)
     q = oracle.borntomo_adjoint(p, wav, s, refl, d, kind=WEM_DATA_TIME, prec=64)
     assert rel_l2(a, q) < TOL_OP, ("tomo adj", rel_l2(a, q))
+
+
+@pytest.mark.parametrize("case", ["n768t0", "n512t0p"])
+@pytest.mark.parametrize("mode", ["compat", "exact"])
+def test_ext_born_warp_tap0(gpu_lib, oracle, case, mode):
+    """Frequency-extended Born on the warp kernels at tap 0: per-frequency
+    tables, the spectral reuse of the as-coded adjoint and the extended
+    last-row rule (one shot's LinUp^H term)."""
+    from wemgpu.core import ExtBornOp
+    p, par, wav, s, rho = small_case(nz=10, ns=3, adjoint_mode=mode, **WARP_CASES[case])
+    nf = oracle.count_freqs(p)[0]
+    rng = np.random.default_rng(19)
+    s3 = (np.repeat(s[None], nf, 0) * (1 + 0.02 * rng.standard_normal((nf, 1, 1)))).astype(np.complex64)
+    r3 = np.repeat(rho[None], nf, 0)
+    ds = (rand_c(rng, s3.shape) * 1e-8).astype(np.complex64)
+    dr = (rand_c(rng, s3.shape) * 0.1).astype(np.complex64)
+    op = ExtBornOp(p, wav, s3, r3)
+    g = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    op.forward(ds, dr, g)
+    o = oracle.extborn_forward(p, wav, s3, r3, ds, dr, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(g, o) < TOL_OP, rel_l2(g, o)
+    d = (rng.random(g.shape) - .5).astype(np.float32)
+    a0, a1 = np.zeros_like(s3), np.zeros_like(s3)
+    op.adjoint(a0, a1, d)
+    b0, b1 = oracle.extborn_adjoint(p, wav, s3, r3, d, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(a0, b0) < TOL_OP, rel_l2(a0, b0)
+    assert rel_l2(a1, b1) < TOL_OP, rel_l2(a1, b1)
+
+
+@pytest.mark.parametrize("kw", [dict(prop="pspi", nref=2), dict(ntaylor=0), dict(ntaylor=2)])
+def test_bornrefl_borntomo_shared_memory_path(gpu_lib, oracle, kw):
+    """BornRefl / BornTomo with several references (PSPI) and with Taylor
+    orders the warp kernels do not serve (shared-memory kernels)."""
+    from wemgpu.core import BornReflOp, BornTomoOp
+    p, par, wav, s, rho = small_case(nz=10, ns=2, **kw)
+    nf = oracle.count_freqs(p)[0]
+    rng = np.random.default_rng(43)
+    m = rand_c(rng, (nf, p.nz, p.nx)) * 0.1
+    d = (rng.random((p.ns, p.nr, p.nt)) - .5).astype(np.float32)
+    op = BornReflOp(p, wav, s)
+    g = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    op.forward(m, g)
+    assert rel_l2(g, oracle.bornrefl_forward(p, wav, s, m, prec=64)) < TOL_OP
+    a = np.zeros((nf, p.nz, p.nx), np.complex64)
+    op.adjoint(a, d)
+    assert rel_l2(a, oracle.bornrefl_adjoint(p, wav, s, d, prec=64)) < TOL_OP
+    refl = (rand_c(rng, (nf, p.nz, p.nx)) * 0.2).astype(np.complex64)
+    dm = (rand_c(rng, (p.nz, p.nx)) * 1e-8).astype(np.complex64)
+    op = BornTomoOp(p, wav, s)
+    op.set_refl(refl)
+    g = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    op.forward(dm, g)
+    assert rel_l2(g, oracle.borntomo_forward(p, wav, s, refl, dm, prec=64)) < TOL_OP
+    a = np.zeros((p.nz, p.nx), np.complex64)
+    op.adjoint(a, d)
+    assert rel_l2(a, oracle.borntomo_adjoint(p, wav, s, refl, d, prec=64)) < TOL_OP
