@@ -437,3 +437,23 @@ def test_bornrefl_borntomo_shared_memory_path(gpu_lib, oracle, kw):
     a = np.zeros((p.nz, p.nx), np.complex64)
     op.adjoint(a, d)
     assert rel_l2(a, oracle.borntomo_adjoint(p, wav, s, refl, d, prec=64)) < TOL_OP
+
+
+@pytest.mark.parametrize("kw", [dict(), dict(nx=240, pad=4, tap=4), dict(nx=768, pad=0, tap=0)])
+@pytest.mark.parametrize("nz,ns", [(2, 1), (3, 1), (5, 9)])
+def test_small_geometries(gpu_lib, oracle, kw, nz, ns):
+    """Smallest depth axes (one step), one shot and more shots than rows per
+    CTA, on the shared-memory kernels (N = 72) and the warp kernels (256, 768)."""
+    from wemgpu.core import BornOp, WemOp
+    p, par, wav, s, rho = small_case(nz=nz, ns=ns, **kw)
+    d = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    WemOp(p, wav).forward(s, rho, d)
+    o = oracle.wem_forward(p, wav, s, rho, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(d, o) < TOL_OP, ("wem", rel_l2(d, o))
+    rng = np.random.default_rng(51)
+    dd = (rng.random(d.shape) - .5).astype(np.float32)
+    a0, a1 = np.zeros_like(s), np.zeros_like(s)
+    BornOp(p, wav, s, rho).adjoint(a0, a1, dd)
+    q0, q1 = oracle.born_adjoint(p, wav, s, rho, dd, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(a0, q0) < TOL_OP, ("adj s", rel_l2(a0, q0))
+    assert rel_l2(a1, q1) < TOL_OP, ("adj rho", rel_l2(a1, q1))
