@@ -297,6 +297,35 @@ int wemop_onestep_noalloc(const wem_params* p, const void* slow_row, const void*
                           const signed char* refidx, int nxg, float freq, int adj,
                           const void* in, void* out, int nrow, int add, void* stream);
 
+/* ------------------------------------------- model-space interpolation
+ * Coarse-to-fine interpolation of a 2D complex model, the preconditioner of
+ * the FWI driver (scripts/fwi.py:45-68):
+ *   data[i2][i1] = sum_j2 sum_j1 F2[i2][j2] F1[i1][j1] model[j2][j1],
+ * model complex [nm2][nm1] (coarse), data complex [nd2][nd1] (fine), axis 1
+ * fast.  The separable filters depend on the sampling intervals only (the
+ * axes' origins are not used, as in the reference).  Pointers may be host
+ * or device memory; add as above.
+ *
+ * lanczos2d_create: LanczosInterpolation2D
+ *   (operator/src/LanczosInterpolation2D.h:14-125; Operator.py:436-445);
+ *   a[0], a[1] = half widths in coarse samples along axes 1 and 2.
+ * spline2d_create: Spline2D (operator/src/Spline2D.h:14-130;
+ *   Operator.py:447-478), the cubic of parameters (a, b); its adjoint then
+ *   copies the model's edge columns and rows from their neighbours
+ *   (Spline2D.h:84-92), so it is not the transpose at the edges.
+ * Both need at least 2 coarse samples per axis and positive intervals. */
+typedef struct interp2d_handle interp2d_handle;
+
+/* replaces pyOp.LanczosInterpolation2D(model, data, a) (operator/src/python/pyOp.cpp:55-64) */
+int lanczos2d_create(int nm1, float dm1, int nm2, float dm2, int nd1, float dd1, int nd2, float dd2,
+                     const float* a, interp2d_handle** out);
+/* replaces pyOp.Spline2D(model, data, a, b) (operator/src/python/pyOp.cpp:66-75) */
+int spline2d_create(int nm1, float dm1, int nm2, float dm2, int nd1, float dd1, int nd2, float dd2,
+                    float a, float b, interp2d_handle** out);
+void interp2d_destroy(interp2d_handle* h);
+int interp2d_forward(interp2d_handle* h, const void* model, void* data, int add);
+int interp2d_adjoint(interp2d_handle* h, void* model, const void* data, int add);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,7 +21,7 @@ def lib():
 def _declared():
     src = open(os.path.join(ROOT, "include", "wemgpu.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b([a-z_]+)\s*\(", src)) - {"if", "sizeof", "for", "while"})
+    return sorted(set(re.findall(r"\b([a-z_][a-z0-9_]*)\s*\(", src)) - {"if", "sizeof", "for", "while"})
 
 
 def test_exports_every_declared_symbol(lib):

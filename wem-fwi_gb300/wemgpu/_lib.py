@@ -70,6 +70,11 @@ _SIGS = {
     "wemop_scatter": (_i, [_h, _i, _f, _i, _v, _v, _i, _i]),
     "wemop_refsampler": (_i, [_h, _v, _v]),
     "wemop_onestep_noalloc": (_i, [_pp, _v, _v, _v, _i, _f, _i, _v, _v, _i, _i, _v]),
+    "lanczos2d_create": (_i, [_i, _f, _i, _f, _i, _f, _i, _f, ctypes.POINTER(_f), ctypes.POINTER(_h)]),
+    "spline2d_create": (_i, [_i, _f, _i, _f, _i, _f, _i, _f, _f, _f, ctypes.POINTER(_h)]),
+    "interp2d_destroy": (None, [_h]),
+    "interp2d_forward": (_i, [_h, _v, _v, _i]),
+    "interp2d_adjoint": (_i, [_h, _v, _v, _i]),
 }
 
 EXPORTED = tuple(_SIGS)

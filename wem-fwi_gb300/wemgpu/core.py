@@ -316,6 +316,45 @@ class RowOps:
         return sref, idx
 
 
+class Interp2DOp:
+    """Coarse-to-fine model interpolation (lanczos2d_* / spline2d_*): model
+    complex ``[nm2][nm1]`` -> data complex ``[nd2][nd1]``.  ``m_axes`` and
+    ``d_axes`` are ``((n1, d1), (n2, d2))``; ``kind`` is ``"lanczos"`` (``a`` =
+    two half widths in coarse samples) or ``"spline"`` (``a``, ``b`` the cubic's
+    parameters)."""
+
+    def __init__(self, kind, m_axes, d_axes, a, b=0.0):
+        (nm1, dm1), (nm2, dm2) = m_axes
+        (nd1, dd1), (nd2, dd2) = d_axes
+        self.model_shape = (int(nm2), int(nm1))
+        self.data_shape = (int(nd2), int(nd1))
+        self.h = ctypes.c_void_p()
+        geo = (int(nm1), float(dm1), int(nm2), float(dm2), int(nd1), float(dd1), int(nd2), float(dd2))
+        if kind == "lanczos":
+            aa = (ctypes.c_float * 2)(float(a[0]), float(a[1]))
+            _lib.call("lanczos2d_create", *geo, aa, ctypes.byref(self.h))
+        elif kind == "spline":
+            _lib.call("spline2d_create", *geo, float(a), float(b), ctypes.byref(self.h))
+        else:
+            raise ValueError(f"unknown interpolation {kind!r}")
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and h.value:
+            try:
+                _lib.load().interp2d_destroy(h)
+            except Exception:
+                pass
+
+    def forward(self, model, data, add=False):
+        _lib.call("interp2d_forward", self.h, ptr(model, np.complex64, self.model_shape, "model"),
+                  ptr(data, np.complex64, self.data_shape, "data", True), int(bool(add)))
+
+    def adjoint(self, model, data, add=False):
+        _lib.call("interp2d_adjoint", self.h, ptr(model, np.complex64, self.model_shape, "model", True),
+                  ptr(data, np.complex64, self.data_shape, "data"), int(bool(add)))
+
+
 def _like(x):
     if _is_torch(x):
         return torch.zeros_like(x)

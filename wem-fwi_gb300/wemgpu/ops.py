@@ -236,3 +236,64 @@ class BornTomo(Propagator):
 
     def adjoint(self, add, model, data):
         self.cppMode.adjoint(model.getNdArray(), data.getNdArray(), add)
+
+
+class LanczosInterpolation2D(Propagator):
+    """Coarse-to-fine windowed-sinc interpolation of a 2D complex model
+    (Operator.py:436-445; operator/src/LanczosInterpolation2D.h), the model
+    preconditioner of scripts/fwi.py:45-68.  ``a`` holds the half widths in
+    coarse samples along axes 1 and 2 (a third entry is ignored)."""
+
+    def __init__(self, model, data, a=[3, 3, 3]):
+        self.a = list(a)
+        self.setDomainRange(model, data)
+        self.cppMode = core.Interp2DOp("lanczos", _axes2(model), _axes2(data), self.a[:2])
+
+    def __setstate__(self, state):
+        self.__dict__ = state.copy()
+        self.cppMode = core.Interp2DOp("lanczos", _axes2(self.domain), _axes2(self.range), self.a[:2])
+
+    def forward(self, add, model, data):
+        self.cppMode.forward(model.getNdArray(), data.getNdArray(), add)
+
+    def adjoint(self, add, model, data):
+        self.cppMode.adjoint(model.getNdArray(), data.getNdArray(), add)
+
+
+class Spline(Propagator):
+    """Cubic-spline interpolation base (Operator.py:447-465).  ``type`` names
+    a member of the (a, b) family: 'CR-spline' (0.5, 0), 'B-spline' (0, 1),
+    'MN-spline' (1/3, 1/3).  As in the reference, the filter is built from
+    the ``a`` and ``b`` arguments; ``type`` sets the attributes ``a``, ``b``
+    that an unpickled operator is rebuilt with."""
+
+    _TYPES = {"CR-spline": (0.5, 0.0), "B-spline": (0.0, 1.0), "MN-spline": (1 / 3, 1 / 3)}
+
+    def __init__(self, model, data, a=1, b=0, type=None):
+        self.a, self.b = self._TYPES.get(type, (a, b))
+        self.setDomainRange(model, data)
+
+    def forward(self, add, model, data):
+        self.cppMode.forward(model.getNdArray(), data.getNdArray(), add)
+
+    def adjoint(self, add, model, data):
+        self.cppMode.adjoint(model.getNdArray(), data.getNdArray(), add)
+
+
+class Spline2D(Spline):
+    """2D cubic-spline interpolation (Operator.py:467-478; operator/src/Spline2D.h).
+    Its adjoint copies the model's edge columns and rows from their
+    neighbours, as the reference's does, so a dot test fails at the edges."""
+
+    def __init__(self, model, data, a=1, b=0, type=None):
+        super().__init__(model, data, a, b, type=type)
+        self.cppMode = core.Interp2DOp("spline", _axes2(model), _axes2(data), a, b)
+
+    def __setstate__(self, state):
+        self.__dict__ = state.copy()
+        self.cppMode = core.Interp2DOp("spline", _axes2(self.domain), _axes2(self.range), self.a, self.b)
+
+
+def _axes2(vec):
+    h = vec.getHyper()
+    return tuple((h.getAxis(i).n, h.getAxis(i).d) for i in (1, 2))
