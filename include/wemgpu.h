@@ -106,7 +106,23 @@ typedef struct wem_params {
   int   refs_mode;     /* WEM_REFS_ASCODED (default) | WEM_REFS_NEAREST */
   int   nbin;          /* bins of WEM_DATA_FREQ data; 0 = nt + tpad */
   int   phase_law;     /* WEM_PHASE_ISPC (default) | WEM_PHASE_EXACT_KZ */
+  /* conformal-map geometry of WEM and BornFull, one map per shot
+   * (PropParam.h:88-137; conformal/src): every shot propagates in its own
+   * mapped coordinates ("cmap").
+   *   WEM_CMAP_NONE  identity (Identity.h), the default;
+   *   WEM_CMAP_LOG   shift-and-scale onto the unit disc around the source
+   *                  followed by the complex logarithm with inner radius
+   *                  eps_log (ShiftAndScale.h, ComplexLog.h/.cpp): the source
+   *                  becomes a line along the first mapped depth;
+   *   WEM_CMAP_ROT   rotation of the grid by cmap_angles[is] radians
+   *                  (Rotation.h), ns angles (the reference reads them from
+   *                  the JSON file named by "cmap_angles", key "a"). */
+  int   cmap;
+  float eps_log;              /* default 0.01 ("eps_log") */
+  const float* cmap_angles;   /* ns angles for WEM_CMAP_ROT */
 } wem_params;
+
+enum { WEM_CMAP_NONE = 0, WEM_CMAP_LOG = 1, WEM_CMAP_ROT = 2 };
 
 void wem_params_default(wem_params* p);
 

@@ -28,7 +28,8 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compile the restatement with g++ (no external libraries)."""
-    if force or not os.path.exists(_LIB):
+    # make rebuilds only what changed
+    if force or _lib is None:
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB
 

@@ -10,6 +10,7 @@
 #include <functional>
 #include <thread>
 
+#include "cmap_oracle.hpp"
 #include "wem_oracle.hpp"
 
 namespace wo {
@@ -137,18 +138,31 @@ struct DataF {
   C<R>* at(int is, int ir, int b) { return &v[((size_t)is * nr + ir) * nb + b]; }
 };
 
+// the source of shot is: the acquisition's point, or the points of a
+// conformal map (several points of one shot all carry the wavelet)
+template <class R>
+void spread_source(const Problem<R>& P, int is, const Inject<R>* src_ov, C<R>* W, int nx, C<R> wv) {
+  if (!src_ov) {
+    P.src_inj(is).spread(W, nx, &wv);
+    return;
+  }
+  std::vector<C<R>> vals(src_ov->ix.size(), wv);
+  src_ov->spread(W, nx, vals.data());
+}
+
 // ------------------------------------------------------------ WEM forward
 // WEM::full_fwd (propagator/src/wem_prop.cpp:9-78) for one padded model.
 template <class R>
 void wem_row(const Problem<R>& P, const Core<R>& core, const std::vector<C<R>>& r, int is, int f,
-             DataF<R>& D, int bin_col, std::vector<C<R>>& W, Work<R>& wk) {
+             DataF<R>& D, int bin_col, std::vector<C<R>>& W, Work<R>& wk, const Inject<R>* src_ov = nullptr,
+             const Inject<R>* rec_ov = nullptr) {
   const int nx = core.nxg, nz = core.nz;
   R w = Core<R>::omega(P.F.freq[f]);
   std::fill(W.begin(), W.end(), C<R>(0));
   C<R> wv = P.wave_f[P.F.bin[f]];
-  P.src_inj(is).spread(W.data(), nx, &wv);
+  spread_source(P, is, src_ov, W.data(), nx, wv);
   down_fwd(core, w, W.data(), W.data(), true, wk);
-  Inject<R> rec = P.rec_inj();
+  Inject<R> rec = rec_ov ? *rec_ov : P.rec_inj();
   std::vector<C<R>> vals(rec.ix.size());
   auto record = [&]() {
     for (size_t i = 0; i < vals.size(); ++i) vals[i] = *D.at(is, (int)i, bin_col);
@@ -239,11 +253,12 @@ struct BornBg {
 template <class R>
 void born_row_fwd(const Problem<R>& P, const Core<R>& core, const std::vector<C<R>>& r, const DRefl<R>& dR,
                   const std::vector<C<R>>& gm0, const std::vector<C<R>>& gm1, int is, int f, DataF<R>& D,
-                  std::vector<C<R>>& bg, std::vector<C<R>>& sc, std::vector<C<R>>& dr, Work<R>& wk) {
+                  std::vector<C<R>>& bg, std::vector<C<R>>& sc, std::vector<C<R>>& dr, Work<R>& wk,
+                  const Inject<R>* src_ov = nullptr, const Inject<R>* rec_ov = nullptr) {
   const int nx = core.nxg;
   const int bin = P.F.bin[f];
   R w = Core<R>::omega(P.F.freq[f]);
-  Inject<R> rec = P.rec_inj();
+  Inject<R> rec = rec_ov ? *rec_ov : P.rec_inj();
   std::vector<C<R>> vals(rec.ix.size());
   auto record = [&](const std::vector<C<R>>& W) {
     for (size_t i = 0; i < vals.size(); ++i) vals[i] = *D.at(is, (int)i, bin);
@@ -253,7 +268,7 @@ void born_row_fwd(const Problem<R>& P, const Core<R>& core, const std::vector<C<
   // down background wavefield
   std::fill(bg.begin(), bg.end(), C<R>(0));
   C<R> wv = P.wave_f[bin];
-  P.src_inj(is).spread(bg.data(), nx, &wv);
+  spread_source(P, is, src_ov, bg.data(), nx, wv);
   down_fwd(core, w, bg.data(), bg.data(), true, wk);
   // forward scattering
   lindown_fwd(core, w, bg.data(), gm0.data(), sc.data(), false, wk);
@@ -284,11 +299,11 @@ template <class R>
 void born_row_adj(const Problem<R>& P, const Core<R>& core, const std::vector<C<R>>& r, const DRefl<R>& dR,
                   std::vector<C<R>>& gm0, std::vector<C<R>>& gm1, int is, int f, DataF<R>& D, bool exact,
                   bool ext_order, std::vector<C<R>>& bg, std::vector<C<R>>& sc, std::vector<C<R>>& dr,
-                  Work<R>& wk) {
+                  Work<R>& wk, const Inject<R>* src_ov = nullptr, const Inject<R>* rec_ov = nullptr) {
   const int nx = core.nxg;
   const int bin = P.F.bin[f];
   R w = Core<R>::omega(P.F.freq[f]);
-  Inject<R> rec = P.rec_inj();
+  Inject<R> rec = rec_ov ? *rec_ov : P.rec_inj();
   std::vector<C<R>> vals(rec.ix.size());
   auto inject_data = [&]() {  // Injection::forward 3D, add = 0
     std::fill(sc.begin(), sc.end(), C<R>(0));
@@ -308,7 +323,7 @@ void born_row_adj(const Problem<R>& P, const Core<R>& core, const std::vector<C<
   };
   std::fill(bg.begin(), bg.end(), C<R>(0));
   C<R> wv = P.wave_f[bin];
-  P.src_inj(is).spread(bg.data(), nx, &wv);
+  spread_source(P, is, src_ov, bg.data(), nx, wv);
   down_fwd(core, w, bg.data(), bg.data(), true, wk);
   // born_prop.cpp:193-199 reflectivity first; ext_born_prop.cpp:159-165 the
   // forward-scattering term first
@@ -405,6 +420,144 @@ void born_adjoint(const wem_params& p, const float* wavelet, const float* bs2, c
       }
   store(ds2, m0.data(), nm, add);
   store(drho, m1.data(), nm, add);
+}
+
+// ------------------------------------------------------- conformal maps
+// One shot of a cmap operator: its chain of maps, the shot's parameters on
+// the mapped grid, its devices there, and the mapped background
+// (wem_prop.cpp:19-45, born_prop.cpp:28-70).
+template <class R>
+struct CmapShot {
+  cm::ShotChain chain;
+  wem_params ps{};
+  Inject<R> src, rec;
+  std::vector<C<R>> sp, dp, r;
+  std::unique_ptr<Core<R>> core;
+  std::unique_ptr<DRefl<R>> drefl;
+};
+
+template <class R>
+void cmap_shot_setup(const Problem<R>& P, int is, const float* s2, const float* rho, bool born, CmapShot<R>& S) {
+  const wem_params& p = P.p;
+  check(p.cmap == 1 || p.cmap == 2, "cmap must be 0, 1 or 2");
+  check(p.cmap != 2 || p.cmap_angles != nullptr, "cmap 2 needs cmap_angles");
+  check(p.cmap != 1 || p.nr >= 2, "cmap 1 needs at least 2 receivers");
+  const cm::Hyper model{p.nx, p.nz, p.ox, p.dx, p.oz, p.dz};
+  S.chain = cm::shot_chain(p.cmap, model, P.src.iz[is], P.src.ix[is], p.eps_log,
+                           p.cmap == 2 ? p.cmap_angles[is] : 0.f);
+  const cm::Hyper& h = S.chain.out();
+  S.ps = p;
+  S.ps.ns = 1;
+  S.ps.cmap = 0;
+  S.ps.ox = h.o1;
+  S.ps.dx = h.d1;
+  S.ps.oz = h.o2;
+  S.ps.dz = h.d2;
+  // devices on the mapped grid
+  std::vector<int> sz, sx, rz, rx;
+  S.chain.points({P.src.iz[is]}, {P.src.ix[is]}, sz, sx);
+  S.chain.points(P.rec.iz, P.rec.ix, rz, rx);
+  for (size_t i = 0; i < rz.size(); ++i)
+    check(rz[i] >= 0 && rz[i] < h.n2 && rx[i] >= 0 && rx[i] < h.n1, "cmap: a receiver maps outside the grid");
+  for (size_t i = 1; i < sz.size(); ++i) check(sz[i] == sz[0], "cmap: source points of a shot at several depths");
+  S.src = Inject<R>(sx, sz, p.ngs, p.pad);
+  S.rec = Inject<R>(rx, rz, p.ngr, p.pad);
+  // background: mapped, edge padded; Reflect from it; then the Jacobian,
+  // twice, by flat index of the padded grid; the rest sees the scaled grid
+  const size_t n = (size_t)p.nx * p.nz;
+  std::vector<C<R>> ms = S.chain.forward(load<R>(s2, n)), mr = S.chain.forward(load<R>(rho, n));
+  const int nxg = P.nxg;
+  S.sp.assign((size_t)nxg * p.nz, C<R>(0));
+  S.dp.assign((size_t)nxg * p.nz, C<R>(0));
+  pad_x(ms.data(), S.sp.data(), p.nz, p.nx, p.pad, true);
+  pad_x(mr.data(), S.dp.data(), p.nz, p.nx, p.pad, true);
+  S.r = reflect_coefs(S.sp.data(), S.dp.data(), nxg, p.nz);
+  S.chain.scale_by_jacobian(S.sp.data());
+  S.chain.scale_by_jacobian(S.sp.data());
+  S.core = std::make_unique<Core<R>>(S.ps, S.sp.data(), nxg, p.nz);
+  if (born) S.drefl = std::make_unique<DRefl<R>>(S.sp.data(), S.dp.data(), nxg, p.nz);
+}
+
+// a perturbation on the shot's mapped grid, zero padded (born_prop.cpp:50-57)
+template <class R>
+std::vector<C<R>> cmap_perturbation(const Problem<R>& P, const CmapShot<R>& S, const float* m) {
+  const wem_params& p = P.p;
+  std::vector<C<R>> mm = S.chain.forward(load<R>(m, (size_t)p.nx * p.nz));
+  std::vector<C<R>> out((size_t)P.nxg * p.nz, C<R>(0));
+  pad_x(mm.data(), out.data(), p.nz, p.nx, p.pad, false);
+  return out;
+}
+
+template <class R>
+void cmap_wem_forward(const wem_params& p, const float* wavelet, const float* s2, const float* rho, void* data,
+                      int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  DataF<R> D = new_dataf(P);
+  const int nf = P.nfreq();
+  parallel_for(p.ns, nthreads, [&](int is, int) {
+    CmapShot<R> S;
+    cmap_shot_setup(P, is, s2, rho, false, S);
+    Work<R> wk(S.core->N, P.nxg);
+    std::vector<C<R>> W((size_t)P.nxg * p.nz);
+    for (int f = 0; f < nf; ++f) wem_row(P, *S.core, S.r, is, f, D, P.F.bin[f], W, wk, &S.src, &S.rec);
+  });
+  emit_data(P, D, data, kind, add, nthreads);
+}
+
+template <class R>
+void cmap_born_forward(const wem_params& p, const float* wavelet, const float* bs2, const float* brho,
+                       const float* ds2, const float* drho, void* data, int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  DataF<R> D = new_dataf(P);
+  const int nf = P.nfreq();
+  const size_t ng = (size_t)P.nxg * p.nz;
+  parallel_for(p.ns, nthreads, [&](int is, int) {
+    CmapShot<R> S;
+    cmap_shot_setup(P, is, bs2, brho, true, S);
+    std::vector<C<R>> gm0 = cmap_perturbation(P, S, ds2), gm1 = cmap_perturbation(P, S, drho);
+    Work<R> wk(S.core->N, P.nxg);
+    std::vector<C<R>> bg(ng), sc(ng), dr(ng);
+    for (int f = 0; f < nf; ++f)
+      born_row_fwd(P, *S.core, S.r, *S.drefl, gm0, gm1, is, f, D, bg, sc, dr, wk, &S.src, &S.rec);
+  });
+  emit_data(P, D, data, kind, add, nthreads);
+}
+
+// every shot's gradient, unpadded on its mapped grid, comes back through the
+// inverse map and the shots are summed in order (born_prop.cpp:217-232)
+template <class R>
+void cmap_born_adjoint(const wem_params& p, const float* wavelet, const float* bs2, const float* brho, float* ds2,
+                       float* drho, const void* data, int kind, bool add, int nthreads) {
+  Problem<R> P(p, wavelet);
+  DataF<R> D = absorb_data(P, data, kind, nthreads);
+  const bool exact = p.adjoint_mode == WEM_ADJ_EXACT;
+  const int nf = P.nfreq(), nx = P.nxg, nz = p.nz;
+  const size_t ng = (size_t)nx * nz, nm = (size_t)p.nx * nz;
+  std::vector<std::vector<C<R>>> back0(p.ns), back1(p.ns);
+  parallel_for(p.ns, nthreads, [&](int is, int) {
+    CmapShot<R> S;
+    cmap_shot_setup(P, is, bs2, brho, true, S);
+    Work<R> wk(S.core->N, nx);
+    std::vector<C<R>> bg(ng), sc(ng), dr(ng), g0(ng, C<R>(0)), g1(ng, C<R>(0));
+    for (int f = 0; f < nf; ++f)
+      born_row_adj(P, *S.core, S.r, *S.drefl, g0, g1, is, f, D, exact, false, bg, sc, dr, wk, &S.src, &S.rec);
+    std::vector<C<R>> m0(nm), m1(nm);
+    for (int iz = 0; iz < nz; ++iz)
+      for (int ix = 0; ix < p.nx; ++ix) {
+        m0[(size_t)iz * p.nx + ix] = g0[(size_t)iz * nx + ix + p.pad];
+        m1[(size_t)iz * p.nx + ix] = g1[(size_t)iz * nx + ix + p.pad];
+      }
+    back0[is] = S.chain.inverse(m0);
+    back1[is] = S.chain.inverse(m1);
+  });
+  std::vector<C<R>> t0(nm, C<R>(0)), t1(nm, C<R>(0));
+  for (int is = 0; is < p.ns; ++is)
+    for (size_t i = 0; i < nm; ++i) {
+      t0[i] += back0[is][i];
+      t1[i] += back1[is][i];
+    }
+  store(ds2, t0.data(), nm, add);
+  store(drho, t1.data(), nm, add);
 }
 
 // --------------------------------------------------- frequency-extended
@@ -733,8 +886,14 @@ int oracle_fft(int n, double* x, int sign) {
 int oracle_wem_forward(const wem_params* p, const float* wavelet, const float* s2, const float* rho,
                        void* data, int kind, int add, int prec, int nthreads) {
   return run_guarded([&] {
-    if (prec == 64) wem_forward<double>(*p, wavelet, s2, rho, data, kind, add, nthreads);
-    else wem_forward<float>(*p, wavelet, s2, rho, data, kind, add, nthreads);
+    if (p->cmap) {
+      if (prec == 64) cmap_wem_forward<double>(*p, wavelet, s2, rho, data, kind, add, nthreads);
+      else cmap_wem_forward<float>(*p, wavelet, s2, rho, data, kind, add, nthreads);
+    } else if (prec == 64) {
+      wem_forward<double>(*p, wavelet, s2, rho, data, kind, add, nthreads);
+    } else {
+      wem_forward<float>(*p, wavelet, s2, rho, data, kind, add, nthreads);
+    }
   });
 }
 
@@ -742,8 +901,14 @@ int oracle_born_forward(const wem_params* p, const float* wavelet, const float* 
                         const float* ds2, const float* drho, void* data, int kind, int add, int prec,
                         int nthreads) {
   return run_guarded([&] {
-    if (prec == 64) born_forward<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
-    else born_forward<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+    if (p->cmap) {
+      if (prec == 64) cmap_born_forward<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+      else cmap_born_forward<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+    } else if (prec == 64) {
+      born_forward<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+    } else {
+      born_forward<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+    }
   });
 }
 
@@ -751,8 +916,14 @@ int oracle_born_adjoint(const wem_params* p, const float* wavelet, const float* 
                         float* ds2, float* drho, const void* data, int kind, int add, int prec, int nthreads,
                         int fchunks) {
   return run_guarded([&] {
-    if (prec == 64) born_adjoint<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads, fchunks);
-    else born_adjoint<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads, fchunks);
+    if (p->cmap) {
+      if (prec == 64) cmap_born_adjoint<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+      else cmap_born_adjoint<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads);
+    } else if (prec == 64) {
+      born_adjoint<double>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads, fchunks);
+    } else {
+      born_adjoint<float>(*p, wavelet, bs2, brho, ds2, drho, data, kind, add, nthreads, fchunks);
+    }
   });
 }
 

@@ -57,3 +57,23 @@ def rel_l2(a, b):
     a = np.asarray(a, np.complex128)
     b = np.asarray(b, np.complex128)
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def cmap_case(cmap, nx=64, nz=32, ns=3, nr=24, tap=0, pad=0, prop="ssf", nref=1, adjoint_mode="compat",
+              angles=None, eps_log=0.01, seed=1, ngs=0, ngr=1, nt=128, dt=0.008, fmin=6.0, fmax=14.0):
+    """Conformal-map problem (PropParam.h:88-137): grid spacing 12.5 m from
+    the origin (so coordinates convert to grid cells exactly), sources
+    inside the model, receivers along the surface."""
+    s, rho = layered_model(nz, nx, seed)
+    d = 12.5
+    sx = [d * (nx * (k + 1) // (ns + 1)) for k in range(ns)]
+    sz = [d * (nz // 2 + (k % 2) * 3) for k in range(ns)]
+    rx = [d * (1 + (nx - 3) * k // max(nr - 1, 1)) for k in range(nr)]
+    rz = [0.0] * nr
+    par = dict(sx=sx, sz=sz, rx=rx, rz=rz, prop=prop, nref=nref, tap=tap, pad=pad, fmin=fmin, fmax=fmax,
+               ngs=ngs, ngr=ngr, adjoint_mode=adjoint_mode, cmap=cmap, eps_log=eps_log)
+    if cmap == 2:
+        par["cmap_angles"] = list(angles if angles is not None else np.linspace(0.5, -0.5, ns))
+    p = make_params(par, nx=nx, nz=nz, dx=d, dz=d, nt=nt, dt=dt)
+    wav = ricker(nt, dt, 10.0)
+    return p, par, wav, s, rho

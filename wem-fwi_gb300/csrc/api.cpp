@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "cmap.h"
 #include "kernels.h"
 #include "planner.h"
 #include "wemgpu.h"
@@ -196,8 +197,37 @@ class Engine {
     F_ = geo_.nfreq();
     M_ = ext ? F_ : 1;
     M_img_ = (ext || kind == 1) ? F_ : 1;
+    // conformal maps (wem_prop.cpp:19-45, born_prop.cpp:28-70): every shot
+    // propagates on its own mapped grid, so each gets an engine of one shot
+    // with that grid, its mapped devices and its gather tables
+    std::vector<ShotMap> maps;
+    if (p.cmap != WEM_CMAP_NONE) {
+      require(!ext && kind == 0, "cmap applies to WEM and BornFull only");
+      maps = make_shot_maps(p, geo_);
+    }
     int dev = 0;
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    if (!maps.empty()) {
+      for (int s = 0; s < geo_.ns; ++s) {
+        const ShotMap& m = maps[s];
+        wem_params ps = p;
+        ps.cmap = WEM_CMAP_NONE;
+        ps.ns = 1;
+        ps.ox = m.o1;
+        ps.dx = m.d1;
+        ps.oz = m.o2;
+        ps.dz = m.d2;
+        Geometry gs = geo_;
+        gs.ns = 1;
+        gs.sx = m.src_x;
+        gs.sz = {m.src_z};
+        gs.sptr = {0, (int)m.src_x.size()};
+        gs.rx = m.rec_x;
+        gs.rz = m.rec_z;
+        shots_.push_back(std::unique_ptr<Engine>(new Engine(ps, gs, m, born)));
+      }
+      return;
+    }
     build_static();
     ctx_.ext_model = kind == 1 ? 1 : 0;
     ctx_.no_fwd_record = kind == 2 ? 1 : 0;
@@ -209,7 +239,17 @@ class Engine {
 
   void set_background(const void* s2, const void* rho) {
     require(s2 && rho, "background model is NULL");
-    build_background(s2, rho);
+    if (!shots_.empty()) {
+      // kept here; every shot maps it onto its grid when it runs
+      const size_t nm = (size_t)p_.nz * p_.nx * 8;
+      Staged a, b;
+      a.in(s2, nm);
+      b.in(rho, nm);
+      cuda_check(cudaMemcpy(cm_bg0_.get(nm), a.dev, nm, cudaMemcpyDeviceToDevice), "copy background");
+      cuda_check(cudaMemcpy(cm_bg1_.get(nm), b.dev, nm, cudaMemcpyDeviceToDevice), "copy background");
+    } else {
+      build_background(s2, rho);
+    }
     have_bg_ = true;
   }
 
@@ -223,6 +263,15 @@ class Engine {
   int warp_G(int which) const { return g_plain ? 1 : std::min(geo_.ns, warp_rows_per_group(ctx_, which)); }
 
   void wem_forward(const void* s2, const void* rho, void* data, int kind, int add) {
+    if (!shots_.empty()) {
+      require(s2 && rho && data, "NULL argument");
+      const size_t nm = (size_t)p_.nz * p_.nx * 8;
+      Staged a, b;
+      a.in(s2, nm);
+      b.in(rho, nm);
+      for (int s = 0; s < geo_.ns; ++s) shots_[s]->wem_forward(a.dev, b.dev, shot_data(data, kind, s), kind, add);
+      return;
+    }
     set_background(s2, rho);
     zero_bins();
     wem_pass();
@@ -247,6 +296,28 @@ class Engine {
   // tables built once for both passes)
   double fwi_gradient(const void* s2, const void* rho, const void* dobs, void* g_s2, void* g_rho) {
     require(s2 && rho && dobs && g_s2 && g_rho, "NULL argument");
+    if (!shots_.empty()) {
+      const size_t nm = (size_t)p_.nz * p_.nx;
+      Staged a, b, ob, o0, o1;
+      a.in(s2, nm * 8);
+      b.in(rho, nm * 8);
+      ob.in(dobs, (size_t)geo_.ns * geo_.nr * p_.nt * 4);
+      o0.out(g_s2, nm * 8, false);
+      o1.out(g_rho, nm * 8, false);
+      float2* g0 = cm_g0_.as<float2>(nm);
+      float2* g1 = cm_g1_.as<float2>(nm);
+      double loss = 0;
+      for (int s = 0; s < geo_.ns; ++s) {
+        Engine& e = *shots_[s];
+        loss += e.fwi_gradient(a.dev, b.dev, shot_data(ob.dev, WEM_DATA_TIME, s), g0, g1);
+        e.image_back(g0, (float2*)o0.dev, s > 0);
+        e.image_back(g1, (float2*)o1.dev, s > 0);
+      }
+      cuda_check(cudaStreamSynchronize(0), "fwi_gradient");
+      o0.finish(g_s2);
+      o1.finish(g_rho);
+      return loss;
+    }
     set_background(s2, rho);
     zero_bins();
     wem_pass();
@@ -265,6 +336,18 @@ class Engine {
 
   void born_forward(const void* ds2, const void* drho, void* data, int kind, int add) {
     require(have_bg_, "background not set");
+    if (!shots_.empty()) {
+      require(ds2 && drho && data, "NULL argument");
+      const size_t nm = (size_t)p_.nz * p_.nx * 8;
+      Staged a, b;
+      a.in(ds2, nm);
+      b.in(drho, nm);
+      for (int s = 0; s < geo_.ns; ++s) {
+        shots_[s]->set_background(cm_bg0_.p, cm_bg1_.p);
+        shots_[s]->born_forward(a.dev, b.dev, shot_data(data, kind, s), kind, add);
+      }
+      return;
+    }
     const size_t plane = (size_t)p_.nz * geo_.nxg;
     float2* dm0 = dm0_.as<float2>((size_t)M_ * plane);
     float2* dm1 = dm1_.as<float2>((size_t)M_ * plane);
@@ -368,6 +451,27 @@ class Engine {
   void born_adjoint(void* ds2, void* drho, const void* data, int kind, int add) {
     require(have_bg_, "background not set");
     require(ds2 && drho && data, "NULL argument");
+    if (!shots_.empty()) {
+      // every shot's gradient is brought back to the model grid by the
+      // inverse map and summed in shot order (born_prop.cpp:217-232)
+      const size_t nm = (size_t)p_.nz * p_.nx;
+      Staged o0, o1;
+      o0.out(ds2, nm * 8, add != 0);
+      o1.out(drho, nm * 8, add != 0);
+      float2* g0 = cm_g0_.as<float2>(nm);
+      float2* g1 = cm_g1_.as<float2>(nm);
+      for (int s = 0; s < geo_.ns; ++s) {
+        Engine& e = *shots_[s];
+        e.set_background(cm_bg0_.p, cm_bg1_.p);
+        e.born_adjoint(g0, g1, shot_data(data, kind, s), kind, 0);
+        e.image_back(g0, (float2*)o0.dev, s > 0 || add);
+        e.image_back(g1, (float2*)o1.dev, s > 0 || add);
+      }
+      cuda_check(cudaStreamSynchronize(0), "born_adjoint");
+      o0.finish(ds2);
+      o1.finish(drho);
+      return;
+    }
     absorb(data, kind);
     adj_pass();
     grad_out(ds2, drho, add);
@@ -429,7 +533,50 @@ class Engine {
     o1.finish(drho);
   }
 
+  // a model-grid field of this shot's mapped grid back onto the model grid
+  // (the conformal map's inverse), into or onto out
+  void image_back(const float2* mapped, float2* out, bool add) {
+    require(map_ != nullptr, "not a conformal-map shot");
+    launch_cmap_gather(mapped, map_->inv.as<int>(map_->n), out, map_->n, add ? 1 : 0, 0);
+    cuda_check(cudaGetLastError(), "cmap gather launch");
+  }
+
  private:
+  // one shot of a conformal-map operator: its mapped grid (p.dx, p.dz) and
+  // devices (g) and the gather tables of its map
+  Engine(const wem_params& p, const Geometry& g, const ShotMap& m, bool born)
+      : p_(p), ext_(false), born_(born), kind_(0) {
+    geo_ = g;
+    F_ = geo_.nfreq();
+    M_ = 1;
+    M_img_ = 1;
+    build_static();
+    map_.reset(new MapDev);
+    map_->n = p.nx * p.nz;
+    upload(map_->fwd, m.fwd);
+    upload(map_->inv, m.inv);
+    map_->js = m.js;
+    map_->scale = m.js != 1.f || !m.jl.empty();
+    if (!m.jl.empty()) map_->jl_d = upload(map_->jl, m.jl);
+  }
+
+  // a shot's slice of caller data
+  void* shot_data(const void* data, int kind, int s) const {
+    const size_t per = (size_t)geo_.nr * (kind == WEM_DATA_TIME ? (size_t)p_.nt * 4 : (size_t)geo_.nbin * 8);
+    return (char*)const_cast<void*>(data) + per * s;
+  }
+
+  struct MapDev {
+    int n = 0;
+    Buf fwd, inv, jl;
+    float js = 1;
+    const float* jl_d = nullptr;
+    bool scale = false;
+  };
+  std::unique_ptr<MapDev> map_;                // this engine is one shot of a conformal-map operator
+  std::vector<std::unique_ptr<Engine>> shots_;  // this operator runs one engine per mapped shot
+  Buf cm_bg0_, cm_bg1_, cm_g0_, cm_g1_, cm_map0_, cm_map1_, cm_map2_, spr_, sptr_;
+
   wem_params p_;
   bool ext_, born_;
   int kind_ = 0;
@@ -494,6 +641,7 @@ class Engine {
     ctx_.bin = upload(bin_, fidx);
     ctx_.wave = upload(wave_, to_f2(g.wave_at));
     ctx_.sx = upload(sx_, g.sx);
+    ctx_.sptr = g.sptr.empty() ? nullptr : upload(sptr_, g.sptr);
     ctx_.sz = upload(sz_, g.sz);
     ctx_.gs = upload(gs_, gsf);
     ctx_.gr = upload(gr_, grf);
@@ -533,10 +681,30 @@ class Engine {
     Staged ss, sr;
     ss.in(s2, n * 8);
     sr.in(rho, n * 8);
+    const float2 *s_in = (const float2*)ss.dev, *r_in = (const float2*)sr.dev;
+    if (map_) {
+      // the model on this shot's mapped grid (wem_prop.cpp:24-25)
+      float2* ms = cm_map0_.as<float2>(n);
+      float2* mr = cm_map1_.as<float2>(n);
+      launch_cmap_gather(s_in, map_->fwd.as<int>(n), ms, (int)n, -1, 0);
+      launch_cmap_gather(r_in, map_->fwd.as<int>(n), mr, (int)n, -1, 0);
+      s_in = ms;
+      r_in = mr;
+    }
     float2* sp = sp_.as<float2>((size_t)M_ * plane);
     float2* dp = dp_.as<float2>((size_t)M_ * plane);
-    launch_pad_edge((const float2*)ss.dev, sp, M_, nz, nx, p_.pad, 0);
-    launch_pad_edge((const float2*)sr.dev, dp, M_, nz, nx, p_.pad, 0);
+    launch_pad_edge(s_in, sp, M_, nz, nx, p_.pad, 0);
+    launch_pad_edge(r_in, dp, M_, nz, nx, p_.pad, 0);
+    // Reflect keeps the padded slowness as mapped; the Jacobian then scales
+    // it, by flat index of the padded grid, for everything else
+    // (wem_prop.cpp:35-40, born_prop.cpp:44-48)
+    const float2* spr = nullptr;
+    if (map_ && map_->scale) {
+      float2* u = spr_.as<float2>(plane);
+      cuda_check(cudaMemcpyAsync(u, sp, plane * 8, cudaMemcpyDeviceToDevice, 0), "copy slowness");
+      launch_cmap_jacobian(sp, nz * nx, map_->js, map_->jl_d, 0);
+      spr = u;
+    }
     float2* dsref = sref_.as<float2>((size_t)M_ * nz * nref);
     signed char* dref = ref_.as<signed char>((size_t)M_ * plane);
     const bool device_refs = nref == 1 && (p_.refs_mode == WEM_REFS_NEAREST || nz <= nxg - 2);
@@ -550,11 +718,13 @@ class Engine {
           throw Fail(WEM_EINVAL, "Ref velocity " + std::to_string(h[i].x) + " at the layer " +
                                      std::to_string((i / nref) % nz));
     } else {
-      std::vector<float> hs = host_floats(s2, 2 * n);
+      std::vector<float2> hs((size_t)M_ * plane);
+      cuda_check(cudaMemcpy(hs.data(), sp, hs.size() * 8, cudaMemcpyDeviceToHost), "D2H slowness");
       std::vector<float2> sref((size_t)M_ * nz * nref);
       std::vector<signed char> ref((size_t)M_ * plane);
       for (int m = 0; m < M_; ++m) {
-        std::vector<cd> spm = pad_model(hs.data() + 2 * (size_t)m * nz * nx, nz, nx, p_.pad, true);
+        std::vector<cd> spm(plane);
+        for (size_t i = 0; i < plane; ++i) spm[i] = cd(hs[(size_t)m * plane + i].x, hs[(size_t)m * plane + i].y);
         std::vector<cd> sr_m;
         std::vector<signed char> ref_m;
         refsampler(p_, spm, nxg, nz, sr_m, ref_m);
@@ -577,7 +747,7 @@ class Engine {
       a1_ = a1b_.as<float2>((size_t)M_ * plane);
       b1_ = b1b_.as<float2>((size_t)M_ * plane);
     }
-    launch_point_tables(M_, nz, nxg, nref, p_.ntaylor, p_.eps, sp, dp, dsref, dref, q, rc, sc, a0_, b0_, a1_, b1_,
+    launch_point_tables(M_, nz, nxg, nref, p_.ntaylor, p_.eps, sp, spr, dp, dsref, dref, q, rc, sc, a0_, b0_, a1_, b1_,
                         0);
     ctx_.rc = rc;
     ctx_.sc = sc;
@@ -691,8 +861,16 @@ class Engine {
   void pad_perturbation(const void* m, float2* out, int slices) {
     require(m != nullptr, "perturbation is NULL");
     Staged s;
-    s.in(m, (size_t)slices * p_.nz * p_.nx * 8);
-    launch_pad_model((const float2*)s.dev, out, slices, p_.nz, p_.nx, p_.pad, 0);
+    const size_t n = (size_t)slices * p_.nz * p_.nx;
+    s.in(m, n * 8);
+    const float2* src = (const float2*)s.dev;
+    if (map_) {
+      // the perturbation on this shot's mapped grid, unscaled (born_prop.cpp:50-51)
+      float2* t = cm_map2_.as<float2>(n);
+      launch_cmap_gather(src, map_->fwd.as<int>(n), t, (int)n, -1, 0);
+      src = t;
+    }
+    launch_pad_model(src, out, slices, p_.nz, p_.nx, p_.pad, 0);
     cuda_check(cudaGetLastError(), "pad launch");
     cuda_check(cudaStreamSynchronize(0), "pad");
   }
@@ -911,6 +1089,8 @@ void wem_params_default(wem_params* p) {
   p->adjoint_mode = WEM_ADJ_COMPAT;
   p->refs_mode = WEM_REFS_ASCODED;
   p->phase_law = WEM_PHASE_ISPC;
+  p->cmap = WEM_CMAP_NONE;
+  p->eps_log = 0.01f;
 }
 
 const char* wem_last_error(void) { return g_error.c_str(); }

@@ -203,16 +203,20 @@ __device__ void scatter_rows(const DevCtx& c, const float2* tw, int f, int z, in
 }
 
 // ------------------------------------------------- injection / recording
-// Injection.cpp:8-19 (source of shot s0 + r at depth z)
+// Injection.cpp:8-19 (source of shot s0 + r at depth z): one thread per
+// row, points and window taps in order (the windows of several points of a
+// shot may overlap)
 __device__ void inject_src(const DevCtx& c, float2* W, int ldw, int nrow, int s0, int f, int z) {
-  const int w = 2 * c.ngs + 1;
   const float2 wv = c.wave[f];
-  for (int i = threadIdx.x; i < nrow * w; i += blockDim.x) {
-    int r = i / w, g = i - r * w;
-    int s = s0 + r;
+  for (int r = threadIdx.x; r < nrow; r += blockDim.x) {
+    const int s = s0 + r;
     if (c.sz[s] != z) continue;
-    int x = c.sx[s] + g - c.ngs + c.pad;
-    if (x >= 0 && x < c.nxg) W[(size_t)r * ldw + x] = c_add(W[(size_t)r * ldw + x], c_scale(wv, c.gs[g]));
+    const int p0 = c.sptr ? c.sptr[s] : s, p1 = c.sptr ? c.sptr[s + 1] : s + 1;
+    for (int pt = p0; pt < p1; ++pt)
+      for (int g = 0; g <= 2 * c.ngs; ++g) {
+        const int x = c.sx[pt] + g - c.ngs + c.pad;
+        if (x >= 0 && x < c.nxg) W[(size_t)r * ldw + x] = c_add(W[(size_t)r * ldw + x], c_scale(wv, c.gs[g]));
+      }
   }
 }
 

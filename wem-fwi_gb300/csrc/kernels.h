@@ -37,7 +37,8 @@ struct DevCtx {
   const float* omega;           // [F] 2 pi f
   const int* bin;               // [F] data bin of each frequency
   const float2* wave;           // [F] wavelet spectrum at bin[f]
-  const int* sx;                // [ns] source x (unpadded grid index)
+  const int* sx;                // [ns] source x (unpadded grid index), or the points of sptr
+  const int* sptr;              // [ns + 1] source points of each shot in sx, or null: one per shot
   const int* sz;                // [ns] source depth index
   const float* gs;              // [2 ngs + 1] source window
   const float* gr;              // [2 ngr + 1] receiver window
@@ -121,9 +122,18 @@ void launch_pad_edge(const float2* in, float2* out, int M, int nz, int nx, int p
 void launch_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref, cudaStream_t st);
 // q (SSF split step, may be null), rc, and for the Born operators sc and the
 // dReflect pairs (null to skip) of every padded point
+// sp_refl: the slowness of the Reflect/dReflect coefficients when it differs
+// from sp (conformal maps scale sp by the Jacobian after Reflect is built);
+// null = sp
 void launch_point_tables(int M, int nz, int nxg, int nref, int ntaylor, float eps, const float2* sp,
-                         const float2* dp, const float2* sref, const signed char* ref, float2* q, float2* rc,
-                         float2* sc, float2* a0, float2* b0, float2* a1, float2* b1, cudaStream_t st);
+                         const float2* sp_refl, const float2* dp, const float2* sref, const signed char* ref,
+                         float2* q, float2* rc, float2* sc, float2* a0, float2* b0, float2* a1, float2* b1,
+                         cudaStream_t st);
+// conformal maps: out[i] = in[idx[i]] (0 where idx < 0); add < 0 overwrites,
+// 0/1 as the operators' add
+void launch_cmap_gather(const float2* in, const int* idx, float2* out, int n, int add, cudaStream_t st);
+// sp[k] *= js, *= jl[k] (jl may be null), twice, for k < n
+void launch_cmap_jacobian(float2* sp, int n, float js, const float* jl, cudaStream_t st);
 
 // ---- helpers
 void launch_pad_model(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st);

@@ -354,23 +354,26 @@ __device__ __forceinline__ float2 sc_iw(const DevCtx& c, float om, int mode) {
   return make_float2(0.f, mode == 0 ? -wdz : wdz);
 }
 
-// add gs[g] wavelet into the row of shot s at depth z (Injection.cpp:8-19)
+// add gs[g] wavelet into the row of shot s at depth z for every source
+// point of the shot (Injection.cpp:8-19)
 template <int E>
 __device__ __forceinline__ void w_inject_src(const WRow& w, float2 (&v)[E], int s, int f, int z) {
   const DevCtx& c = w.c;
   if (c.sz[s] != z) return;
   const float2 wv = c.wave[f];
-  for (int g = -c.ngs; g <= c.ngs; ++g) {
-    int x = c.sx[s] + g + c.pad;
-    if (x < 0 || x >= c.nxg) continue;
-    int n = x + w.tap;
-    if ((n & 31) != w.lane) continue;
-    const int jn = n >> 5;
-    const float2 add = c_scale(wv, c.gs[g + c.ngs]);
+  const int p0 = c.sptr ? c.sptr[s] : s, p1 = c.sptr ? c.sptr[s + 1] : s + 1;
+  for (int pt = p0; pt < p1; ++pt)
+    for (int g = -c.ngs; g <= c.ngs; ++g) {
+      int x = c.sx[pt] + g + c.pad;
+      if (x < 0 || x >= c.nxg) continue;
+      int n = x + w.tap;
+      if ((n & 31) != w.lane) continue;
+      const int jn = n >> 5;
+      const float2 add = c_scale(wv, c.gs[g + c.ngs]);
 #pragma unroll
-    for (int j = 0; j < E; ++j)
-      if (j == jn) v[j] = c_add(v[j], add);
-  }
+      for (int j = 0; j < E; ++j)
+        if (j == jn) v[j] = c_add(v[j], add);
+    }
 }
 
 // data[s][i][bin] += sum_g gr[g] v[rx_i + g] for receivers at depth z

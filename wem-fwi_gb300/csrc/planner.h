@@ -35,6 +35,9 @@ struct Geometry {
   std::vector<int> bin;      // wavelet/data bin of each frequency
   int nt_pad = 0, nbin = 0;
   std::vector<int> sx, sz, rx, rz;  // device grid indices (unpadded x)
+  // several source points per shot: shot s injects at sx[sptr[s] .. sptr[s+1])
+  // and depth sz[s]; empty: one point per shot, sx[s]
+  std::vector<int> sptr;
   std::vector<double> gs, gr;       // cos^2 spreading windows
   std::vector<cd> wave_at;          // wavelet spectrum at bin[f]
   int nfreq() const { return (int)freq.size(); }

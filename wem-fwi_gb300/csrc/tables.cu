@@ -64,8 +64,8 @@ __global__ void k_sref(const float2* sp, float2* sref, int M, int nz, int nxg, i
 // coefficients (Scatter.cpp:77-86, Scatter.h:36) and dReflect pairs
 // (dReflect.h:18-27, 40-47) of every padded point
 __global__ void k_point_tables(int M, int nz, int nxg, int nref, int nt, double eps, const float2* sp,
-                               const float2* dp, const float2* sref, const signed char* ref, float2* q,
-                               float2* rc, float2* sc, float2* a0, float2* b0, float2* a1, float2* b1) {
+                               const float2* spr, const float2* dp, const float2* sref, const signed char* ref,
+                               float2* q, float2* rc, float2* sc, float2* a0, float2* b0, float2* a1, float2* b1) {
   const size_t plane = (size_t)nz * nxg;
   const size_t total = (size_t)M * plane;
   const double coef[5] = {1., 1. / 2., 3. / 8., 5. / 16., 35. / 128.};
@@ -85,10 +85,19 @@ __global__ void k_point_tables(int M, int nz, int nxg, int nref, int nt, double 
     }
     cdd r = mk(0, 0), va0 = r, vb0 = r, va1 = r, vb1 = r;
     if (z >= 1) {
-      const cdd su = mk(sp[i - nxg]), du = mk(dp[i - nxg]);
-      const cdd u = mul(d, csqrt(su)), w = mul(du, csqrt(s));
-      r = dvd(sub(u, w), add(u, w));
+      const cdd du = mk(dp[i - nxg]);
+      {
+        // Reflect is built from spr, the slowness before any conformal-map
+        // Jacobian (born_prop.cpp:44-47); dReflect, built after the scaling
+        // from the same arrays (Born_refl.cpp:10-11), and the split step
+        // and Scatter see sp
+        const cdd sr = mk(spr[i]), sur = mk(spr[i - nxg]);
+        const cdd u = mul(d, csqrt(sur)), w = mul(du, csqrt(sr));
+        r = dvd(sub(u, w), add(u, w));
+      }
       if (sc) {
+        const cdd su = mk(sp[i - nxg]);
+        const cdd u = mul(d, csqrt(su)), w = mul(du, csqrt(s));
         cdd v = cpow(add(u, w), -2.0);
         cdd s1s2 = dvd(mul(du, d), v);
         cdd r1r2 = dvd(mul(mk(2, 0), mul(su, s)), v);
@@ -132,11 +141,55 @@ void launch_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nre
 }
 
 void launch_point_tables(int M, int nz, int nxg, int nref, int ntaylor, float eps, const float2* sp,
-                         const float2* dp, const float2* sref, const signed char* ref, float2* q, float2* rc,
-                         float2* sc, float2* a0, float2* b0, float2* a1, float2* b1, cudaStream_t st) {
+                         const float2* sp_refl, const float2* dp, const float2* sref, const signed char* ref,
+                         float2* q, float2* rc, float2* sc, float2* a0, float2* b0, float2* a1, float2* b1,
+                         cudaStream_t st) {
   size_t n = (size_t)M * nz * nxg;
-  k_point_tables<<<grid_of(n), 256, 0, st>>>(M, nz, nxg, nref, ntaylor + 1, (double)eps, sp, dp, sref, ref, q, rc,
-                                             sc, a0, b0, a1, b1);
+  k_point_tables<<<grid_of(n), 256, 0, st>>>(M, nz, nxg, nref, ntaylor + 1, (double)eps, sp, sp_refl ? sp_refl : sp,
+                                             dp, sref, ref, q, rc, sc, a0, b0, a1, b1);
+  note_launch();
+}
+
+// ---- conformal maps
+namespace {
+__global__ void k_cmap_gather(const float2* in, const int* idx, float2* out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int j = idx[i];
+  out[i] = j >= 0 ? in[j] : make_float2(0.f, 0.f);
+}
+__global__ void k_cmap_gather_add(const float2* in, const int* idx, float2* out, int n, int add) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int j = idx[i];
+  const float2 v = j >= 0 ? in[j] : make_float2(0.f, 0.f);
+  out[i] = add ? make_float2(out[i].x + v.x, out[i].y + v.y) : v;
+}
+// ConformalMap::scaleByJacobian twice on the padded slowness, by flat index
+__global__ void k_cmap_jacobian(float2* sp, int n, float js, const float* jl) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  float2 v = sp[k];
+  for (int rep = 0; rep < 2; ++rep) {
+    v.x = __fmul_rn(v.x, js);
+    v.y = __fmul_rn(v.y, js);
+    if (jl) {
+      v.x = __fmul_rn(v.x, jl[k]);
+      v.y = __fmul_rn(v.y, jl[k]);
+    }
+  }
+  sp[k] = v;
+}
+}  // namespace
+
+void launch_cmap_gather(const float2* in, const int* idx, float2* out, int n, int add, cudaStream_t st) {
+  if (add < 0) k_cmap_gather<<<(n + 255) / 256, 256, 0, st>>>(in, idx, out, n);
+  else k_cmap_gather_add<<<(n + 255) / 256, 256, 0, st>>>(in, idx, out, n, add);
+  note_launch();
+}
+
+void launch_cmap_jacobian(float2* sp, int n, float js, const float* jl, cudaStream_t st) {
+  k_cmap_jacobian<<<(n + 255) / 256, 256, 0, st>>>(sp, n, js, jl);
   note_launch();
 }
 

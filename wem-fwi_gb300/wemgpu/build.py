@@ -21,8 +21,13 @@ LIB = os.path.join(OUT_DIR, "libwemgpu.so")
 OBJ_DIR = os.path.join(OUT_DIR, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels.cu", "kernels_w.cu", "tables.cu", "noalloc.cu", "interp.cu", "api.cpp", "planner.cpp"] + [
+SOURCES = ["kernels.cu", "kernels_w.cu", "tables.cu", "noalloc.cu", "interp.cu", "api.cpp", "planner.cpp", "cmap.cpp"] + [
     f"kw_e{e}_{p}.cu" for e in (32, 24, 16, 12, 8) for p in ("adj", "wem", "fwd")]
+
+# host code whose float results must not depend on the machine: the
+# conformal maps turn float coordinates into grid indices, so no multiply-add
+# may be fused on one machine and not on another
+HOST_EXACT = {"cmap.cpp"}
 
 
 def _nvcc() -> str:
@@ -52,6 +57,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         cmd = [nvcc, *common, "-c", os.path.join(CSRC, src), "-o", obj]
         if src.endswith(".cu"):
             cmd[1:1] = [*ARCH, "-lineinfo", "-Xptxas", "-v"] if verbose else [*ARCH, "-lineinfo"]
+        if src in HOST_EXACT:
+            cmd[1:1] = ["-Xcompiler", "-ffp-contract=off"]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -10,6 +10,7 @@ the defaults the reference's ``getInt/getFloat`` calls use.
 from __future__ import annotations
 
 import ctypes
+import json
 from typing import Any, Mapping
 
 import numpy as np
@@ -44,6 +45,7 @@ class WemParams(ctypes.Structure):
         ("nfreq", ctypes.c_int),
         ("adjoint_mode", ctypes.c_int), ("refs_mode", ctypes.c_int), ("nbin", ctypes.c_int),
         ("phase_law", ctypes.c_int),
+        ("cmap", ctypes.c_int), ("eps_log", ctypes.c_float), ("cmap_angles", _fp),
     ]
 
     def __init__(self, *a, **kw):
@@ -57,7 +59,7 @@ class WemParams(ctypes.Structure):
         return c
 
     def as_dict(self) -> dict:
-        return {n: getattr(self, n) for n, _ in self._fields_ if not n.endswith(("_x", "_z"))}
+        return {n: getattr(self, n) for n, t in self._fields_ if t is not _fp}
 
 
 _DEFAULTS = dict(
@@ -67,6 +69,7 @@ _DEFAULTS = dict(
     prop="ssf", nref=1, tap=0, pad=0, tpad=0, ngs=0, ngr=0, ntaylor=1,
     eps=0.04, fmin=1.0, fmax=0.0, nfreq=0,
     adjoint_mode="compat", refs_mode="ascoded", nbin=0, phase_law="ispc",
+    cmap=0, eps_log=0.01,
 )
 
 
@@ -92,9 +95,9 @@ def make_params(par: Any, *, nx: int, nz: int, dx: float, dz: float,
     p.ox = float(given["ox"]) if "ox" in given else float(ox)
     p.oz = float(given["oz"]) if "oz" in given else float(oz)
     p.nt, p.dt, p.ot = int(nt), float(dt), float(ot)
-    for k in ("ns", "nr", "nref", "tap", "pad", "tpad", "ngs", "ngr", "ntaylor", "nfreq", "nbin"):
+    for k in ("ns", "nr", "nref", "tap", "pad", "tpad", "ngs", "ngr", "ntaylor", "nfreq", "nbin", "cmap"):
         setattr(p, k, int(m[k]))
-    for k in ("osx", "osz", "dsx", "dsz", "orx", "orz", "drx", "drz", "eps", "fmin", "fmax"):
+    for k in ("osx", "osz", "dsx", "dsz", "orx", "orz", "drx", "drz", "eps", "fmin", "fmax", "eps_log"):
         setattr(p, k, float(m[k]))
     prop = m["prop"]
     p.prop = WEM_PROP_PSPI if str(prop).lower() == "pspi" or prop == WEM_PROP_PSPI else WEM_PROP_SSF
@@ -104,7 +107,14 @@ def make_params(par: Any, *, nx: int, nz: int, dx: float, dz: float,
     p.refs_mode = WEM_REFS_NEAREST if str(rm).lower() == "nearest" or rm == WEM_REFS_NEAREST else WEM_REFS_ASCODED
     pl = m["phase_law"]
     p.phase_law = WEM_PHASE_EXACT_KZ if str(pl).lower() == "exact_kz" or pl == WEM_PHASE_EXACT_KZ else WEM_PHASE_ISPC
-    # irregular geometry: explicit coordinate lists replace the regular grid
+    # irregular geometry: explicit coordinate lists, or the JSON file named by
+    # "coord" (keys sx, sz, rx, rz; Device.h:65-85), replace the regular grid
+    if m.get("coord"):
+        with open(m["coord"]) as f:
+            coords = json.load(f)
+        for key in ("sx", "sz", "rx", "rz"):
+            if key in coords and key not in m:
+                m[key] = coords[key]
     for key, field, count in (("sx", "src_x", "ns"), ("sz", "src_z", "ns"),
                               ("rx", "rec_x", "nr"), ("rz", "rec_z", "nr")):
         if key in m and m[key] is not None:
@@ -115,4 +125,14 @@ def make_params(par: Any, *, nx: int, nz: int, dx: float, dz: float,
                 p.nr = int(arr.size)
             p._keep.append(arr)
             setattr(p, field, arr.ctypes.data_as(_fp))
+    # rotation angles of cmap = 2: a list, or the JSON file named by
+    # "cmap_angles" with key "a" (PropParam.h:119-129)
+    ang = m.get("cmap_angles")
+    if ang is not None:
+        if isinstance(ang, str):
+            with open(ang) as f:
+                ang = json.load(f)["a"]
+        arr = np.ascontiguousarray(np.asarray(ang, dtype=np.float32))
+        p._keep.append(arr)
+        p.cmap_angles = arr.ctypes.data_as(_fp)
     return p
