@@ -185,6 +185,32 @@ std::vector<float> host_floats(const void* p, size_t nfloat) {
   return h;
 }
 
+// FFT1_r over time (FFT1_r.cpp:74-96) restricted to the propagated bins
+// (consecutive, PropParam.h:75-78): unitary DFT matrices in double, rounded
+// once; the forward takes e^{-i a}, the inverse keeps Re(B e^{i a})
+struct DftMatrices {
+  std::vector<float> wf, wi;  // [nt][2F], [2F][nt]
+};
+
+DftMatrices dft_matrices(const Geometry& g, int nt) {
+  const int n = g.nt_pad, F = g.nfreq(), F2 = 2 * F;
+  DftMatrices m;
+  m.wf.resize((size_t)nt * F2);
+  m.wi.resize((size_t)F2 * nt);
+  const long double pi = 3.14159265358979323846264338327950288L;
+  const double sc = 1.0 / std::sqrt((double)n);
+  for (int k = 0; k < nt; ++k)
+    for (int f = 0; f < F; ++f) {
+      const long double a = 2 * pi * (long double)((long long)g.bin[f] * k % n) / n;
+      const float cs = (float)(std::cos(a) * sc), sn = (float)(std::sin(a) * sc);
+      m.wf[(size_t)k * F2 + 2 * f] = cs;
+      m.wf[(size_t)k * F2 + 2 * f + 1] = -sn;
+      m.wi[(size_t)(2 * f) * nt + k] = cs;
+      m.wi[(size_t)(2 * f + 1) * nt + k] = -sn;
+    }
+  return m;
+}
+
 class Engine {
  public:
   // kind: 0 BornFull / WEM, 1 BornRefl, 2 BornTomo (propagator/src/ext_born_refl.cpp,
@@ -208,6 +234,8 @@ class Engine {
     int dev = 0;
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     if (!maps.empty()) {
+      // the shots share the time <-> frequency matrices
+      dft_ = std::make_shared<const DftMatrices>(dft_matrices(geo_, p.nt));
       for (int s = 0; s < geo_.ns; ++s) {
         const ShotMap& m = maps[s];
         wem_params ps = p;
@@ -224,7 +252,7 @@ class Engine {
         gs.sptr = {0, (int)m.src_x.size()};
         gs.rx = m.rec_x;
         gs.rz = m.rec_z;
-        shots_.push_back(std::unique_ptr<Engine>(new Engine(ps, gs, m, born)));
+        shots_.push_back(std::unique_ptr<Engine>(new Engine(ps, gs, m, born, dft_)));
       }
       return;
     }
@@ -544,8 +572,9 @@ class Engine {
  private:
   // one shot of a conformal-map operator: its mapped grid (p.dx, p.dz) and
   // devices (g) and the gather tables of its map
-  Engine(const wem_params& p, const Geometry& g, const ShotMap& m, bool born)
-      : p_(p), ext_(false), born_(born), kind_(0) {
+  Engine(const wem_params& p, const Geometry& g, const ShotMap& m, bool born,
+         std::shared_ptr<const DftMatrices> dft)
+      : p_(p), ext_(false), born_(born), kind_(0), dft_(std::move(dft)) {
     geo_ = g;
     F_ = geo_.nfreq();
     M_ = 1;
@@ -580,6 +609,7 @@ class Engine {
   wem_params p_;
   bool ext_, born_;
   int kind_ = 0;
+  std::shared_ptr<const DftMatrices> dft_;
   int M_img_ = 1;  // image slices: per frequency for the extended operators and BornRefl
   bool have_bg_ = false;
   Geometry geo_;
@@ -648,26 +678,9 @@ class Engine {
     ctx_.rptr = upload(rptr_, rptr);
     ctx_.rid = upload(rid_, ord);
     ctx_.rxs = upload(rxs_, rxs);
-    // FFT1_r over time (FFT1_r.cpp:74-96) restricted to the propagated bins
-    // (consecutive, PropParam.h:75-78): unitary DFT matrices in double,
-    // rounded once; the forward takes e^{-i a}, the inverse keeps Re(B e^{i a})
-    {
-      const int n = g.nt_pad, nt = p_.nt, F2 = 2 * F_;
-      std::vector<float> wf((size_t)nt * F2), wi((size_t)F2 * nt);
-      const long double pi = 3.14159265358979323846264338327950288L;
-      const double sc = 1.0 / std::sqrt((double)n);
-      for (int k = 0; k < nt; ++k)
-        for (int f = 0; f < F_; ++f) {
-          const long double a = 2 * pi * (long double)((long long)g.bin[f] * k % n) / n;
-          const float cs = (float)(std::cos(a) * sc), sn = (float)(std::sin(a) * sc);
-          wf[(size_t)k * F2 + 2 * f] = cs;
-          wf[(size_t)k * F2 + 2 * f + 1] = -sn;
-          wi[(size_t)(2 * f) * nt + k] = cs;
-          wi[(size_t)(2 * f + 1) * nt + k] = -sn;
-        }
-      upload(wfwd_, wf);
-      upload(winv_, wi);
-    }
+    if (!dft_) dft_ = std::make_shared<const DftMatrices>(dft_matrices(g, p_.nt));
+    upload(wfwd_, dft_->wf);
+    upload(winv_, dft_->wi);
     bins_ = binsbuf_.as<float2>((size_t)g.ns * g.nr * F_);
   }
 
