@@ -64,10 +64,16 @@ class Clocks:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # the timed region starts once the sampler is running: wait for
+            # its first line and keep only what follows
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.lines.clear()
         except Exception:
             self.proc = None
         return self
@@ -326,9 +332,10 @@ def run_gpu(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
-def cpu_sample(cfg, seconds=15.0, nthreads=0):
+def cpu_sample(cfg, seconds=15.0, nthreads=0, nshots=0):
     """The CPU restatement (oracle, fp32) on a bounded sample of the same
-    workload: the first shots and frequencies, all depths."""
+    workload: the first shots (``nshots``, or as many as take about
+    ``seconds``), every frequency, all depths."""
     from oracle import oracle as O
     from wemgpu import synthetic as S
     O.build()
@@ -336,7 +343,7 @@ def cpu_sample(cfg, seconds=15.0, nthreads=0):
     # grow the sample (shots, each with the workload's full frequency axis and
     # all depths) until it takes about `seconds`
     p_full = S.params_of(cfg)
-    nsk = 1
+    nsk = nshots or 1
     while True:
         par = dict(cfg["par"], ns=nsk)
         c = dict(cfg, par=par)
@@ -347,7 +354,7 @@ def cpu_sample(cfg, seconds=15.0, nthreads=0):
         O.born_adjoint(p, cfg["wavelet"], cfg["slow"], cfg["rho"], syn, kind=0, prec=32, nthreads=nthreads,
                        fchunks=max(1, nthreads))
         dt = time.perf_counter() - t0
-        if dt > 0.5 * seconds or nsk >= p_full.ns:
+        if nshots or dt > 0.5 * seconds or nsk >= p_full.ns:
             break
         nsk = min(p_full.ns, max(nsk + 1, int(nsk * seconds / max(dt, 1e-3))))
     rate = row_steps(p, nf) / dt
@@ -361,9 +368,14 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     cfg = workload(args.small)
+    # the sample is sized once, so that all warm-up and timed steps together
+    # take about two minutes (1-10 s each), then every step repeats it
+    per_step = min(10.0, max(1.0, 120.0 / (args.warmup + args.steps)))
+    first = cpu_sample(cfg, seconds=per_step)
+    nshots = int(first["sample"].split()[0])
     res = []
     for i in range(args.warmup + args.steps):
-        r = cpu_sample(cfg, seconds=10.0)
+        r = cpu_sample(cfg, nshots=nshots) if i else first
         if i >= args.warmup:
             res.append(r["value"])
     v = float(np.median(res))
@@ -386,7 +398,7 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--small", action="store_true", help="reduced case (profiling captures)")
