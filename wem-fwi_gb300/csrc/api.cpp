@@ -252,7 +252,7 @@ class Engine {
         gs.sptr = {0, (int)m.src_x.size()};
         gs.rx = m.rec_x;
         gs.rz = m.rec_z;
-        shots_.push_back(std::unique_ptr<Engine>(new Engine(ps, gs, m, born, dft_)));
+        shots_.push_back(std::unique_ptr<Engine>(new Engine(ps, gs, m, born, dft_, ws_)));
       }
       return;
     }
@@ -312,7 +312,7 @@ class Engine {
     const bool wp = warp_path();
     int G = wp ? warp_G(0) : pick_G([&](int g) { return smem_wem(ctx_, g); });
     for_chunks(G, plane * 8, [&](const Group* gd, int ng, int rows) {
-      float2* A = store1_.as<float2>((size_t)rows * plane);
+      float2* A = ws_->store1.as<float2>((size_t)rows * plane);
       if (wp) timed("k_wem", [&] { launch_pass_warp(0, ctx_, gd, ng, nullptr, nullptr, A, nullptr, nullptr, bins_, nullptr, nullptr, 0, 0); });
       else timed("k_wem", [&] { launch_wem(ctx_, gd, ng, G, A, bins_, 0); });
       cuda_check(cudaGetLastError(), "k_wem launch");
@@ -395,8 +395,8 @@ class Engine {
     const bool wp = warp_path();
     int G = wp ? warp_G(1) : pick_G([&](int g) { return smem_born_fwd(ctx_, g); });
     for_chunks(G, 2 * plane * 8, [&](const Group* gd, int ng, int rows) {
-      float2* A = store1_.as<float2>((size_t)rows * plane);
-      float2* B = store2_.as<float2>((size_t)rows * plane);
+      float2* A = ws_->store1.as<float2>((size_t)rows * plane);
+      float2* B = ws_->store2.as<float2>((size_t)rows * plane);
       if (wp) timed("k_born_fwd", [&] { launch_pass_warp(1, ctx_, gd, ng, dm0, drm, A, B, nullptr, bins_, nullptr, nullptr, 0, 0); });
       else timed("k_born_fwd", [&] { launch_born_fwd(ctx_, gd, ng, G, dm0, drm, A, B, bins_, 0); });
       cuda_check(cudaGetLastError(), "k_born_fwd launch");
@@ -519,11 +519,11 @@ class Engine {
     const int nfield = reuse ? 3 : 2;
     // per row: two stored fields (three with spectral reuse); per group: two partial images
     for_chunks(G, nfield * plane * 8 + (2 * plane * 8 + G - 1) / G, [&](const Group* gd, int ng, int rows) {
-      float2* BG = store1_.as<float2>((size_t)rows * plane);
-      float2* T = store2_.as<float2>((size_t)rows * plane);
-      float2* SG = reuse ? store3_.as<float2>((size_t)rows * plane) : nullptr;
-      float2* pr = part1_.as<float2>((size_t)ng * plane);
-      float2* ps = part2_.as<float2>((size_t)ng * plane);
+      float2* BG = ws_->store1.as<float2>((size_t)rows * plane);
+      float2* T = ws_->store2.as<float2>((size_t)rows * plane);
+      float2* SG = reuse ? ws_->store3.as<float2>((size_t)rows * plane) : nullptr;
+      float2* pr = ws_->part1.as<float2>((size_t)ng * plane);
+      float2* ps = ws_->part2.as<float2>((size_t)ng * plane);
       if (wp) timed("k_born_adj", [&] { launch_pass_warp(2, ctx_, gd, ng, nullptr, nullptr, BG, T, SG, bins_, pr, ps, compat, 0); });
       else timed("k_born_adj", [&] { launch_born_adj(ctx_, gd, ng, G, BG, T, bins_, pr, ps, compat, 0); });
       cuda_check(cudaGetLastError(), "k_born_adj launch");
@@ -570,11 +570,21 @@ class Engine {
   }
 
  private:
+  // the large buffers: stored fields, per-group partial images and the
+  // per-frequency phase / split-step tables.  The shots of a conformal-map
+  // operator run one after another and rebuild their tables before every
+  // pass, so they share one set.
+  struct Scratch {
+    Buf store1, store2, store3, part1, part2, ph, fac;
+  };
+  std::shared_ptr<Scratch> ws_ = std::make_shared<Scratch>();
+
   // one shot of a conformal-map operator: its mapped grid (p.dx, p.dz) and
   // devices (g) and the gather tables of its map
   Engine(const wem_params& p, const Geometry& g, const ShotMap& m, bool born,
-         std::shared_ptr<const DftMatrices> dft)
+         std::shared_ptr<const DftMatrices> dft, std::shared_ptr<Scratch> ws)
       : p_(p), ext_(false), born_(born), kind_(0), dft_(std::move(dft)) {
+    ws_ = std::move(ws);
     geo_ = g;
     F_ = geo_.nfreq();
     M_ = 1;
@@ -618,11 +628,11 @@ class Engine {
   // static tables
   Buf tw_, kx_, taper_, omega_, bin_, wave_, sx_, sz_, gs_, gr_, rptr_, rid_, rxs_, wfwd_, winv_;
   // background tables
-  Buf sref_, ref_, q_, sc_, rc_, a0b_, b0b_, a1b_, b1b_, ph_, fac_, sp_, dp_;
+  Buf sref_, ref_, q_, sc_, rc_, a0b_, b0b_, a1b_, b1b_, sp_, dp_;
   float2 *a0_ = nullptr, *b0_ = nullptr, *a1_ = nullptr, *b1_ = nullptr;
   // workspaces
   std::vector<Group> chunk_;  // host copy of the groups of the current launch
-  Buf rcf_, binsbuf_, groups_, store1_, store2_, store3_, dsyn_, lossbuf_, part1_, part2_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
+  Buf rcf_, binsbuf_, groups_, dsyn_, lossbuf_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
   float2* bins_ = nullptr;
 
   void build_static() {
@@ -764,11 +774,11 @@ class Engine {
                         0);
     ctx_.rc = rc;
     ctx_.sc = sc;
-    float2* ph = ph_.as<float2>((size_t)F_ * nz * nref * geo_.N);
+    float2* ph = ws_->ph.as<float2>((size_t)F_ * nz * nref * geo_.N);
     launch_phase_tables(ctx_, dsref, p_.eps, ph, 0);
     ctx_.ph = ph;
     if (ssf) {
-      float2* fac = fac_.as<float2>((size_t)F_ * plane);
+      float2* fac = ws_->fac.as<float2>((size_t)F_ * plane);
       launch_fac_tables(ctx_, q, fac, 0);
       ctx_.fac = fac;
     } else {
