@@ -290,6 +290,43 @@ int wemop_scatter(wemop_handle* h, int iz, float freq, int adj,
  * Replaces RefSampler::getRefSlow / getRefLoc (RefSampler.h:19-20). */
 int wemop_refsampler(wemop_handle* h, void* sref, int* refidx);
 
+/* SplitStep of one depth on the listed points (propagator/src/SplitStep.cpp:5-29;
+ * py_wem_ops.cpp SplitStep, setFreq/setLocation/setSlow/setDepth): point x
+ * of each row gets m[x] exp(-i w dz (s[iz][x] - sref) / sqrt(sref)) (adjoint
+ * exp(+i w dz conj(...))), s the handle's slowness^2, dz its p.dz.  As in the
+ * reference the listed points are assigned, not accumulated; the other
+ * points are zero without add and untouched with it.  in, out [nrow][nxg]. */
+int wemop_splitstep(wemop_handle* h, int iz, float freq, float sref_re, float sref_im,
+                    const int* loc, int nloc, int adj, const void* in, void* out,
+                    int nrow, int add);
+/* LinDown of one field [nz][nxg] with the background wavefield bg [nz][nxg]
+ * (LinOneWay.cpp:33-85; py_wem_ops.cpp LinDown): per depth bg m, the Taylor
+ * scatter (p.ntaylor; adjoint as p.adjoint_mode) and the depth step (p.prop),
+ * added into the next depth; the adjoint runs upwards.  As the reference,
+ * the forward clears the first output row whatever add says, and so does the
+ * compat adjoint with the last row (LinOneWay.cpp:64-65); the exact adjoint
+ * is the transpose.  in and out must differ. */
+int wemop_lindown(wemop_handle* h, const void* bg, float freq, int adj, const void* in,
+                  void* out, int add);
+
+/* Element-wise operators of py_wem_ops (no handle). */
+/* IC (ic.cpp:5-45): out (+)= bg in, adjoint conj(bg) in, over n values */
+int wem_ic(const void* bg, int n, int adj, const void* in, void* out, int add);
+/* Phshift (Phshift_cmplx.cpp:8-113, phase_shift.ispc:2-32): rows of n
+ * wavenumber samples (the k grid of a row of n points at spacing dx) times
+ * the phase-shift factor of slowness s = s_re + i s_im at frequency freq over
+ * dz, with p->eps and p->phase_law; the adjoint takes the conjugate factor. */
+int wem_phshift(const wem_params* p, int n, float dx, float dz, float freq, float s_re,
+                float s_im, int adj, const void* in, void* out, int nrow, int add);
+/* Reflect (Reflect.h:12-48) of the grid (slow2, rho) [nz][nx]: out = r in,
+ * adjoint conj(r) in; assigned, as the reference's (no add). */
+int wem_reflect(const void* slow2, const void* rho, int nx, int nz, int adj, const void* in,
+                void* out);
+/* dReflect (dReflect.h:11-84) at (slow2, rho) [nz][nx]: forward data (+)=
+ * dR(dslow2, drho), adjoint (dslow2, drho) (+)= dR^H data. */
+int wem_dreflect(const void* slow2, const void* rho, int nx, int nz, int adj, void* dslow2,
+                 void* drho, void* data, int add);
+
 /* One SSF/PSPI depth step that allocates no memory (no counterpart in the
  * reference).  It exists for callers that cannot call cudaMalloc while they
  * run: code that owns all device memory up front (a fixed arena or memory

@@ -218,3 +218,56 @@ def refsampler(p, slow_padded):
     idx = np.zeros((p.nz, nxg), np.int32)
     _call("oracle_refsampler", ctypes.byref(p), _ptr(_c64(slow_padded)), nxg, _ptr(sref), _ptr(idx))
     return sref, idx
+
+
+def phshift(p, n, dx, dz, freq, s, adj, x, out=None, add=False, prec=32):
+    """Phshift of rows of n wavenumber samples (Phshift_cmplx.cpp:47-113)."""
+    x = _c64(x)
+    out = np.zeros_like(x) if out is None else out
+    _call("oracle_phshift", ctypes.byref(p), int(n), ctypes.c_float(dx), ctypes.c_float(dz), ctypes.c_float(freq),
+          ctypes.c_float(np.real(s)), ctypes.c_float(np.imag(s)), int(adj), _ptr(x), _ptr(out), x.size // n,
+          int(add), prec)
+    return out
+
+
+def splitstep(p, slow, iz, freq, sref, loc, adj, x, out=None, add=False, prec=32):
+    """SplitStep of depth iz on the points loc (SplitStep.cpp:5-29)."""
+    x = _c64(x)
+    nxg = slow.shape[-1]
+    out = np.zeros_like(x) if out is None else out
+    loc = np.ascontiguousarray(loc, dtype=np.int32)
+    _call("oracle_splitstep", ctypes.byref(p), _ptr(_c64(slow)), nxg, int(iz), ctypes.c_float(freq),
+          ctypes.c_float(np.real(sref)), ctypes.c_float(np.imag(sref)), _ptr(loc), loc.size, int(adj), _ptr(x),
+          _ptr(out), x.size // nxg, int(add), prec)
+    return out
+
+
+def lindown(p, slow, bg, freq, adj, x, out=None, add=False, prec=32):
+    """LinDown of one field (LinOneWay.cpp:33-85)."""
+    x = _c64(x)
+    nxg = slow.shape[-1]
+    out = np.zeros_like(x) if out is None else out
+    _call("oracle_lindown", ctypes.byref(p), _ptr(_c64(slow)), nxg, _ptr(_c64(bg)), ctypes.c_float(freq), int(adj),
+          _ptr(x), _ptr(out), int(add), prec)
+    return out
+
+
+def reflect(slow, rho, adj, x):
+    """Reflect (Reflect.h:12-48), in double."""
+    x = _c64(x)
+    out = np.zeros_like(x)
+    nz, nx = slow.shape
+    _call("oracle_reflect", _ptr(_c64(slow)), _ptr(_c64(rho)), nx, nz, int(adj), _ptr(x), _ptr(out))
+    return out
+
+
+def dreflect(slow, rho, adj, m0=None, m1=None, data=None, add=False):
+    """dReflect (dReflect.h:11-84), in double: forward returns data, adjoint
+    (m0, m1)."""
+    nz, nx = slow.shape
+    m0 = np.zeros(slow.shape, np.complex64) if m0 is None else _c64(m0).copy()
+    m1 = np.zeros(slow.shape, np.complex64) if m1 is None else _c64(m1).copy()
+    data = np.zeros(slow.shape, np.complex64) if data is None else _c64(data).copy()
+    _call("oracle_dreflect", _ptr(_c64(slow)), _ptr(_c64(rho)), nx, nz, int(adj), _ptr(m0), _ptr(m1), _ptr(data),
+          int(add))
+    return (m0, m1) if adj else data

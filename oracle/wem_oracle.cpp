@@ -1068,6 +1068,131 @@ int oracle_scatter(const wem_params* p, const float* slow, int nxg, int iz, floa
   });
 }
 
+extern "C++" {
+// Phshift::forward/adjoint (Phshift_cmplx.cpp:47-113): rows of n k samples,
+// k grid of a row of n points at spacing dx (Phshift_cmplx.cpp:8-24)
+template <class R>
+static void phshift_rows(const wem_params& p, int n, float dx, float dz, float freq, float sre, float sim, int adj,
+                         const float* in, float* out, int nrow, int add) {
+  std::vector<R> k(n, R(0));
+  const R dk = (R)(2 * kPi / ((double)dx * (n - 1)));
+  for (int ik = 0; ik < n / 2; ++ik) k[ik] = ik * dk;
+  for (int ik = 1; ik < n / 2; ++ik) k[n - ik] = -k[ik];
+  const R w = Core<R>::omega(freq);
+  const C<R> s((R)sre, (R)sim);
+  for (int r = 0; r < nrow; ++r)
+    for (int ik = 0; ik < n; ++ik) {
+      C<R> f = ps_factor(w, k[ik], (R)dz, s, (R)p.eps, p.phase_law);
+      if (adj) f = std::conj(f);
+      const size_t i = (size_t)r * n + ik;
+      C<R> v = f * C<R>((R)in[2 * i], (R)in[2 * i + 1]);
+      if (add) v += C<R>((R)out[2 * i], (R)out[2 * i + 1]);
+      out[2 * i] = (float)v.real();
+      out[2 * i + 1] = (float)v.imag();
+    }
+}
+
+// SplitStep::forward/adjoint (SplitStep.cpp:5-29) at depth iz of the grid
+template <class R>
+static void splitstep_rows(const wem_params& p, const float* slow, int nxg, int iz, float freq, float sre,
+                           float sim, const int* loc, int nloc, int adj, const float* in, float* out, int nrow,
+                           int add) {
+  const R w = Core<R>::omega(freq);
+  const C<R> sref((R)sre, (R)sim), I(0, 1);
+  for (int r = 0; r < nrow; ++r) {
+    float* o = out + 2 * (size_t)r * nxg;
+    const float* a = in + 2 * (size_t)r * nxg;
+    std::vector<float> src(a, a + 2 * (size_t)nxg);  // in may alias out
+    if (!add) std::fill(o, o + 2 * (size_t)nxg, 0.f);
+    for (int i = 0; i < nloc; ++i) {
+      const int x = loc[i];
+      const C<R> st((R)slow[2 * ((size_t)iz * nxg + x)], (R)slow[2 * ((size_t)iz * nxg + x) + 1]);
+      const C<R> u = (st - sref) / std::sqrt(sref);
+      const C<R> corr = adj ? I * w * (R)p.dz * std::conj(u) : -I * w * (R)p.dz * u;
+      const C<R> v = C<R>((R)src[2 * x], (R)src[2 * x + 1]) * std::exp(corr);
+      o[2 * x] = (float)v.real();
+      o[2 * x + 1] = (float)v.imag();
+    }
+  }
+}
+
+template <class R>
+static void lindown_field(const wem_params& p, const float* slow, int nxg, const float* bg, float freq, int adj,
+                          const float* in, float* out, int add) {
+  RowOp<R> op(p, slow, nxg);
+  Work<R> wk(op.core.N, nxg);
+  const size_t n = (size_t)nxg * p.nz;
+  std::vector<C<R>> b = load<R>(bg, n), x = load<R>(in, n), y = load<R>(out, n);
+  const R w = Core<R>::omega(freq);
+  if (!adj) lindown_fwd(op.core, w, b.data(), x.data(), y.data(), add != 0, wk);
+  else lindown_adj(op.core, w, b.data(), y.data(), x.data(), add != 0, p.adjoint_mode == WEM_ADJ_EXACT, wk);
+  store(out, y.data(), n, false);
+}
+}
+
+int oracle_phshift(const wem_params* p, int n, float dx, float dz, float freq, float sre, float sim, int adj,
+                   const float* in, float* out, int nrow, int add, int prec) {
+  return run_guarded([&] {
+    check(n >= 2 && dx > 0, "bad row");
+    if (prec == 64) phshift_rows<double>(*p, n, dx, dz, freq, sre, sim, adj, in, out, nrow, add);
+    else phshift_rows<float>(*p, n, dx, dz, freq, sre, sim, adj, in, out, nrow, add);
+  });
+}
+
+int oracle_splitstep(const wem_params* p, const float* slow, int nxg, int iz, float freq, float sre, float sim,
+                     const int* loc, int nloc, int adj, const float* in, float* out, int nrow, int add, int prec) {
+  return run_guarded([&] {
+    check(iz >= 0 && iz < p->nz, "depth index out of range");
+    for (int i = 0; i < nloc; ++i) check(loc[i] >= 0 && loc[i] < nxg, "location out of the row");
+    if (prec == 64) splitstep_rows<double>(*p, slow, nxg, iz, freq, sre, sim, loc, nloc, adj, in, out, nrow, add);
+    else splitstep_rows<float>(*p, slow, nxg, iz, freq, sre, sim, loc, nloc, adj, in, out, nrow, add);
+  });
+}
+
+int oracle_lindown(const wem_params* p, const float* slow, int nxg, const float* bg, float freq, int adj,
+                   const float* in, float* out, int add, int prec) {
+  return run_guarded([&] {
+    if (prec == 64) lindown_field<double>(*p, slow, nxg, bg, freq, adj, in, out, add);
+    else lindown_field<float>(*p, slow, nxg, bg, freq, adj, in, out, add);
+  });
+}
+
+// Reflect (Reflect.h:12-48): out = r in / conj(r) in
+int oracle_reflect(const float* slow2, const float* rho, int nx, int nz, int adj, const float* in, float* out) {
+  return run_guarded([&] {
+    const size_t n = (size_t)nx * nz;
+    std::vector<C<double>> s = load<double>(slow2, n), d = load<double>(rho, n), x = load<double>(in, n);
+    std::vector<C<double>> r = reflect_coefs(s.data(), d.data(), nx, nz);
+    for (size_t i = 0; i < n; ++i) x[i] = (adj ? std::conj(r[i]) : r[i]) * x[i];
+    store(out, x.data(), n, false);
+  });
+}
+
+// dReflect (dReflect.h:11-84): data (+)= dR(m0, m1) or (m0, m1) (+)= dR^H data
+int oracle_dreflect(const float* slow2, const float* rho, int nx, int nz, int adj, float* m0, float* m1, float* data,
+                    int add) {
+  return run_guarded([&] {
+    const size_t n = (size_t)nx * nz;
+    std::vector<C<double>> s = load<double>(slow2, n), d = load<double>(rho, n);
+    DRefl<double> dr(s.data(), d.data(), nx, nz);
+    if (!adj) {
+      std::vector<C<double>> a = load<double>(m0, n), b = load<double>(m1, n), y(n, C<double>(0));
+      if (add) y = load<double>(data, n);
+      dr.fwd(a.data(), b.data(), y.data());
+      store(data, y.data(), n, false);
+    } else {
+      std::vector<C<double>> y = load<double>(data, n), a(n, C<double>(0)), b(n, C<double>(0));
+      if (add) {
+        a = load<double>(m0, n);
+        b = load<double>(m1, n);
+      }
+      dr.adj(a.data(), b.data(), y.data());
+      store(m0, a.data(), n, false);
+      store(m1, b.data(), n, false);
+    }
+  });
+}
+
 int oracle_refsampler(const wem_params* p, const float* slow, int nxg, float* sref, int* refidx) {
   return run_guarded([&] {
     std::vector<C<float>> s = load<float>(slow, (size_t)nxg * p->nz);

@@ -1007,6 +1007,9 @@ class RowOps {
     c_.tw = upload(tw_, to_f2(twiddles(N_)));
     c_.kx = upload(kx_, kf);
     c_.taperN = upload(taper_, tpf);
+    std::vector<float2> sf(sp.size());
+    for (size_t i = 0; i < sp.size(); ++i) sf[i] = make_float2(hs[2 * i], hs[2 * i + 1]);
+    slow_d_ = upload(slow_, sf);
     c_.ref = upload(ref_, t_.ref);
     c_.sc = upload(sc_, to_f2(t_.sc));
     c_.rc = upload(rc_, to_f2(t_.rc));
@@ -1054,12 +1057,58 @@ class RowOps {
     so.finish(out);
   }
 
+  // LinDown (LinOneWay.cpp:33-85) of one field [nz][nxg]: per depth the
+  // imaging condition with the background row, the Taylor scatter and the
+  // depth step, added into the next row; the adjoint runs the transposed
+  // chain upwards.  As in the reference, the forward clears the first output
+  // row whatever add says, and the compat adjoint the last one (the exact
+  // adjoint, the transpose, leaves it).
+  void lindown(const void* bg, float freq, int adj, const void* in, void* out, int add) {
+    require(bg && in && out, "NULL argument");
+    require(in != out, "lindown needs distinct model and data");
+    set_freq(freq);
+    const int nz = p_.nz, nx = nxg_;
+    const size_t plane = (size_t)nz * nx;
+    Staged sb, si, so;
+    sb.in(bg, plane * 8);
+    si.in(in, plane * 8);
+    so.out(out, plane * 8, add != 0);
+    const float2* b = (const float2*)sb.dev;
+    const float2* x = (const float2*)si.dev;
+    float2* o = (float2*)so.dev;
+    float2* t = row_.as<float2>(2 * (size_t)nx);
+    float2* u = t + nx;
+    const int G = this->G();
+    const int exact = p_.adjoint_mode == WEM_ADJ_EXACT ? 1 : 0;
+    if (!add) cuda_check(cudaMemsetAsync(o, 0, plane * 8, 0), "memset");
+    if (!adj) {
+      cuda_check(cudaMemsetAsync(o, 0, (size_t)nx * 8, 0), "memset");
+      for (int iz = 0; iz < nz - 1; ++iz) {
+        launch_diag_rows(x + (size_t)iz * nx, b + (size_t)iz * nx, t, nx, 1, 0, 0, 0);
+        launch_scatter(c_, 0, iz, 0, exact, t, u, 1, 0, G, 0);
+        launch_onestep(c_, 0, iz, 0, u, t, 1, 0, G, 0);
+        launch_scale_add(o + (size_t)(iz + 1) * nx, t, nx, 0);
+      }
+    } else {
+      if (!exact) cuda_check(cudaMemsetAsync(o + (size_t)(nz - 1) * nx, 0, (size_t)nx * 8, 0), "memset");
+      for (int iz = nz - 1; iz > 0; --iz) {
+        launch_onestep(c_, 0, iz - 1, 1, x + (size_t)iz * nx, t, 1, 0, G, 0);
+        launch_scatter(c_, 0, iz - 1, 1, exact, t, u, 1, 0, G, 0);
+        launch_diag_rows(u, b + (size_t)(iz - 1) * nx, t, nx, 1, 1, 0, 0);
+        launch_scale_add(o + (size_t)(iz - 1) * nx, t, nx, 0);
+      }
+    }
+    cuda_check(cudaGetLastError(), "lindown kernels");
+    cuda_check(cudaStreamSynchronize(0), "lindown");
+    so.finish(out);
+  }
+
   wem_params p_;
   int nxg_, N_ = 0;
   SliceTables t_;
   DevCtx c_{};
-  Buf tw_, kx_, taper_, ref_, sc_, rc_, sref_, q_, omega_, ph_, fac_;
-  float2 *sref_d_ = nullptr, *q_d_ = nullptr;
+  Buf tw_, kx_, taper_, ref_, sc_, rc_, sref_, q_, omega_, ph_, fac_, slow_, row_;
+  float2 *sref_d_ = nullptr, *q_d_ = nullptr, *slow_d_ = nullptr;
   float freq_ = 0;
   bool have_freq_ = false;
 };
@@ -1357,6 +1406,168 @@ int wemop_refsampler(wemop_handle* h, void* sref, int* refidx) {
       s[2 * i + 1] = (float)R.t_.sref[i].imag();
     }
     for (size_t i = 0; i < R.t_.ref.size(); ++i) refidx[i] = R.t_.ref[i];
+  });
+}
+
+int wemop_splitstep(wemop_handle* h, int iz, float freq, float sref_re, float sref_im, const int* loc, int nloc,
+                    int adj, const void* in, void* out, int nrow, int add) {
+  return guard([&] {
+    require(h && in && out && (loc || nloc == 0), "NULL argument");
+    RowOps& R = *h->r;
+    require(iz >= 0 && iz < R.p_.nz, "depth index out of range");
+    require(nloc >= 0 && nrow >= 0, "negative count");
+    require(!(sref_re == 0.f && sref_im == 0.f), "reference slowness is zero");
+    std::vector<int> hl(loc, loc + nloc);
+    for (int x : hl) require(x >= 0 && x < R.nxg_, "split-step location out of the row");
+    Buf lb;
+    const int* dl = upload(lb, hl);
+    const size_t per = R.nxg_;
+    const bool alias = in == out;
+    Staged si, so;
+    // points off the list keep the output's contents (zero without add)
+    so.out(out, per * nrow * 8, add != 0 || alias);
+    if (alias) si.dev = so.dev; else si.in(in, per * nrow * 8);
+    if (!add) cuda_check(cudaMemsetAsync(so.dev, 0, per * nrow * 8, 0), "memset");
+    const float w = (float)(2 * 3.14159265358979323846 * (double)freq);
+    launch_splitstep(R.slow_d_ + (size_t)iz * R.nxg_, dl, nloc, R.nxg_, nrow, (double)(w * R.p_.dz), sref_re,
+                     sref_im, adj, (const float2*)si.dev, (float2*)so.dev, 0);
+    cuda_check(cudaGetLastError(), "splitstep kernel");
+    cuda_check(cudaStreamSynchronize(0), "splitstep");
+    so.finish(out);
+  });
+}
+
+int wemop_lindown(wemop_handle* h, const void* bg, float freq, int adj, const void* in, void* out, int add) {
+  return guard([&] {
+    require(h != nullptr, "NULL handle");
+    h->r->lindown(bg, freq, adj, in, out, add);
+  });
+}
+
+int wem_ic(const void* bg, int n, int adj, const void* in, void* out, int add) {
+  return guard([&] {
+    require(bg && in && out && n >= 0, "bad arguments");
+    Staged sb, si, so;
+    sb.in(bg, (size_t)n * 8);
+    so.out(out, (size_t)n * 8, add != 0 || in == out);
+    if (in == out) si.dev = so.dev; else si.in(in, (size_t)n * 8);
+    launch_diag_rows((const float2*)si.dev, (const float2*)sb.dev, (float2*)so.dev, n, 1, adj ? 1 : 0, add, 0);
+    cuda_check(cudaGetLastError(), "ic kernel");
+    cuda_check(cudaStreamSynchronize(0), "ic");
+    so.finish(out);
+  });
+}
+
+int wem_phshift(const wem_params* p, int n, float dx, float dz, float freq, float s_re, float s_im, int adj,
+                const void* in, void* out, int nrow, int add) {
+  return guard([&] {
+    require(p && in && out, "NULL argument");
+    require(n >= 2 && nrow >= 0 && dx > 0, "bad row length or spacing");
+    require(p->phase_law == WEM_PHASE_ISPC || p->phase_law == WEM_PHASE_EXACT_KZ, "phase_law must be 0 or 1");
+    // the factor of every k sample from the depth step's phase-table kernel
+    // on a one-row table, then applied to the rows
+    Buf kb, ob, sb, fb;
+    std::vector<double> k = k_grid(n, dx);
+    DevCtx c{};
+    c.N = n;
+    c.nz = 1;
+    c.nref = 1;
+    c.nfreq = 1;
+    c.dz = dz;
+    c.phase_law = p->phase_law;
+    c.kx = upload(kb, std::vector<float>(k.begin(), k.end()));
+    c.omega = upload(ob, std::vector<float>{(float)(2 * 3.14159265358979323846 * (double)freq)});
+    const float2* sref = upload(sb, std::vector<float2>{make_float2(s_re, s_im)});
+    float2* f = fb.as<float2>(n);
+    launch_phase_tables(c, sref, p->eps, f, 0);
+    const bool alias = in == out;
+    Staged si, so;
+    so.out(out, (size_t)n * nrow * 8, add != 0 || alias);
+    if (alias) si.dev = so.dev; else si.in(in, (size_t)n * nrow * 8);
+    launch_diag_rows((const float2*)si.dev, f, (float2*)so.dev, n, nrow, adj ? 1 : 0, add, 0);
+    cuda_check(cudaGetLastError(), "phshift kernels");
+    cuda_check(cudaStreamSynchronize(0), "phshift");
+    so.finish(out);
+  });
+}
+
+// Reflect / dReflect coefficients of one grid from the point-table kernel
+struct ReflTables {
+  Buf s, d, rc, sc, a0, b0, a1, b1;
+  DevCtx c{};
+  ReflTables(const void* slow2, const void* rho, int nx, int nz, bool born) {
+    require(slow2 && rho && nx >= 1 && nz >= 2, "bad reflectivity arguments");
+    const size_t n = (size_t)nx * nz;
+    Staged ss, sr;
+    ss.in(slow2, n * 8);
+    sr.in(rho, n * 8);
+    float2* sp = s.as<float2>(n);
+    float2* dp = d.as<float2>(n);
+    cuda_check(cudaMemcpy(sp, ss.dev, n * 8, cudaMemcpyDeviceToDevice), "copy");
+    cuda_check(cudaMemcpy(dp, sr.dev, n * 8, cudaMemcpyDeviceToDevice), "copy");
+    launch_point_tables(1, nz, nx, 1, 0, 0.f, sp, nullptr, dp, nullptr, nullptr, nullptr, rc.as<float2>(n),
+                        born ? sc.as<float2>(n) : nullptr, born ? a0.as<float2>(n) : nullptr,
+                        born ? b0.as<float2>(n) : nullptr, born ? a1.as<float2>(n) : nullptr,
+                        born ? b1.as<float2>(n) : nullptr, 0);
+    cuda_check(cudaGetLastError(), "point tables");
+    c.nz = nz;
+    c.nxg = nx;
+    c.pad = 0;
+  }
+};
+
+int wem_reflect(const void* slow2, const void* rho, int nx, int nz, int adj, const void* in, void* out) {
+  return guard([&] {
+    require(in && out, "NULL argument");
+    ReflTables T(slow2, rho, nx, nz, false);
+    const size_t n = (size_t)nx * nz;
+    const bool alias = in == out;
+    Staged si, so;
+    so.out(out, n * 8, alias);
+    if (alias) si.dev = so.dev; else si.in(in, n * 8);
+    // Reflect.h:34-47 assigns r m (conj(r) d): the output never accumulates
+    launch_diag_rows((const float2*)si.dev, (const float2*)T.rc.p, (float2*)so.dev, (int)n, 1, adj ? 1 : 0, 0, 0);
+    cuda_check(cudaGetLastError(), "reflect kernel");
+    cuda_check(cudaStreamSynchronize(0), "reflect");
+    so.finish(out);
+  });
+}
+
+int wem_dreflect(const void* slow2, const void* rho, int nx, int nz, int adj, void* dslow2, void* drho, void* data,
+                 int add) {
+  return guard([&] {
+    require(dslow2 && drho && data, "NULL argument");
+    ReflTables T(slow2, rho, nx, nz, true);
+    const size_t n = (size_t)nx * nz;
+    const float2 *a0 = (const float2*)T.a0.p, *b0 = (const float2*)T.b0.p;
+    const float2 *a1 = (const float2*)T.a1.p, *b1 = (const float2*)T.b1.p;
+    if (!adj) {
+      Staged m0, m1, d;
+      m0.in(dslow2, n * 8);
+      m1.in(drho, n * 8);
+      d.out(data, n * 8, add != 0);
+      Buf tb;
+      float2* t = add ? tb.as<float2>(n) : (float2*)d.dev;
+      launch_drefl_fwd(T.c, 1, a0, b0, a1, b1, (const float2*)m0.dev, (const float2*)m1.dev, t, 0);
+      if (add) launch_scale_add((float2*)d.dev, t, n, 0);
+      cuda_check(cudaGetLastError(), "dreflect kernels");
+      cuda_check(cudaStreamSynchronize(0), "dreflect");
+      d.finish(data);
+    } else {
+      Staged d, g0, g1;
+      d.in(data, n * 8);
+      g0.out(dslow2, n * 8, add != 0);
+      g1.out(drho, n * 8, add != 0);
+      Buf zb;
+      float2* zero = zb.as<float2>(n);
+      cuda_check(cudaMemsetAsync(zero, 0, n * 8, 0), "memset");
+      launch_grad_assemble(T.c, 1, a0, b0, a1, b1, (const float2*)d.dev, zero, (float2*)g0.dev, (float2*)g1.dev, nx,
+                           add, 0);
+      cuda_check(cudaGetLastError(), "dreflect kernels");
+      cuda_check(cudaStreamSynchronize(0), "dreflect");
+      g0.finish(dslow2);
+      g1.finish(drho);
+    }
   });
 }
 

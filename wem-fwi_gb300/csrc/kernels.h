@@ -155,4 +155,13 @@ void launch_copy_rows(const float2* src, int lds, float2* dst, int ldd, int nrow
                       cudaStream_t st);
 void launch_scale_add(float2* y, const float2* x, size_t n, cudaStream_t st);
 
+// ---- element-wise operators of the row-level API (rowops.cu)
+// out[r][k] = f[k] in[r][k] (conj(f) with conj), added with add
+void launch_diag_rows(const float2* in, const float2* f, float2* out, int n, int nrow, int conj, int add,
+                      cudaStream_t st);
+// SplitStep at the points loc[0..nloc) of rows of nx points (srow: the
+// slowness^2 row of the depth); the other points are not touched
+void launch_splitstep(const float2* srow, const int* loc, int nloc, int nx, int nrow, double wdz, double sr,
+                      double si, int adj, const float2* in, float2* out, cudaStream_t st);
+
 }  // namespace wg

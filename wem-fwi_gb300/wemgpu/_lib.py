@@ -70,6 +70,12 @@ _SIGS = {
     "wemop_scatter": (_i, [_h, _i, _f, _i, _v, _v, _i, _i]),
     "wemop_refsampler": (_i, [_h, _v, _v]),
     "wemop_onestep_noalloc": (_i, [_pp, _v, _v, _v, _i, _f, _i, _v, _v, _i, _i, _v]),
+    "wemop_splitstep": (_i, [_h, _i, _f, _f, _f, _v, _i, _i, _v, _v, _i, _i]),
+    "wemop_lindown": (_i, [_h, _v, _f, _i, _v, _v, _i]),
+    "wem_ic": (_i, [_v, _i, _i, _v, _v, _i]),
+    "wem_phshift": (_i, [_pp, _i, _f, _f, _f, _f, _f, _i, _v, _v, _i, _i]),
+    "wem_reflect": (_i, [_v, _v, _i, _i, _i, _v, _v]),
+    "wem_dreflect": (_i, [_v, _v, _i, _i, _i, _v, _v, _v, _i]),
     "lanczos2d_create": (_i, [_i, _f, _i, _f, _i, _f, _i, _f, ctypes.POINTER(_f), ctypes.POINTER(_h)]),
     "spline2d_create": (_i, [_i, _f, _i, _f, _i, _f, _i, _f, _f, _f, ctypes.POINTER(_h)]),
     "interp2d_destroy": (None, [_h]),

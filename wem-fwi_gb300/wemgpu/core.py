@@ -309,11 +309,67 @@ class RowOps:
                   ptr(out, np.complex64), n, int(bool(add)))
         return out
 
+    def splitstep(self, iz, freq, sref, loc, adj, x, out=None, add=False):
+        """SplitStep of depth iz on the points ``loc`` (wemop_splitstep)."""
+        out = _like(x) if out is None else out
+        n = self._rows(x, self.nxg)
+        loc = np.ascontiguousarray(loc, dtype=np.int32).reshape(-1)
+        _lib.call("wemop_splitstep", self.h, int(iz), float(freq), float(np.real(sref)), float(np.imag(sref)),
+                  ctypes.c_void_p(loc.ctypes.data), int(loc.size), int(adj), ptr(x, np.complex64),
+                  ptr(out, np.complex64, None, "out", True), n, int(bool(add)))
+        return out
+
+    def lindown(self, bg, freq, adj, x, out=None, add=False):
+        """LinDown of one field [nz][nxg] around the background wavefield bg."""
+        out = _like(x) if out is None else out
+        shape = (self.nz, self.nxg)
+        _lib.call("wemop_lindown", self.h, ptr(bg, np.complex64, shape, "bg"), float(freq), int(adj),
+                  ptr(x, np.complex64, shape, "in"), ptr(out, np.complex64, shape, "out", True), int(bool(add)))
+        return out
+
     def refsampler(self):
         sref = np.zeros((self.nz, self.p.nref), np.complex64)
         idx = np.zeros((self.nz, self.nxg), np.int32)
         _lib.call("wemop_refsampler", self.h, ptr(sref, np.complex64), ctypes.c_void_p(idx.ctypes.data))
         return sref, idx
+
+
+def ic(bg, adj, x, out, add=False):
+    """Imaging condition out (+)= bg x (adjoint conj(bg) x), element-wise."""
+    n = int(np.prod(x.shape)) if not _is_torch(x) else x.numel()
+    _lib.call("wem_ic", ptr(bg, np.complex64, tuple(x.shape), "bg"), n, int(adj), ptr(x, np.complex64),
+              ptr(out, np.complex64, tuple(x.shape), "out", True), int(bool(add)))
+    return out
+
+
+def phshift(p: WemParams, dx, dz, freq, s, adj, x, out, add=False):
+    """Phase shift of rows of wavenumber samples (wem_phshift)."""
+    n = x.shape[-1]
+    nrow = (int(np.prod(x.shape)) if not _is_torch(x) else x.numel()) // n
+    _lib.call("wem_phshift", ctypes.byref(p), int(n), float(dx), float(dz), float(freq), float(np.real(s)),
+              float(np.imag(s)), int(adj), ptr(x, np.complex64), ptr(out, np.complex64, tuple(x.shape), "out", True),
+              nrow, int(bool(add)))
+    return out
+
+
+def reflect(slow2, rho, adj, x, out):
+    """Reflect of the grid (slow2, rho): out = r x (conj(r) x)."""
+    nz, nx = slow2.shape[-2], slow2.shape[-1]
+    shape = (nz, nx)
+    _lib.call("wem_reflect", ptr(slow2, np.complex64, shape, "slowness"), ptr(rho, np.complex64, shape, "density"),
+              nx, nz, int(adj), ptr(x, np.complex64, shape, "in"), ptr(out, np.complex64, shape, "out", True))
+    return out
+
+
+def dreflect(slow2, rho, adj, m0, m1, data, add=False):
+    """dReflect at (slow2, rho): forward data (+)= dR(m0, m1), adjoint
+    (m0, m1) (+)= dR^H data."""
+    nz, nx = slow2.shape[-2], slow2.shape[-1]
+    shape = (nz, nx)
+    _lib.call("wem_dreflect", ptr(slow2, np.complex64, shape, "slowness"), ptr(rho, np.complex64, shape, "density"),
+              nx, nz, int(adj), ptr(m0, np.complex64, shape, "dslowness", True),
+              ptr(m1, np.complex64, shape, "ddensity", True), ptr(data, np.complex64, shape, "data", True),
+              int(bool(add)))
 
 
 class Interp2DOp:

@@ -78,8 +78,15 @@ class Propagator:
         out = []
         for add in (False, True):
             if add:
+                # the outputs' prior contents get the norms of L m and L^H d:
+                # much larger ones would swamp the added part in fp32
+                nd, nm = d1.norm(), m1.norm()
                 m1.rand(seed + 11)
                 d1.rand(seed + 13)
+                if nm > 0:
+                    m1.scale(nm / max(m1.norm(), 1e-300))
+                if nd > 0:
+                    d1.scale(nd / max(d1.norm(), 1e-300))
                 m1c, d1c = m1.clone(), d1.clone()
             self.forward(add, m, d1)
             self.adjoint(add, m1, d)

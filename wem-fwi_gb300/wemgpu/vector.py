@@ -157,6 +157,11 @@ class SuperVector:
             v.rand(None if seed is None else seed + i)
         return self
 
+    def scale(self, s) -> "SuperVector":
+        for v in self.vecs:
+            v.scale(s)
+        return self
+
     def dot(self, other: "SuperVector") -> float:
         return sum(a.dot(b) for a, b in zip(self.vecs, other.vecs))
 
