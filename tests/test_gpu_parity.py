@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from cases import pad_edge, rand_c, rel_l2, small_case
-from wemgpu.params import WEM_DATA_FREQ, WEM_DATA_TIME
+from wemgpu.params import WEM_DATA_FREQ, WEM_DATA_TIME, make_params
 
 pytestmark = pytest.mark.gpu
 
@@ -457,3 +457,40 @@ def test_small_geometries(gpu_lib, oracle, kw, nz, ns):
     q0, q1 = oracle.born_adjoint(p, wav, s, rho, dd, kind=WEM_DATA_TIME, prec=64)
     assert rel_l2(a0, q0) < TOL_OP, ("adj s", rel_l2(a0, q0))
     assert rel_l2(a1, q1) < TOL_OP, ("adj rho", rel_l2(a1, q1))
+
+
+def test_born_dot_reference_setup(gpu_lib):
+    """The set-up of the reference's Born dot test (scripts/unit_tests/
+    dot_test_born.py:13-77): 300 x 300 at 10 m, slowness 1/2000 as the script
+    sets it, 5 shots 20 m apart, receivers every cell at 1000 m depth, 15
+    frequencies from 1 Hz, SSF, N = 300 (shared-memory kernels).  The exact
+    adjoint passes to 1e-5; the compat adjoint (the reference's own) is not
+    a transpose and is only checked to be finite."""
+    from wemgpu.core import BornOp
+    n, nt, dt = 300, 1500, 0.002
+    par = dict(ns=5, osx=0.0, dsx=20.0, osz=0.0, nr=n, orx=0.0, drx=10.0, orz=1000.0, prop="ssf", nref=1, tap=0,
+               fmin=1, fmax=0, nfreq=15, ngs=0, ngr=0, ntaylor=1)
+    t = np.arange(nt) * dt
+    wav = ((1 - 2 * (np.pi * 5 * t) ** 2) * np.exp(-(np.pi * 5 * t) ** 2)).astype(np.float32)
+    s = np.full((n, n), 1 / 2000, np.complex64)
+    rho = np.ones((n, n), np.complex64)
+    rng = np.random.default_rng(13)
+    m0, m1 = rand_c(rng, s.shape), rand_c(rng, s.shape)
+    n0, n1 = rand_c(rng, s.shape), rand_c(rng, s.shape)
+    for mode in ("exact", "compat"):
+        p = make_params(dict(par, adjoint_mode=mode), nx=n, nz=n, dx=10.0, dz=10.0, nt=nt, dt=dt)
+        op = BornOp(p, wav, s, rho)
+        d = np.zeros((p.ns, p.nr, p.nt), np.float32)
+        op.forward(n0 + 0.5 * m0, n1 + 0.5 * m1, d)
+        Lm = np.zeros_like(d)
+        op.forward(m0, m1, Lm)
+        a0, a1 = np.zeros_like(m0), np.zeros_like(m1)
+        op.adjoint(a0, a1, d)
+        lhs = np.vdot(d.astype(np.float64), Lm.astype(np.float64))
+        rhs = (np.vdot(a0.astype(np.complex128), m0.astype(np.complex128)).real +
+               np.vdot(a1.astype(np.complex128), m1.astype(np.complex128)).real)
+        ratio = abs(lhs - rhs) / abs(lhs)
+        if mode == "exact":
+            assert ratio < 1e-5, ratio
+        else:
+            assert np.isfinite(ratio)

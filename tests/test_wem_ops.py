@@ -195,3 +195,16 @@ def test_reference_dot_tests(gpu_lib):
         if (errs[0] if name in assign else max(errs)) > 1e-4:
             bad[name] = errs
     assert not bad, bad
+
+
+@pytest.mark.gpu
+def test_phshift_dot_reference_setup(gpu_lib):
+    """propagator/test/dotPh.cpp:18-53: Phshift(dz 5) on rows of 500 samples at
+    spacing 0.001, 5 Hz, slowness 0.002."""
+    from wemgpu import wem_ops as wem
+    from wemgpu.vector import Hypercube, Vector
+    h = Hypercube(ns=[500], ds=[0.001])
+    row = Vector(h, np.zeros(500, np.complex64), storage="dataComplex")
+    op = wem.Phshift(row, row.clone(), h, 5.0, 5, 0.002, 0)
+    assert max(op.dotTest()) <= 1e-5
+
