@@ -132,7 +132,9 @@ def make_params(par: Any, *, nx: int, nz: int, dx: float, dz: float,
         if isinstance(ang, str):
             with open(ang) as f:
                 ang = json.load(f)["a"]
-        arr = np.ascontiguousarray(np.asarray(ang, dtype=np.float32))
+        arr = np.ascontiguousarray(np.asarray(ang, dtype=np.float32)).reshape(-1)
+        if p.cmap == 2 and arr.size < p.ns:
+            raise ValueError(f"cmap_angles holds {arr.size} angles for {p.ns} shots")
         p._keep.append(arr)
         p.cmap_angles = arr.ctypes.data_as(_fp)
     return p
