@@ -111,11 +111,11 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def workload(small=False):
+def workload(small=False, small_shots=8):
     from wemgpu import synthetic as S
     cfg = S.c3()
     if small:  # a reduced case of the same kernels for profiling captures
-        cfg["par"] = dict(cfg["par"], ns=8, dsx=cfg["par"]["dsx"] * 4, fmax=6.0)
+        cfg["par"] = dict(cfg["par"], ns=small_shots, dsx=cfg["par"]["dsx"] * 32 // small_shots, fmax=6.0)
     return cfg
 
 
@@ -171,7 +171,7 @@ def run_gpu(args, rank, world):
     lib = _lib.load()
     dev = torch.device(f"cuda:{int(os.environ.get('LOCAL_RANK', 0))}")
     torch.cuda.set_device(dev)
-    cfg = workload(args.small)
+    cfg = workload(args.small, args.small_shots)
     p = S.params_of(cfg)
     # weak scaling: every rank owns its own block of shots of the same size
     nf = WemOp(p, cfg["wavelet"]).nfreq()
@@ -367,7 +367,7 @@ def run_reference(args, rank, world):
     """CPU restatement on the host cores, same config / metric / unit."""
     if rank != 0:
         return
-    cfg = workload(args.small)
+    cfg = workload(args.small, args.small_shots)
     # the sample is sized once, so that all warm-up and timed steps together
     # take about two minutes (1-10 s each), then every step repeats it
     per_step = min(10.0, max(1.0, 120.0 / (args.warmup + args.steps)))
@@ -402,6 +402,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--small", action="store_true", help="reduced case (profiling captures)")
+    ap.add_argument("--small-shots", type=int, default=8, help="shots of the reduced case")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
