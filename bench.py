@@ -133,7 +133,7 @@ def config_of(p, nf, world, small):
     return {"workload": "c3 FWI gradient: WEM fwd + residual + Born adjoint (compat)",
             "nx": p.nx, "nz": p.nz, "dx": p.dx, "shots": p.ns * world, "freqs": nf, "fft_n": p.nx + 2 * p.pad,
             "prop": "ssf", "depth_steps_per_iter": row_steps(p, nf) * world,
-            "l2": "inputs larger than L2 (stored wavefields ~11 GB per pass)",
+            "l2": "inputs larger than L2 (stored wavefields ~17 GB per Born adjoint pass)",
             "small": bool(small)}
 
 
