@@ -555,6 +555,8 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
     if (!act) continue;
     w_record<E>(w, W, s, bin, z, bins);
     if (z == 0) break;
+    // without the shared-memory row, bring the row of the next depth into L2
+    if (!L.row_bytes && lane == 0 && z >= 2) l2_prefetch(A + (size_t)(z - 2) * nxg, nxg * 8);
     const Tabs T = ring.tabs(z);
     // W = P_z W + R[z-1] down[z-1]
 #pragma unroll 1
