@@ -323,12 +323,14 @@ __device__ __forceinline__ void sc_pre(const WRow& w, const Tabs& T, int mode, c
   }
 }
 // mid: the (k / omega)^2 filter, with the 1/N of the inverse transform
+// (one division per call: k^2 times 1 / omega^2)
 template <int E>
 __device__ __forceinline__ void sc_mid(const WRow& w, float om, float2 (&X)[E]) {
+  const float s = w.c.invN / (om * om);
 #pragma unroll
   for (int j = 0; j < E; ++j) {
-    const float kw = w.kx[w.lane + 32 * j] / om;
-    X[j] = c_scale(X[j], kw * kw * w.c.invN);
+    const float k = w.kx[w.lane + 32 * j];
+    X[j] = c_scale(X[j], k * k * s);
   }
 }
 // post, one point: i w dz (c_0 u + c_1 filtered) with the mode's conjugations;
@@ -338,10 +340,11 @@ __device__ __forceinline__ void sc_mid(const WRow& w, float om, float2 (&X)[E]) 
 // point is masked between them)
 template <int E>
 __device__ __forceinline__ void sc_spec(const WRow& w, float om, const float2 (&X)[E], float2 (&Y)[E]) {
+  const float s = 1.f / (om * om);
 #pragma unroll
   for (int j = 0; j < E; ++j) {
-    const float kw = w.kx[w.lane + 32 * j] / om;
-    Y[j] = c_scale(X[j], kw * kw);
+    const float k = w.kx[w.lane + 32 * j];
+    Y[j] = c_scale(X[j], k * k * s);
   }
 }
 __device__ __forceinline__ float2 sc_val(float2 iw, int mode, bool t1, float2 k0, float2 k1, float2 u, float2 x) {
@@ -1101,10 +1104,11 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
         if (reuse) {
           // filtered spectrum of T[z+1], every point (tap 0: N = nxg)
           float2* g = SG + (size_t)(z + 1) * nxg;
+          const float s2 = 1.f / (om * om);
 #pragma unroll
           for (int j = 0; j < E; ++j) {
-            const float kw = w.kx[lane + 32 * j] / om;
-            g[lane + 32 * j] = c_scale(X[j], kw * kw);
+            const float k = w.kx[lane + 32 * j];
+            g[lane + 32 * j] = c_scale(X[j], k * k * s2);
           }
         }
       }
