@@ -37,6 +37,8 @@ bool g_plain = false;
 int g_path = 0;  // 0 automatic, 1 shared-memory kernels, 2 warp-per-row kernels
 std::vector<std::pair<std::string, KStat>> g_stats;
 
+std::mutex g_stats_mu;  // engines may run on several host threads
+
 KStat& stat_of(const std::string& name) {
   for (auto& kv : g_stats)
     if (kv.first == name) return kv.second;
@@ -60,19 +62,54 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// one cuBLAS handle per device for the time <-> frequency GEMMs, created on
-// first use and kept for the life of the process
-cublasHandle_t blas_handle() {
-  static std::mutex mu;
-  static cublasHandle_t handles[64] = {};
-  int dev = 0;
-  cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
-  require(dev >= 0 && dev < 64, "device index out of range");
-  std::lock_guard<std::mutex> lock(mu);
-  if (!handles[dev] && cublasCreate(&handles[dev]) != CUBLAS_STATUS_SUCCESS)
-    throw Fail(WEM_EDEVICE, "cublasCreate failed");
-  return handles[dev];
-}
+// cuBLAS handles for the time <-> frequency GEMMs: a per-device pool, one
+// handle lent to a caller for the length of a call (host threads that run
+// engines side by side each hold their own); handles are created on first
+// need and kept for the life of the process
+class BlasLease {
+ public:
+  BlasLease() {
+    cuda_check(cudaGetDevice(&dev_), "cudaGetDevice");
+    require(dev_ >= 0 && dev_ < kMaxDev, "device index out of range");
+    {
+      std::lock_guard<std::mutex> lock(mu());
+      auto& f = pool()[dev_];
+      if (!f.empty()) {
+        h_ = f.back();
+        f.pop_back();
+      }
+    }
+    if (!h_ && cublasCreate(&h_) != CUBLAS_STATUS_SUCCESS) throw Fail(WEM_EDEVICE, "cublasCreate failed");
+    // the calling thread's default stream, where its engine's kernels run
+    if (cublasSetStream(h_, cudaStreamPerThread) != CUBLAS_STATUS_SUCCESS) {
+      give_back();
+      throw Fail(WEM_EDEVICE, "cublasSetStream failed");
+    }
+  }
+  ~BlasLease() { give_back(); }
+  BlasLease(const BlasLease&) = delete;
+  BlasLease& operator=(const BlasLease&) = delete;
+  cublasHandle_t get() const { return h_; }
+
+ private:
+  static constexpr int kMaxDev = 64;
+  static std::mutex& mu() {
+    static std::mutex m;
+    return m;
+  }
+  static std::vector<cublasHandle_t>* pool() {
+    static std::vector<cublasHandle_t> p[kMaxDev];
+    return p;
+  }
+  void give_back() {
+    if (!h_) return;
+    std::lock_guard<std::mutex> lock(mu());
+    pool()[dev_].push_back(h_);
+    h_ = nullptr;
+  }
+  int dev_ = 0;
+  cublasHandle_t h_ = nullptr;
+};
 
 void blas_check(cublasStatus_t st, const char* what) {
   if (st != CUBLAS_STATUS_SUCCESS) throw Fail(WEM_EDEVICE, std::string(what) + ": cuBLAS status " + std::to_string((int)st));
@@ -173,6 +210,7 @@ void timed(const char* name, Fn fn) {
   cuda_check(cudaEventElapsedTime(&ms, a, b), "event");
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  std::lock_guard<std::mutex> lock(g_stats_mu);
   KStat& k = stat_of(name);
   k.ms += ms;
   k.n += 1;
@@ -902,8 +940,8 @@ class Engine {
   // GEMM with the inverse DFT matrix of the propagated bins
   void bins_to_time(float* t, int add) {
     const int ntr = geo_.ns * geo_.nr;
-    cublasHandle_t h = blas_handle();
-    blas_check(cublasSetStream(h, 0), "cublasSetStream");
+    BlasLease lease;
+    cublasHandle_t h = lease.get();
     const float one = 1.f, beta = add ? 1.f : 0.f;
     blas_check(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, p_.nt, ntr, 2 * F_, &one, (const float*)winv_.p, p_.nt,
                            (const float*)bins_, 2 * F_, &beta, t, p_.nt),
@@ -914,8 +952,8 @@ class Engine {
   // time traces on the device -> internal bins
   void time_to_bins(const float* t) {
     const int ntr = geo_.ns * geo_.nr;
-    cublasHandle_t h = blas_handle();
-    blas_check(cublasSetStream(h, 0), "cublasSetStream");
+    BlasLease lease;
+    cublasHandle_t h = lease.get();
     const float one = 1.f, zero = 0.f;
     blas_check(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, 2 * F_, ntr, p_.nt, &one, (const float*)wfwd_.p, 2 * F_, t,
                            p_.nt, &zero, (float*)bins_, 2 * F_),
@@ -1174,6 +1212,7 @@ int wem_stats_enable(int on) {
 int wem_stats_get(const char* kernel, double* total_ms, long long* launches) {
   return guard([&] {
     require(kernel && total_ms && launches, "NULL argument");
+    std::lock_guard<std::mutex> lock(g_stats_mu);
     KStat& k = stat_of(kernel);
     *total_ms = k.ms;
     *launches = k.n;
@@ -1190,6 +1229,7 @@ int wem_set_plain(int plain) {
   return WEM_OK;
 }
 int wem_stats_reset(void) {
+  std::lock_guard<std::mutex> lock(g_stats_mu);
   g_stats.clear();
   return WEM_OK;
 }

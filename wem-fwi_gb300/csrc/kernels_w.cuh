@@ -16,6 +16,7 @@
 // Invariant: points of the padded row outside the model grid (the FFT zero
 // pad of width tap on each side) are zero in every state array.
 #pragma once
+#include <mutex>
 #include <cmath>
 
 #include "kernels.h"
@@ -1373,15 +1374,15 @@ bool adj2_fits(const DevCtx& c) {
 }
 // W_96 twiddles of this translation unit's copy of c_w96
 inline void init_w96() {
-  static bool init = false;
-  if (init) return;
-  float2 h[96];
-  for (int k = 0; k < 96; ++k) {
-    long double a = -2.0L * 3.14159265358979323846264338327950288L * k / 96;
-    h[k] = make_float2((float)std::cos(a), (float)std::sin(a));
-  }
-  cudaMemcpyToSymbol(c_w96, h, sizeof(h));
-  init = true;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    float2 h[96];
+    for (int k = 0; k < 96; ++k) {
+      long double a = -2.0L * 3.14159265358979323846264338327950288L * k / 96;
+      h[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    cudaMemcpyToSymbol(c_w96, h, sizeof(h));
+  });
 }
 
 }  // namespace

@@ -50,7 +50,12 @@ def build(force: bool = False, verbose: bool = False) -> str:
         return LIB
     nvcc = _nvcc()
     os.makedirs(OBJ_DIR, exist_ok=True)
-    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
+    # stream 0 of every launch and runtime call is the calling thread's
+    # default stream: host threads that drive separate engines run on the
+    # GPU concurrently (the per-thread default stream still synchronises with
+    # the legacy default stream other libraries use)
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "--default-stream", "per-thread",
+              "-DCUDA_API_PER_THREAD_DEFAULT_STREAM=1", "-I", INCLUDE, "-I", CSRC]
 
     def compile_one(src: str) -> str:
         obj = os.path.join(OBJ_DIR, src + ".o")
