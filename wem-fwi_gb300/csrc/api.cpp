@@ -15,6 +15,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "cmap.h"
@@ -272,8 +273,13 @@ class Engine {
     int dev = 0;
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     if (!maps.empty()) {
-      // the shots share the time <-> frequency matrices
+      // the shots share the time <-> frequency matrices; they run on
+      // `workers_` host threads (shot s on thread s mod workers_, in order),
+      // each thread with its own large buffers
       dft_ = std::make_shared<const DftMatrices>(dft_matrices(geo_, p.nt));
+      workers_ = std::max(1, std::min(geo_.ns, kShotWorkers));
+      for (int w = 0; w < workers_; ++w) worker_ws_.push_back(std::make_shared<Scratch>());
+      acc_.resize(workers_);
       for (int s = 0; s < geo_.ns; ++s) {
         const ShotMap& m = maps[s];
         wem_params ps = p;
@@ -290,7 +296,7 @@ class Engine {
         gs.sptr = {0, (int)m.src_x.size()};
         gs.rx = m.rec_x;
         gs.rz = m.rec_z;
-        shots_.push_back(std::unique_ptr<Engine>(new Engine(ps, gs, m, born, dft_, ws_)));
+        shots_.push_back(std::unique_ptr<Engine>(new Engine(ps, gs, m, born, dft_, worker_ws_[s % workers_])));
       }
       return;
     }
@@ -335,7 +341,7 @@ class Engine {
       Staged a, b;
       a.in(s2, nm);
       b.in(rho, nm);
-      for (int s = 0; s < geo_.ns; ++s) shots_[s]->wem_forward(a.dev, b.dev, shot_data(data, kind, s), kind, add);
+      for_shots([&](int s, int) { shots_[s]->wem_forward(a.dev, b.dev, shot_data(data, kind, s), kind, add); });
       return;
     }
     set_background(s2, rho);
@@ -370,18 +376,22 @@ class Engine {
       ob.in(dobs, (size_t)geo_.ns * geo_.nr * p_.nt * 4);
       o0.out(g_s2, nm * 8, false);
       o1.out(g_rho, nm * 8, false);
-      float2* g0 = cm_g0_.as<float2>(nm);
-      float2* g1 = cm_g1_.as<float2>(nm);
-      double loss = 0;
-      for (int s = 0; s < geo_.ns; ++s) {
+      std::vector<double> losses(geo_.ns, 0.0);
+      for_shots([&](int s, int w) {
         Engine& e = *shots_[s];
-        loss += e.fwi_gradient(a.dev, b.dev, shot_data(ob.dev, WEM_DATA_TIME, s), g0, g1);
-        e.image_back(g0, (float2*)o0.dev, s > 0);
-        e.image_back(g1, (float2*)o1.dev, s > 0);
-      }
-      cuda_check(cudaStreamSynchronize(0), "fwi_gradient");
+        ShotAcc& A = acc_[w];
+        float2* g0 = A.g0.as<float2>(nm);
+        float2* g1 = A.g1.as<float2>(nm);
+        losses[s] = e.fwi_gradient(a.dev, b.dev, shot_data(ob.dev, WEM_DATA_TIME, s), g0, g1);
+        e.image_back(g0, A.s0.as<float2>(nm), s >= workers_);
+        e.image_back(g1, A.s1.as<float2>(nm), s >= workers_);
+        cuda_check(cudaStreamSynchronize(0), "fwi_gradient");
+      });
+      sum_workers((float2*)o0.dev, (float2*)o1.dev, nm, false);
       o0.finish(g_s2);
       o1.finish(g_rho);
+      double loss = 0;
+      for (double v : losses) loss += v;
       return loss;
     }
     set_background(s2, rho);
@@ -408,10 +418,10 @@ class Engine {
       Staged a, b;
       a.in(ds2, nm);
       b.in(drho, nm);
-      for (int s = 0; s < geo_.ns; ++s) {
+      for_shots([&](int s, int) {
         shots_[s]->set_background(cm_bg0_.p, cm_bg1_.p);
         shots_[s]->born_forward(a.dev, b.dev, shot_data(data, kind, s), kind, add);
-      }
+      });
       return;
     }
     const size_t plane = (size_t)p_.nz * geo_.nxg;
@@ -519,21 +529,24 @@ class Engine {
     require(ds2 && drho && data, "NULL argument");
     if (!shots_.empty()) {
       // every shot's gradient is brought back to the model grid by the
-      // inverse map and summed in shot order (born_prop.cpp:217-232)
+      // inverse map (born_prop.cpp:217-232); each worker thread sums its
+      // shots in order, then the workers' sums are added in worker order
       const size_t nm = (size_t)p_.nz * p_.nx;
       Staged o0, o1;
       o0.out(ds2, nm * 8, add != 0);
       o1.out(drho, nm * 8, add != 0);
-      float2* g0 = cm_g0_.as<float2>(nm);
-      float2* g1 = cm_g1_.as<float2>(nm);
-      for (int s = 0; s < geo_.ns; ++s) {
+      for_shots([&](int s, int w) {
         Engine& e = *shots_[s];
+        ShotAcc& A = acc_[w];
+        float2* g0 = A.g0.as<float2>(nm);
+        float2* g1 = A.g1.as<float2>(nm);
         e.set_background(cm_bg0_.p, cm_bg1_.p);
         e.born_adjoint(g0, g1, shot_data(data, kind, s), kind, 0);
-        e.image_back(g0, (float2*)o0.dev, s > 0 || add);
-        e.image_back(g1, (float2*)o1.dev, s > 0 || add);
-      }
-      cuda_check(cudaStreamSynchronize(0), "born_adjoint");
+        e.image_back(g0, A.s0.as<float2>(nm), s >= workers_);
+        e.image_back(g1, A.s1.as<float2>(nm), s >= workers_);
+        cuda_check(cudaStreamSynchronize(0), "born_adjoint");
+      });
+      sum_workers((float2*)o0.dev, (float2*)o1.dev, nm, add != 0);
       o0.finish(ds2);
       o1.finish(drho);
       return;
@@ -628,6 +641,7 @@ class Engine {
     M_ = 1;
     M_img_ = 1;
     build_static();
+    ctx_.one_row = 1;  // one shot: every group is one (shot, frequency) row
     map_.reset(new MapDev);
     map_->n = p.nx * p.nz;
     upload(map_->fwd, m.fwd);
@@ -635,6 +649,60 @@ class Engine {
     map_->js = m.js;
     map_->scale = m.js != 1.f || !m.jl.empty();
     if (!m.jl.empty()) map_->jl_d = upload(map_->jl, m.jl);
+  }
+
+  // fn(shot, worker) for every shot, on workers_ host threads: worker w
+  // runs shots w, w + workers_, ... in order on its own default stream;
+  // the first failure is rethrown here once every thread has stopped
+  template <class Fn>
+  void for_shots(Fn fn) {
+    const int ns = (int)shots_.size();
+    if (workers_ <= 1) {
+      for (int s = 0; s < ns; ++s) fn(s, 0);
+      return;
+    }
+    int dev = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    // work the caller queued before (its inputs) precedes the workers' streams
+    cuda_check(cudaDeviceSynchronize(), "cmap inputs");
+    std::mutex mu;
+    std::exception_ptr err;
+    std::vector<std::thread> th;
+    for (int w = 0; w < workers_; ++w)
+      th.emplace_back([&, w] {
+        try {
+          cuda_check(cudaSetDevice(dev), "cudaSetDevice");
+          for (int s = w; s < ns; s += workers_) {
+            {
+              std::lock_guard<std::mutex> lock(mu);
+              if (err) return;
+            }
+            fn(s, w);
+          }
+        } catch (...) {
+          std::lock_guard<std::mutex> lock(mu);
+          if (!err) err = std::current_exception();
+        }
+      });
+    for (auto& t : th) t.join();
+    if (err) std::rethrow_exception(err);
+  }
+
+  // out0/out1 (+)= the workers' sums, in worker order
+  void sum_workers(float2* out0, float2* out1, size_t nm, bool add) {
+    for (int w = 0; w < workers_ && w < (int)shots_.size(); ++w) {
+      const float2* s0 = acc_[w].s0.as<float2>(nm);
+      const float2* s1 = acc_[w].s1.as<float2>(nm);
+      if (w == 0 && !add) {
+        cuda_check(cudaMemcpyAsync(out0, s0, nm * 8, cudaMemcpyDeviceToDevice, 0), "copy");
+        cuda_check(cudaMemcpyAsync(out1, s1, nm * 8, cudaMemcpyDeviceToDevice, 0), "copy");
+      } else {
+        launch_scale_add(out0, s0, nm, 0);
+        launch_scale_add(out1, s1, nm, 0);
+      }
+    }
+    cuda_check(cudaGetLastError(), "sum kernels");
+    cuda_check(cudaStreamSynchronize(0), "sum");
   }
 
   // a shot's slice of caller data
@@ -652,7 +720,14 @@ class Engine {
   };
   std::unique_ptr<MapDev> map_;                // this engine is one shot of a conformal-map operator
   std::vector<std::unique_ptr<Engine>> shots_;  // this operator runs one engine per mapped shot
-  Buf cm_bg0_, cm_bg1_, cm_g0_, cm_g1_, cm_map0_, cm_map1_, cm_map2_, spr_, sptr_;
+  static constexpr int kShotWorkers = 8;        // host threads that run the shots side by side
+  int workers_ = 1;
+  std::vector<std::shared_ptr<Scratch>> worker_ws_;
+  struct ShotAcc {
+    Buf g0, g1, s0, s1;  // a shot's mapped gradient; the worker's running sum on the model grid
+  };
+  std::vector<ShotAcc> acc_;
+  Buf cm_bg0_, cm_bg1_, cm_map0_, cm_map1_, cm_map2_, spr_, sptr_;
 
   wem_params p_;
   bool ext_, born_;

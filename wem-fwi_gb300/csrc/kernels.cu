@@ -851,7 +851,10 @@ int grid_for(size_t n) {
 
 template <class K>
 void set_smem(K kernel, size_t bytes) {
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  // the device's bound rather than this launch's size, so concurrent
+  // launches of the kernel from several host threads never undercut another
+  (void)bytes;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_per_block());
 }
 
 size_t al(size_t n) { return (n + 1) & ~size_t(1); }

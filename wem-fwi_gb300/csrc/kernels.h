@@ -25,6 +25,7 @@ struct DevCtx {
   const float2* rcf;            // [F][nz][nxg] per-frequency reflectivity replacing rc, or null
   int no_fwd_record;            // the forward-scattered (down) field is not recorded
   int last_rule;                // compat last depth row: 0 per shot (BornFull), 1 only the last (f, s)
+  int one_row;                  // every group holds one row: the warp kernels use one-row CTAs
   float dz, invN;
   const float2* tw;             // [N] exp(-2 pi i t/N)
   const float2* ph;             // [F][nz][nref][N] phase-shift factors (phase_shift.ispc)

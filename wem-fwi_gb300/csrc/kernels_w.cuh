@@ -441,7 +441,7 @@ struct Carve {
   char* ring;
   char* rows;
   float2* slots;
-  __device__ Carve(const DevCtx& c, const SlotLayout& L, bool with_slots, int nbuf = kW) {
+  __device__ Carve(const DevCtx& c, const SlotLayout& L, bool with_slots, int nbuf = kW, bool with_taper = true) {
     extern __shared__ float4 smem4[];
     char* p = reinterpret_cast<char*>(smem4);
     auto take = [&](size_t bytes) {
@@ -451,7 +451,7 @@ struct Carve {
     };
     tw = reinterpret_cast<float2*>(take((size_t)32 * E * 8));
     kx = reinterpret_cast<float*>(take((size_t)32 * E * 4));
-    taperN = reinterpret_cast<float*>(take((size_t)c.nxg * 4));
+    taperN = with_taper ? reinterpret_cast<float*>(take((size_t)c.nxg * 4)) : nullptr;
     sb0 = reinterpret_cast<float2*>(take((size_t)nbuf * wbuf_len<E>() * 8));
     ring = take((size_t)L.nslots * L.bytes);
     rows = take((size_t)2 * nbuf * L.row_bytes);
@@ -475,7 +475,8 @@ __device__ __forceinline__ void stage_static(const DevCtx& c, const Carve<E>& sm
     sm.tw[i] = c.tw[r * l * (N / (L * R))];
   }
   for (int i = threadIdx.x; i < N; i += blockDim.x) sm.kx[i] = c.kx[i];
-  for (int i = threadIdx.x; i < c.nxg; i += blockDim.x) sm.taperN[i] = c.taperN[i];
+  if (sm.taperN)
+    for (int i = threadIdx.x; i < c.nxg; i += blockDim.x) sm.taperN[i] = c.taperN[i];
 }
 
 // =============================================================== passes
@@ -483,7 +484,7 @@ __device__ __forceinline__ void stage_static(const DevCtx& c, const Carve<E>& sm
 template <int E, bool MR, bool NT, int R>
 __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, const Group* groups, float2* store,
                                                     float2* bins) {
-  const Carve<E> sm(c, L, false, R);
+  const Carve<E> sm(c, L, false, R, R > 1 || !c.fac);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   stage_static<E>(c, sm);
   const Group gp = groups[blockIdx.x];
@@ -1012,7 +1013,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
                                                               float2* storeBG, float2* storeT, float2* storeG,
                                                               const float2* bins, float2* imgR, float2* imgS,
                                                               int compat) {
-  const Carve<E> sm(c, L, false, 2 * R);
+  const Carve<E> sm(c, L, false, 2 * R, R > 1 || !c.fac);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, row = warp >> 1;
   const bool recv = warp & 1;
   stage_static<E>(c, sm);
@@ -1302,16 +1303,28 @@ constexpr int kRowsAdj2 = 8;
 // (16 warps at 128 registers)
 constexpr int kRowsWem = 16;
 
-// which: 4 is WEM with kRowsWem rows per CTA; exchange buffers per CTA
-inline int nbuf_of(int which) { return which == 3 ? 2 * kRowsAdj2 : (which == 4 ? kRowsWem : kW); }
+// which: 4 is WEM with kRowsWem rows per CTA, 5 WEM with one row, 6 the
+// two-warp Born adjoint with one row; exchange buffers per CTA
+inline int nbuf_of(int which) {
+  switch (which) {
+    case 3: return 2 * kRowsAdj2;
+    case 4: return kRowsWem;
+    case 5: return 1;
+    case 6: return 2;
+    default: return kW;
+  }
+}
 // the tables a pass reads: as WEM (0), Born forward (1) or Born adjoint (2)
-inline int tables_of(int which) { return which == 4 ? 0 : (which == 3 ? 2 : which); }
+inline int tables_of(int which) { return (which == 4 || which == 5) ? 0 : ((which == 3 || which == 6) ? 2 : which); }
+// one-row CTAs leave the taper out of shared memory when the split-step table
+// carries it (SSF)
+inline bool taper_of(const DevCtx& c, int which) { return !((which == 5 || which == 6) && c.fac); }
 
 template <int E>
 size_t base_bytes(const DevCtx& c, int which) {
   auto r16 = [](size_t b) { return (b + 15) & ~size_t(15); };
   const int nbuf = nbuf_of(which);
-  return r16((size_t)32 * E * 8) + r16((size_t)32 * E * 4) + r16((size_t)c.nxg * 4) +
+  return r16((size_t)32 * E * 8) + r16((size_t)32 * E * 4) + (taper_of(c, which) ? r16((size_t)c.nxg * 4) : 0) +
          r16((size_t)nbuf * wbuf_len<E>() * 8) + (which == 2 ? r16((size_t)kW * c.nxg * 8) : 0);
 }
 
@@ -1339,7 +1352,9 @@ SlotLayout slot_layout(const DevCtx& c, int pass, int limit) {
   L.dr = which == 1 ? put(rowb) : -1;
   L.bytes = off;
   L.nslots = 3;
-  L.row_bytes = which == 0 ? rowb : 0;
+  // one-row WEM CTAs read the stored row through L2 (prefetched a depth
+  // ahead) so that three of them fit on an SM
+  L.row_bytes = (which == 0 && pass != 5) ? rowb : 0;
   auto total = [&]() {
     return base_bytes<E>(c, pass) + (size_t)L.nslots * L.bytes + (size_t)2 * nbuf_of(pass) * L.row_bytes;
   };
@@ -1372,6 +1387,13 @@ bool adj2_fits(const DevCtx& c) {
   const SlotLayout L3 = slot_layout<E>(c, 3, max_smem_per_block());
   return L3.nslots == 3 && (c.fac || L3.ref >= 0);
 }
+// a kernel may take up to the device's opt-in shared memory per block; set
+// once to that bound (not to one launch's size), so launches of the same
+// kernel from several host threads never see a smaller bound set by another
+template <class K>
+void set_max_smem(K kern) {
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem_per_block());
+}
 // W_96 twiddles of this translation unit's copy of c_w96
 inline void init_w96() {
   static std::once_flag once;
@@ -1392,16 +1414,19 @@ inline void init_w96() {
 template <int E>
 void launch_wem_w(const DevCtx& c, const Group* g, int ng, float2* store, float2* bins, cudaStream_t st) {
   init_w96();
-  const int pass = wem16_fits<E>(c) ? 4 : 0;
+  const bool one = c.one_row && c.nref == 1;
+  const int pass = one ? 5 : (wem16_fits<E>(c) ? 4 : 0);
   const SlotLayout L = slot_layout<E>(c, pass, max_smem_per_block());
   const size_t sm = smem_w<E>(c, pass, L);
-  const int threads = (pass == 4 ? kRowsWem : kW) * 32;
+  const int threads = (pass == 5 ? 1 : (pass == 4 ? kRowsWem : kW)) * 32;
   auto go = [&](auto kern) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    set_max_smem(kern);
     kern<<<ng, threads, sm, st>>>(c, L, g, store, bins);
     note_launch();
   };
   if (c.nref > 1) go(kw_wem<E, true, false, kW>);
+  else if (pass == 5 && c.tap == 0) go(kw_wem<E, false, true, 1>);
+  else if (pass == 5) go(kw_wem<E, false, false, 1>);
   else if (pass == 4 && c.tap == 0) go(kw_wem<E, false, true, kRowsWem>);
   else if (pass == 4) go(kw_wem<E, false, false, kRowsWem>);
   else if (c.tap == 0) go(kw_wem<E, false, true, kW>);
@@ -1411,6 +1436,7 @@ void launch_wem_w(const DevCtx& c, const Group* g, int ng, float2* store, float2
 // rows per CTA the WEM launcher expects
 template <int E>
 int wem_rows_w(const DevCtx& c) {
+  if (c.one_row && c.nref == 1) return 1;
   return wem16_fits<E>(c) ? kRowsWem : kW;
 }
 
@@ -1421,7 +1447,7 @@ void launch_fwd_w(const DevCtx& c, const Group* g, int ng, const float2* dm, con
   const SlotLayout L = slot_layout<E>(c, 1, max_smem_per_block());
   const size_t sm = smem_w<E>(c, 1, L);
   auto go = [&](auto kern) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    set_max_smem(kern);
     kern<<<ng, kW * 32, sm, st>>>(c, L, g, dm, drm, sA, sB, bins);
     note_launch();
   };
@@ -1436,16 +1462,21 @@ void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* 
   const int limit = max_smem_per_block();
   if (adj2_fits<E>(c)) {
     // the two chains of a row on two warps, when their buffers, the full
-    // ring and every table of a depth fit
-    const SlotLayout L3 = slot_layout<E>(c, 3, limit);
+    // ring and every table of a depth fit; one-row CTAs when every group
+    // holds one row
+    const int pass = c.one_row ? 6 : 3;
+    const SlotLayout L3 = slot_layout<E>(c, pass, limit);
     {
-      const size_t sm3 = smem_w<E>(c, 3, L3);
+      const size_t sm3 = smem_w<E>(c, pass, L3);
+      const int threads = 2 * (pass == 6 ? 1 : kRowsAdj2) * 32;
       auto go = [&](auto kern) {
-        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm3);
-        kern<<<ng, 2 * kRowsAdj2 * 32, sm3, st>>>(c, L3, g, sBG, sT, sG, bins, ir, is, compat);
+        set_max_smem(kern);
+        kern<<<ng, threads, sm3, st>>>(c, L3, g, sBG, sT, sG, bins, ir, is, compat);
         note_launch();
       };
-      if (c.tap == 0) go(kw_born_adj2<E, true, kRowsAdj2>);
+      if (pass == 6 && c.tap == 0) go(kw_born_adj2<E, true, 1>);
+      else if (pass == 6) go(kw_born_adj2<E, false, 1>);
+      else if (c.tap == 0) go(kw_born_adj2<E, true, kRowsAdj2>);
       else go(kw_born_adj2<E, false, kRowsAdj2>);
       return;
     }
@@ -1453,7 +1484,7 @@ void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* 
   const SlotLayout L = slot_layout<E>(c, 2, limit);
   const size_t sm = smem_w<E>(c, 2, L);
   auto go = [&](auto kern) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    set_max_smem(kern);
     kern<<<ng, kW * 32, sm, st>>>(c, L, g, sBG, sT, bins, ir, is, compat);
     note_launch();
   };
@@ -1464,7 +1495,8 @@ void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* 
 // rows per CTA the Born adjoint launcher expects
 template <int E>
 int adj_rows_w(const DevCtx& c) {
-  return adj2_fits<E>(c) ? kRowsAdj2 : kW;
+  if (!adj2_fits<E>(c)) return kW;
+  return c.one_row ? 1 : kRowsAdj2;
 }
 // the Born adjoint reuses step spectra in its scatters (and then needs the
 // third stored field of filtered spectra)
