@@ -1455,6 +1455,23 @@ void launch_fwd_w(const DevCtx& c, const Group* g, int ng, const float2* dm, con
   else go(kw_born_fwd<E, false>);
 }
 
+// the two-warp Born adjoint with one-row CTAs (every group holds one row);
+// instantiated in its own translation unit (kw_e<E>_adj1.cu)
+template <int E>
+void launch_adj2_one(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* sT, float2* sG, float2* bins,
+                     float2* ir, float2* is, int compat, cudaStream_t st) {
+  init_w96();
+  const SlotLayout L6 = slot_layout<E>(c, 6, max_smem_per_block());
+  const size_t sm6 = smem_w<E>(c, 6, L6);
+  auto go = [&](auto kern) {
+    set_max_smem(kern);
+    kern<<<ng, 2 * 32, sm6, st>>>(c, L6, g, sBG, sT, sG, bins, ir, is, compat);
+    note_launch();
+  };
+  if (c.tap == 0) go(kw_born_adj2<E, true, 1>);
+  else go(kw_born_adj2<E, false, 1>);
+}
+
 template <int E>
 void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* sT, float2* sG, float2* bins,
                   float2* ir, float2* is, int compat, cudaStream_t st) {
@@ -1462,24 +1479,21 @@ void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* 
   const int limit = max_smem_per_block();
   if (adj2_fits<E>(c)) {
     // the two chains of a row on two warps, when their buffers, the full
-    // ring and every table of a depth fit; one-row CTAs when every group
-    // holds one row
-    const int pass = c.one_row ? 6 : 3;
-    const SlotLayout L3 = slot_layout<E>(c, pass, limit);
-    {
-      const size_t sm3 = smem_w<E>(c, pass, L3);
-      const int threads = 2 * (pass == 6 ? 1 : kRowsAdj2) * 32;
-      auto go = [&](auto kern) {
-        set_max_smem(kern);
-        kern<<<ng, threads, sm3, st>>>(c, L3, g, sBG, sT, sG, bins, ir, is, compat);
-        note_launch();
-      };
-      if (pass == 6 && c.tap == 0) go(kw_born_adj2<E, true, 1>);
-      else if (pass == 6) go(kw_born_adj2<E, false, 1>);
-      else if (c.tap == 0) go(kw_born_adj2<E, true, kRowsAdj2>);
-      else go(kw_born_adj2<E, false, kRowsAdj2>);
+    // ring and every table of a depth fit
+    if (c.one_row) {
+      launch_adj2_one<E>(c, g, ng, sBG, sT, sG, bins, ir, is, compat, st);
       return;
     }
+    const SlotLayout L3 = slot_layout<E>(c, 3, limit);
+    const size_t sm3 = smem_w<E>(c, 3, L3);
+    auto go = [&](auto kern) {
+      set_max_smem(kern);
+      kern<<<ng, 2 * kRowsAdj2 * 32, sm3, st>>>(c, L3, g, sBG, sT, sG, bins, ir, is, compat);
+      note_launch();
+    };
+    if (c.tap == 0) go(kw_born_adj2<E, true, kRowsAdj2>);
+    else go(kw_born_adj2<E, false, kRowsAdj2>);
+    return;
   }
   const SlotLayout L = slot_layout<E>(c, 2, limit);
   const size_t sm = smem_w<E>(c, 2, L);

@@ -1,0 +1,7 @@
+// Warp-per-row Born adjoint with one-row CTAs for N = 32 x 24 = 768.
+#include "kernels_w.cuh"
+
+namespace wg {
+template void launch_adj2_one<24>(const DevCtx&, const Group*, int, float2*, float2*, float2*, float2*, float2*,
+                                   float2*, int, cudaStream_t);
+}  // namespace wg

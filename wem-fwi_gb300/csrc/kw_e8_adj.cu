@@ -2,6 +2,9 @@
 #include "kernels_w.cuh"
 
 namespace wg {
+// the one-row kernels are built in kw_e8_adj1.cu
+extern template void launch_adj2_one<8>(const DevCtx&, const Group*, int, float2*, float2*, float2*, float2*,
+                                          float2*, float2*, int, cudaStream_t);
 template void launch_adj_w<8>(const DevCtx&, const Group*, int, float2*, float2*, float2*, float2*, float2*,
                                 float2*, int, cudaStream_t);
 template bool adj_reuse_w<8>(const DevCtx&, int);
