@@ -38,6 +38,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "FWI gradient s/iter & depth-steps/s, batched+adjoint vs plain GPU at L2<=1e-4"
 PASSES_WEM = 2       # Down + Up (wem_prop.cpp:57,68)
+PASSES_BORN_FWD = 9   # born_prop.cpp:75-113
 PASSES_BORN_ADJ = 10  # born_prop.cpp:190-215: 1 down, 3 Up^H, 2 Down^H, 2 LinDown^H, 1 up, 1 LinUp^H
 
 
@@ -395,6 +396,88 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_config(args):
+    """The other configurations, timed for the record (not the contract
+    line): c1 = WEM forward + Born adjoint (migration) of one shot; c2 = Born
+    forward and Born adjoint (exact, with its dot test) of 48 shots.  GPU
+    times are CUDA events around each call on resident inputs; the CPU
+    restatement is timed on one shot (c1 all of it) with every host thread."""
+    import torch
+    import wemgpu
+    from wemgpu import synthetic as S
+    from wemgpu.core import BornOp, WemOp
+    from oracle import oracle as O
+
+    wemgpu.build()
+    dev = torch.device("cuda:0")
+    par = {"adjoint_mode": "exact"} if args.workload == "c2" else {}
+    cfg = S.CONFIGS[args.workload]()
+    cfg["par"] = dict(cfg["par"], **par)
+    p = S.params_of(cfg)
+    wav = cfg["wavelet"]
+    s = torch.from_numpy(cfg["slow"]).to(dev)
+    rho = torch.from_numpy(cfg["rho"]).to(dev)
+    nf = WemOp(p, wav).nfreq()
+    d = torch.zeros((p.ns, p.nr, p.nt), dtype=torch.float32, device=dev)
+    g0, g1 = torch.zeros_like(s), torch.zeros_like(s)
+    born = BornOp(p, wav, s, rho)
+    if args.workload == "c1":
+        wem = WemOp(p, wav)
+        ops = {"wem_forward": (lambda: wem.forward(s, rho, d), PASSES_WEM),
+               "born_adjoint": (lambda: born.adjoint(g0, g1, d), PASSES_BORN_ADJ)}
+    else:
+        ds = torch.from_numpy(cfg["dslow"]).to(dev)
+        dr = torch.from_numpy(cfg["drho"]).to(dev)
+        ops = {"born_forward": (lambda: born.forward(ds, dr, d), PASSES_BORN_FWD),
+               "born_adjoint": (lambda: born.adjoint(g0, g1, d), PASSES_BORN_ADJ)}
+    out = {"workload": args.workload, "nx": p.nx, "nz": p.nz, "shots": p.ns, "freqs": nf,
+           "fft_n": p.nx + 2 * (p.pad + p.tap), "prop": "pspi" if p.prop else "ssf", "nref": p.nref, "ops": {}}
+    for name, (fn, passes) in ops.items():
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.steps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / args.steps
+        steps = passes * p.ns * nf * (p.nz - 1)
+        out["ops"][name] = {"ms": ms, "depth_steps_per_s": steps / (ms / 1e3), "passes": passes}
+    if args.workload == "c2":
+        # dot test of the exact adjoint at full size (d = L n keeps both
+        # inner products away from cancellation)
+        rng = np.random.default_rng(5)
+        cplx = lambda sc: torch.from_numpy((sc * (rng.standard_normal(s.shape) + 1j * rng.standard_normal(s.shape))).astype(np.complex64)).to(dev)
+        m0, m1, n0, n1 = cplx(1e-7), cplx(1e-2), cplx(1e-7), cplx(1e-2)
+        dn, lm = torch.zeros_like(d), torch.zeros_like(d)
+        born.forward(n0 + 0.5 * m0, n1 + 0.5 * m1, dn)
+        born.forward(m0, m1, lm)
+        born.adjoint(g0, g1, dn)
+        lhs = float(torch.sum(dn.double() * lm.double()))
+        z = lambda a: a.to(torch.complex128)
+        rhs = float((z(g0).conj() * z(m0)).sum().real + (z(g1).conj() * z(m1)).sum().real)
+        out["dot_ratio"] = abs(lhs - rhs) / abs(lhs)
+    if not args.no_cpu:
+        O.build()
+        nt = os.cpu_count() or 1
+        one = dict(cfg, par=dict(cfg["par"], ns=1))
+        p1 = S.params_of(one)
+        t0 = time.perf_counter()
+        if args.workload == "c1":
+            syn = O.wem_forward(p1, wav, cfg["slow"], cfg["rho"], kind=0, nthreads=nt)
+            passes = PASSES_WEM + PASSES_BORN_ADJ
+        else:
+            syn = O.born_forward(p1, wav, cfg["slow"], cfg["rho"], cfg["dslow"], cfg["drho"], kind=0, nthreads=nt)
+            passes = PASSES_BORN_FWD + PASSES_BORN_ADJ
+        O.born_adjoint(p1, wav, cfg["slow"], cfg["rho"], syn, kind=0, nthreads=nt, fchunks=nt)
+        dt = time.perf_counter() - t0
+        out["cpu_oracle"] = {"s_one_shot": dt, "depth_steps_per_s": passes * nf * (p.nz - 1) / dt,
+                             "cores": nt, "kind": "port"}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -406,7 +489,12 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3"],
+                    help="c3 is the benchmark line; c1 and c2 print their own timings for the record")
     args = ap.parse_args()
+    if args.workload != "c3":
+        run_config(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
