@@ -121,11 +121,11 @@ def workload(small=False, small_shots=8):
 
 
 # DRAM bytes (read + write) per (row, depth) of the pass kernels, from ncu
-# captures of the reduced case (8 shots x 21 frequencies, nz 300, N 768;
-# profiles/kw_born_adj2_e24_c3_small.md): the traffic of a launch scales with
-# the rows it carries, so a full launch is this figure x rows x depths.
+# captures of the reduced case (16 shots x 21 frequencies, nz 300, N 768;
+# profiles/kw_born_adj2_e24_c3_small16.md): the traffic of a launch scales
+# with the rows it carries, so a full launch is this figure x rows x depths.
 TRAFFIC_PER_ROW_DEPTH = {
-    "k_born_adj": (1014829999 + 1006327999) / (168 * 300),
+    "k_born_adj": (1950111e3 + 2011472e3) / (336 * 300),
 }
 
 
