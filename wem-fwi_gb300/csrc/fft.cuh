@@ -19,8 +19,32 @@
 
 namespace wg {
 
-__host__ __device__ inline float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__host__ __device__ inline float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add and subtract issue as one paired FP32 instruction on sm_100 and
+// later (add/sub .f32x2: both components in one instruction, each rounded as
+// the scalar operation), halving the issue slots of the transforms'
+// butterflies.
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
+#define WG_F32X2 1
+#endif
+__host__ __device__ inline float2 c_add(float2 a, float2 b) {
+#ifdef WG_F32X2
+  return __fadd2_rn(a, b);
+#else
+  return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+__host__ __device__ inline float2 c_sub(float2 a, float2 b) {
+#ifdef WG_F32X2
+  float2 r;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(r.x), "=f"(r.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return r;
+#else
+  return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
 __host__ __device__ inline float2 c_mul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -44,7 +68,10 @@ __device__ inline void dft2(float2* v) {
 
 __device__ inline void dft4(float2* v, bool inv) {
   float2 s0 = c_add(v[0], v[2]), d0 = c_sub(v[0], v[2]);
-  float2 s1 = c_add(v[1], v[3]), d1 = c_rot(c_sub(v[1], v[3]), inv);
+  // d1 = -i (v1 - v3) (fwd) or +i (v1 - v3) (inv), formed from two scalar
+  // differences so that it lands as a pair for the paired adds below
+  float2 s1 = c_add(v[1], v[3]);
+  float2 d1 = inv ? make_float2(v[3].y - v[1].y, v[1].x - v[3].x) : make_float2(v[1].y - v[3].y, v[3].x - v[1].x);
   v[0] = c_add(s0, s1);
   v[2] = c_sub(s0, s1);
   v[1] = c_add(d0, d1);
@@ -56,7 +83,11 @@ __device__ inline void dft3(float2* v, bool inv) {
   float2 t = c_add(v[1], v[2]);
   float2 d = c_sub(v[1], v[2]);
   float2 y0 = c_add(v[0], t);
+#ifdef WG_F32X2
+  float2 m = __ffma2_rn(t, make_float2(c, c), v[0]);
+#else
   float2 m = make_float2(v[0].x + c * t.x, v[0].y + c * t.y);
+#endif
   // s * i * d
   float2 r = make_float2(-s * d.y, s * d.x);
   v[0] = y0;
