@@ -52,6 +52,14 @@ __host__ __device__ inline float2 c_mul(float2 a, float2 b) {
 __host__ __device__ inline float2 c_mulc(float2 a, float2 b) {
   return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
+// acc + a b and acc + a conj(b) as four fused multiply-adds (the paired add
+// above would otherwise stop the accumulation from contracting)
+__host__ __device__ inline float2 c_fma(float2 acc, float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, fmaf(-a.y, b.y, acc.x)), fmaf(a.x, b.y, fmaf(a.y, b.x, acc.y)));
+}
+__host__ __device__ inline float2 c_fmac(float2 acc, float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, acc.x)), fmaf(a.y, b.x, fmaf(-a.x, b.y, acc.y)));
+}
 __host__ __device__ inline float2 c_conj(float2 a) { return make_float2(a.x, -a.y); }
 __host__ __device__ inline float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 // multiply by -i (fwd) or +i (inv)

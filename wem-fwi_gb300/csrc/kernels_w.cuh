@@ -952,7 +952,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
               const int x = xclamp(w, j, in);
               const float2 k0 = T.c0[x], k1 = t1 ? T.c1[x] : zero, u = tp[x];
               const float2 v = sc_val(iw, scmode, t1, k0, k1, u, X[j]);
-              if (in) slot[x] = c_add(slot[x], c_mulc(v, bu[j]));
+              if (in) slot[x] = c_fmac(slot[x], v, bu[j]);
             }
           }
         }
@@ -964,7 +964,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
           for (int j = 0; j < E; ++j) {
             bool in;
             const float2 r = T.rc[xclamp(w, j, in)];
-            if (in) wd[j] = c_add(wd[j], c_mulc(X[j], r));
+            if (in) wd[j] = c_fmac(wd[j], X[j], r);
           }
           if (!c.no_fwd_record) w_inject_rec<E>(w, wd, s, bin, z - 1, bins);
         } else if (k == 2) {
@@ -978,7 +978,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
             bool in;
             const int x = xclamp(w, j, in);
             const float2 r = Tp.rc[x], b = bgp[x];
-            if (in) bu[j] = c_add(bu[j], c_mul(r, b));
+            if (in) bu[j] = c_fma(bu[j], r, b);
           }
         }
       }

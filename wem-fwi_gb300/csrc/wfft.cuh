@@ -39,6 +39,22 @@ __device__ __forceinline__ float2 wr(int k, bool inv) {
   return inv ? make_float2(w.x, -w.y) : w;
 }
 
+// x W_R^k (conjugate twiddle for INV): the powers -1 and -+i are a negation
+// or a swap, with no multiplication; the others come from the table.  k is a
+// compile-time constant after unrolling, so the switch folds away.
+template <int R, bool INV>
+__device__ __forceinline__ float2 tw_mul(float2 x, int k) {
+  int e = (k % R) * (96 / R);  // exponent in units of 2 pi / 96
+  if (INV) e = (96 - e) % 96;
+  switch (e) {
+    case 0: return x;
+    case 24: return make_float2(x.y, -x.x);   // -i
+    case 48: return make_float2(-x.x, -x.y);  // -1
+    case 72: return make_float2(-x.y, x.x);   // +i
+    default: return c_mul(x, wr<R>(k, INV));
+  }
+}
+
 // ------------------------------------------------ in-register small DFTs
 template <int R, bool INV>
 struct Dft;
@@ -77,7 +93,7 @@ struct Dft {
     for (int k = 0; k < M; ++k) {
       float2 a[P];
 #pragma unroll
-      for (int q = 0; q < P; ++q) a[q] = (q * k == 0) ? sub[q][k] : c_mul(sub[q][k], wr<R>(q * k, INV));
+      for (int q = 0; q < P; ++q) a[q] = tw_mul<R, INV>(sub[q][k], q * k);
       Dft<P, INV>::run(a);
 #pragma unroll
       for (int r = 0; r < P; ++r) v[k + M * r] = a[r];
