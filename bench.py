@@ -125,7 +125,7 @@ def workload(small=False, small_shots=8):
 # profiles/kw_born_adj2_e24_c3_small16.md): the traffic of a launch scales
 # with the rows it carries, so a full launch is this figure x rows x depths.
 TRAFFIC_PER_ROW_DEPTH = {
-    "k_born_adj": (1950111e3 + 2011472e3) / (336 * 300),
+    "k_born_adj": (1948976e3 + 2011706e3) / (336 * 300),
 }
 
 
