@@ -704,6 +704,9 @@ __global__ void k_phase(DevCtx c, const float2* sref, float eps, float2* ph) {
 
 // SSF per-point factor: taper / N * exp(-i w dz q) (SplitStep.cpp:13-14).
 // One CTA row per (frequency, depth) table row, threads over the points.
+// w dz is carried as an unevaluated float pair hi + lo (lo the FMA-exact
+// error of the float product), so the phase w dz q is the float rounding of
+// the exact product with FP32 operations only (FP64 issues slowly here).
 __global__ void k_fac(DevCtx c, const float2* q, float2* fac) {
   const int nrow = c.nfreq * c.nz;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -716,10 +719,10 @@ __global__ void k_fac(DevCtx c, const float2* q, float2* fac) {
     float2 out = zero2();
     if (c.ref[qi] >= 0) {
       const float2 qq = q[qi];
-      const double wdz = (double)c.omega[f] * c.dz;
-      const float amp = expf((float)(wdz * qq.y)) * tp;
+      const float w = c.omega[f], hi = w * c.dz, lo = fmaf(w, c.dz, -hi);
+      const float amp = expf(fmaf(hi, qq.y, lo * qq.y)) * tp;
       float sn, cs;
-      sincosf((float)(wdz * qq.x), &sn, &cs);
+      sincosf(fmaf(hi, qq.x, lo * qq.x), &sn, &cs);
       out = make_float2(amp * cs, -amp * sn);
     }
     fac[(size_t)r * c.nxg + x] = out;
