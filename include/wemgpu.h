@@ -157,6 +157,13 @@ int wem_set_plain(int plain);
  * supported). */
 int wem_set_kernel_path(int path);
 
+/* Rows per CTA of the single-reference warp-per-row kernels (no counterpart
+ * in the reference: launch shape).  0 automatic (one row per CTA when a pass
+ * has no more (shot, frequency) rows than the GPU has SMs, rows of a
+ * frequency grouped per CTA otherwise), 1 grouped rows, 2 one row per CTA.
+ * Results do not depend on it beyond float rounding of the image sums. */
+int wem_set_row_ctas(int mode);
+
 /* ------------------------------------------------ nonlinear modelling (WEM) */
 typedef struct wem_handle wem_handle;
 

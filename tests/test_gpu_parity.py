@@ -234,9 +234,25 @@ def kernel_path(gpu_lib, request):
     _lib.call("wem_set_kernel_path", 0)
 
 
+@pytest.fixture
+def row_ctas(gpu_lib, request):
+    """Rows per CTA of the single-reference warp kernels: 1 grouped rows of a
+    frequency, 2 one row per CTA (0 automatic: one-row CTAs when a pass has
+    no more rows than SMs, which every small case here has)."""
+    from wemgpu import _lib
+    _lib.call("wem_set_row_ctas", request.param)
+    yield request.param
+    _lib.call("wem_set_row_ctas", 0)
+
+
+ROWS = [pytest.param(1, id="grouped"), pytest.param(2, id="onerow")]
+
+
 @pytest.mark.parametrize("case", list(WARP_CASES))
-@pytest.mark.parametrize("kernel_path", [0, 1], indirect=True)
-def test_paths_wem_and_born(gpu_lib, oracle, case, kernel_path):
+@pytest.mark.parametrize("kernel_path,row_ctas", [pytest.param(0, 1, id="warp-grouped"),
+                                                  pytest.param(0, 2, id="warp-onerow"),
+                                                  pytest.param(1, 0, id="smem")], indirect=True)
+def test_paths_wem_and_born(gpu_lib, oracle, case, kernel_path, row_ctas):
     from wemgpu.core import BornOp, WemOp
     kw = WARP_CASES[case]
     for mode in ("compat", "exact"):
@@ -264,7 +280,8 @@ def test_paths_wem_and_born(gpu_lib, oracle, case, kernel_path):
 
 
 @pytest.mark.parametrize("case", ["n768t0", "n256"])
-def test_born_adjoint_many_shots(gpu_lib, oracle, case):
+@pytest.mark.parametrize("row_ctas", ROWS, indirect=True)
+def test_born_adjoint_many_shots(gpu_lib, oracle, case, row_ctas):
     """More shots than rows per CTA: full and partial groups of one frequency."""
     from wemgpu.core import BornOp
     p, par, wav, s, rho = small_case(nz=12, ns=11, **WARP_CASES[case])
@@ -350,7 +367,8 @@ def test_exact_kz_phase_law(gpu_lib, oracle, case):
 
 @pytest.mark.parametrize("case", ["small", "n256", "n768t0"])
 @pytest.mark.parametrize("mode", ["compat", "exact"])
-def test_bornrefl_borntomo(gpu_lib, oracle, case, mode):
+@pytest.mark.parametrize("row_ctas", ROWS, indirect=True)
+def test_bornrefl_borntomo(gpu_lib, oracle, case, mode, row_ctas):
     """BornRefl / BornTomo (ext_born_refl.cpp, ext_born_tomo.cpp) on the Born
     passes against the oracle."""
     from wemgpu.core import BornReflOp, BornTomoOp
@@ -385,7 +403,8 @@ def test_bornrefl_borntomo(gpu_lib, oracle, case, mode):
 
 @pytest.mark.parametrize("case", ["n768t0", "n512t0p"])
 @pytest.mark.parametrize("mode", ["compat", "exact"])
-def test_ext_born_warp_tap0(gpu_lib, oracle, case, mode):
+@pytest.mark.parametrize("row_ctas", ROWS, indirect=True)
+def test_ext_born_warp_tap0(gpu_lib, oracle, case, mode, row_ctas):
     """Frequency-extended Born on the warp kernels at tap 0: per-frequency
     tables, the spectral reuse of the as-coded adjoint and the extended
     last-row rule (one shot's LinUp^H term)."""
@@ -441,7 +460,8 @@ def test_bornrefl_borntomo_shared_memory_path(gpu_lib, oracle, kw):
 
 @pytest.mark.parametrize("kw", [dict(), dict(nx=240, pad=4, tap=4), dict(nx=768, pad=0, tap=0)])
 @pytest.mark.parametrize("nz,ns", [(2, 1), (3, 1), (5, 9)])
-def test_small_geometries(gpu_lib, oracle, kw, nz, ns):
+@pytest.mark.parametrize("row_ctas", ROWS, indirect=True)
+def test_small_geometries(gpu_lib, oracle, kw, nz, ns, row_ctas):
     """Smallest depth axes (one step), one shot and more shots than rows per
     CTA, on the shared-memory kernels (N = 72) and the warp kernels (256, 768)."""
     from wemgpu.core import BornOp, WemOp

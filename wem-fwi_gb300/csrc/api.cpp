@@ -36,6 +36,7 @@ struct KStat {
 bool g_stats_on = false;
 bool g_plain = false;
 int g_path = 0;  // 0 automatic, 1 shared-memory kernels, 2 warp-per-row kernels
+int g_rows = 0;  // 0 automatic, 1 grouped rows per CTA, 2 one-row CTAs
 std::vector<std::pair<std::string, KStat>> g_stats;
 
 std::mutex g_stats_mu;  // engines may run on several host threads
@@ -334,6 +335,20 @@ class Engine {
 
   int warp_G(int which) const { return g_plain ? 1 : std::min(geo_.ns, warp_rows_per_group(ctx_, which)); }
 
+  // Rows per CTA of the single-reference warp kernels.  A launch with no
+  // more (shot, frequency) rows than the GPU has SMs runs one row per CTA,
+  // so the rows spread over as many SMs as there are rows instead of
+  // sharing a few grouped CTAs; larger launches group rows of a frequency.
+  // The shots of a conformal-map operator always run one-row CTAs.
+  void pick_row_ctas() {
+    if (map_) return;
+    int dev = 0, sms = 0;
+    cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
+    cuda_check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    const long long rows = (long long)F_ * geo_.ns;
+    ctx_.one_row = g_rows == 2 ? 1 : (g_rows == 1 ? 0 : (rows <= sms ? 1 : 0));
+  }
+
   void wem_forward(const void* s2, const void* rho, void* data, int kind, int add) {
     if (!shots_.empty()) {
       require(s2 && rho && data, "NULL argument");
@@ -354,6 +369,7 @@ class Engine {
   void wem_pass() {
     const size_t plane = (size_t)p_.nz * geo_.nxg;
     const bool wp = warp_path();
+    if (wp) pick_row_ctas();
     int G = wp ? warp_G(0) : pick_G([&](int g) { return smem_wem(ctx_, g); });
     for_chunks(G, plane * 8, [&](const Group* gd, int ng, int rows) {
       float2* A = ws_->store1.as<float2>((size_t)rows * plane);
@@ -564,6 +580,7 @@ class Engine {
     cuda_check(cudaMemsetAsync(IR, 0, (size_t)M_img_ * plane * 8, 0), "memset");
     cuda_check(cudaMemsetAsync(IS, 0, (size_t)M_img_ * plane * 8, 0), "memset");
     const bool wp = warp_path();
+    if (wp) pick_row_ctas();
     int G = wp ? warp_G(2) : pick_G([&](int g) { return smem_born_adj(ctx_, g); });
     const int compat = p_.adjoint_mode == WEM_ADJ_COMPAT ? 1 : 0;
     const bool reuse = wp && !g_plain && warp_adj_reuse(ctx_, compat);
@@ -1297,6 +1314,12 @@ int wem_set_kernel_path(int path) {
   return guard([&] {
     require(path >= 0 && path <= 2, "path must be 0, 1 or 2");
     g_path = path;
+  });
+}
+int wem_set_row_ctas(int mode) {
+  return guard([&] {
+    require(mode >= 0 && mode <= 2, "mode must be 0, 1 or 2");
+    g_rows = mode;
   });
 }
 int wem_set_plain(int plain) {
