@@ -127,6 +127,15 @@ def workload(small=False, small_shots=8):
 TRAFFIC_PER_ROW_DEPTH = {
     "k_born_adj": (1948976e3 + 2011706e3) / (336 * 300),
 }
+# warp instructions per (row, depth) of the pass kernels (smsp__inst_executed
+# of the same captures; profiles/kw_wem_e24_c3_small16.md for k_wem): the
+# pass kernels are bound by instruction issue, so the line also reports the
+# issue rate they reach against one warp instruction per SM sub-partition
+# per cycle
+INST_PER_ROW_DEPTH = {
+    "k_born_adj": 1392862707 / (336 * 300),
+    "k_wem": 420063462 / (336 * 300),
+}
 
 
 def config_of(p, nf, world, small):
@@ -234,6 +243,18 @@ def run_gpu(args, rank, world):
     traffic = None
     if top in TRAFFIC_PER_ROW_DEPTH:
         traffic = TRAFFIC_PER_ROW_DEPTH[top] * p.ns * nf * p.nz
+    clocks = clk.summary()
+    issue = None
+    if top in INST_PER_ROW_DEPTH:
+        mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+        if mhz:
+            sms = torch.cuda.get_device_properties(dev).multi_processor_count
+            inst = INST_PER_ROW_DEPTH[top] * p.ns * nf * p.nz
+            rate = inst / (top_ms / top_n / 1e3)
+            peak_issue = sms * 4 * mhz * 1e6
+            issue = {"kernel": top, "warp_inst_per_launch": inst, "achieved_ginst_s": rate / 1e9,
+                     "peak_ginst_s": peak_issue / 1e9, "frac": rate / peak_issue,
+                     "source": "instructions per row-depth from the ncu capture, sm clock sampled live"}
 
     # end to end through the public FWI call (wemgpu.autograd.FwiObjective):
     # each step copies the model in from pinned host memory and the loss and
@@ -322,12 +343,13 @@ def run_gpu(args, rank, world):
                              "api": "WemOp/BornOp with numpy host arrays, residual on the host"},
         "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
-                     "algorithmic_bytes": algo, "ms_per_launch": top_ms / top_n, "traffic": traffic},
+                     "algorithmic_bytes": algo, "ms_per_launch": top_ms / top_n, "traffic": traffic,
+                     "issue": issue},
         "kernels": {k: {"ms": v[0] / args.steps, "launches": v[1] // args.steps} for k, v in kstats.items()},
         "gpu_launches": gpu_launches,
         "plain_gpu": plain,
         "cpu_baseline": cpu,
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
