@@ -435,6 +435,9 @@ def run_config(args):
     par = {"adjoint_mode": "exact"} if args.workload == "c2" else {}
     cfg = S.CONFIGS[args.workload]()
     cfg["par"] = dict(cfg["par"], **par)
+    if args.small:  # a reduced case of the same kernels for profiling captures
+        f0 = cfg["par"]["fmin"]
+        cfg["par"] = dict(cfg["par"], ns=min(cfg["par"]["ns"], args.small_shots), fmax=f0 + 2.0)
     p = S.params_of(cfg)
     wav = cfg["wavelet"]
     s = torch.from_numpy(cfg["slow"]).to(dev)
@@ -452,7 +455,7 @@ def run_config(args):
         dr = torch.from_numpy(cfg["drho"]).to(dev)
         ops = {"born_forward": (lambda: born.forward(ds, dr, d), PASSES_BORN_FWD),
                "born_adjoint": (lambda: born.adjoint(g0, g1, d), PASSES_BORN_ADJ)}
-    out = {"workload": args.workload, "nx": p.nx, "nz": p.nz, "shots": p.ns, "freqs": nf,
+    out = {"workload": args.workload, "small": bool(args.small), "nx": p.nx, "nz": p.nz, "shots": p.ns, "freqs": nf,
            "fft_n": p.nx + 2 * (p.pad + p.tap), "prop": "pspi" if p.prop else "ssf", "nref": p.nref, "ops": {}}
     for name, (fn, passes) in ops.items():
         for _ in range(max(args.warmup, 1)):
