@@ -210,6 +210,15 @@ __device__ __forceinline__ void w_zero(float2 (&v)[E]) {
 // the reference loop of SSF.cpp / PSPI.cpp around the transform pair; the
 // single-reference kernels are instantiated without it.
 
+// A row of 32 E points in shared memory in the registers' layout (lane t
+// holds points t + 32 j): the several-reference kernels keep the sum over
+// references here instead of in registers.  Each lane reads and writes only
+// its own points, so no synchronisation is needed.
+struct SRow {
+  float2* p;  // this lane's point j = 0
+  __device__ __forceinline__ float2& operator[](int j) const { return p[32 * j]; }
+};
+
 // forward step, mid: X *= phase row of reference jr (SSF.cpp:18-23, PSPI.cpp:15-20)
 template <int E>
 __device__ __forceinline__ void fwd_mid(const WRow& w, const Tabs& T, int jr, float2 (&X)[E]) {
@@ -223,8 +232,8 @@ __device__ __forceinline__ void fwd_mid(const WRow& w, const Tabs& T, int jr, fl
 // split-step table is zero where a point has no reference, so the index is
 // only read without it (PSPI).  MR: o keeps its value at other points and is
 // cleared at jr = 0.
-template <int E, bool MR>
-__device__ __forceinline__ void fwd_post(const WRow& w, const Tabs& T, int jr, const float2 (&X)[E], float2 (&o)[E]) {
+template <int E, bool MR, class O>
+__device__ __forceinline__ void fwd_post(const WRow& w, const Tabs& T, int jr, const float2 (&X)[E], O&& o) {
   const float2 zero = make_float2(0.f, 0.f);
 #pragma unroll
   for (int j = 0; j < E; ++j) {
@@ -276,8 +285,8 @@ __device__ __forceinline__ void adj_pre(const WRow& w, const Tabs& T, int jr, co
 // adjoint step, mid: X *= conj(phase row jr); MR sums the references'
 // spectra in Y and returns true once X holds the sum (the inverse transform
 // runs after the last reference only)
-template <int E, bool MR>
-__device__ __forceinline__ bool adj_mid(const WRow& w, const Tabs& T, int jr, float2 (&X)[E], float2 (&Y)[MR ? E : 1]) {
+template <int E, bool MR, class YR>
+__device__ __forceinline__ bool adj_mid(const WRow& w, const Tabs& T, int jr, float2 (&X)[E], YR&& Y) {
   const float2* pj = T.ph + (size_t)jr * 32 * E;
   if constexpr (!MR) {
 #pragma unroll
@@ -441,6 +450,7 @@ struct Carve {
   char* ring;
   char* rows;
   float2* slots;
+  float2* yrow;  // several references: one row per warp for the sum over references
   __device__ Carve(const DevCtx& c, const SlotLayout& L, bool with_slots, int nbuf = kW, bool with_taper = true) {
     extern __shared__ float4 smem4[];
     char* p = reinterpret_cast<char*>(smem4);
@@ -456,7 +466,16 @@ struct Carve {
     ring = take((size_t)L.nslots * L.bytes);
     rows = take((size_t)2 * nbuf * L.row_bytes);
     slots = reinterpret_cast<float2*>(take(with_slots ? (size_t)kW * c.nxg * 8 : 0));
+    yrow = reinterpret_cast<float2*>(take(ysum_rows(c, with_slots) * 32 * E * 8));
   }
+  // rows of reference sums in shared memory: the several-reference modelling
+  // and Born forward; the Born adjoint (with image slots) keeps its sum in
+  // registers, since its shared memory is taken by the slots and the table
+  // ring (with the sum there too the ring no longer fits for N = 1024 and the
+  // pass ran 35 % slower)
+  __device__ static size_t ysum_rows(const DevCtx& c, bool with_slots) { return c.nref > 1 && !with_slots ? kW : 0; }
+  // this lane's view of warp `warp`'s reference-sum row
+  __device__ SRow ysum(int warp, int lane) const { return SRow{yrow + (size_t)warp * 32 * E + lane}; }
 };
 
 // twiddles in the per-stage layout of wfft.cuh (gathered from the natural
@@ -497,7 +516,7 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
   const Ring ring{c, L, sm.ring, Src{nullptr, nullptr}, f};
   float2* wrow = reinterpret_cast<float2*>(sm.rows + (size_t)warp * 2 * L.row_bytes);
   float2 W[E], X[E];
-  float2 Y[MR ? E : 1];
+  const SRow Y = sm.ysum(warp, lane);  // used by the several-reference instantiation only
   w_zero<E>(W);
   if (act) w_inject_src<E>(w, W, s, f, 0);
   ring.issue(0);
@@ -611,7 +630,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, SlotLayout L
   const Ring ring{c, L, sm.ring, Src{dm, drm}, f};
   const float2 zero = make_float2(0.f, 0.f);
   float2 bg[E], sd[E], X[E];
-  float2 Y[MR ? E : 1];
+  const SRow Y = sm.ysum(warp, lane);  // used by the several-reference instantiation only
   w_zero<E>(bg);
   w_zero<E>(sd);
   if (act) w_inject_src<E>(w, bg, s, f, 0);
@@ -783,7 +802,7 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
   const float2 zero = make_float2(0.f, 0.f);
   const Ring ring{c, L, sm.ring, Src{nullptr, nullptr}, f};
   float2 X[E];
-  float2 Y[MR ? E : 1];
+  float2 Y[MR ? E : 1];  // the sum over references (in registers: see Carve::ysum_rows)
   // ---------------- down sweep: bg (Down of the source) and wu (Up^H of the data)
   float2 bg[E], wu[E];
   w_zero<E>(bg);
@@ -1325,7 +1344,8 @@ size_t base_bytes(const DevCtx& c, int which) {
   auto r16 = [](size_t b) { return (b + 15) & ~size_t(15); };
   const int nbuf = nbuf_of(which);
   return r16((size_t)32 * E * 8) + r16((size_t)32 * E * 4) + (taper_of(c, which) ? r16((size_t)c.nxg * 4) : 0) +
-         r16((size_t)nbuf * wbuf_len<E>() * 8) + (which == 2 ? r16((size_t)kW * c.nxg * 8) : 0);
+         r16((size_t)nbuf * wbuf_len<E>() * 8) + (which == 2 ? r16((size_t)kW * c.nxg * 8) : 0) +
+         (c.nref > 1 && which != 2 ? r16((size_t)kW * 32 * E * 8) : 0);
 }
 
 // Lays out the ring (and the per-warp rows for WEM) and drops them when the
