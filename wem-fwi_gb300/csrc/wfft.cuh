@@ -21,7 +21,7 @@
 // (k = 4 for E = 8, 16; k = 5 for E = 12, 32), chosen by counting the
 // wavefronts of every exchange write and read of each plan; the natural-order
 // reads stay conflict-free and fold the padding into immediate offsets.
-// E = 24 uses rows of 24 points padded by one (rows_layout).
+// E = 24 uses blocks of two 24-point rows padded by one slot (rows_layout).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -140,19 +140,24 @@ template <int E>
 __device__ __forceinline__ int swz(int i) {
   return i + (i >> swz_shift<E>());
 }
-// E = 24 lays the exchange out as rows of E points padded by one slot
-// instead: every exchange address is then a per-butterfly base plus
-// compile-time offsets, and the stage-0 writes (stride E + 1) are free of
-// bank conflicts
+// E = 24 lays the exchange out instead in blocks of two rows of E points
+// (2 E = 48) padded by one slot: every exchange address is a per-butterfly
+// base plus compile-time offsets; the stage-0 writes (a lane's row starts
+// E slots after the previous lane's, or E + 1 across a block) are free of
+// bank conflicts, and so are the natural-order reads, whose 16-lane halves
+// never cross a block (48 is a multiple of 16).  Counting wavefronts of every
+// exchange access of a transform: 208 against 192 without conflicts (224 with
+// one pad slot per row of 24).
 template <int E>
 __host__ __device__ constexpr bool rows_layout() {
   return E == 24;
 }
 template <int E>
 __device__ __forceinline__ int xaddr(int i) {
-  if constexpr (rows_layout<E>()) return (i / E) * (E + 1) + i % E;
+  if constexpr (rows_layout<E>()) return (i / (2 * E)) * (2 * E + 1) + i % (2 * E);
   else return swz<E>(i);
 }
+// the buffer also holds a row in the swz layout (receiver records)
 template <int E>
 __host__ __device__ constexpr int wbuf_len() {
   return (rows_layout<E>() ? 32 * (E + 1) : 32 * E + ((32 * E) >> swz_shift<E>())) + 2;
@@ -198,12 +203,14 @@ __device__ __forceinline__ void wfft_stage(float2 (&v)[E], float2* sb, const flo
 #pragma unroll
       for (int q = 0; q < R; ++q) v[m + q * M] = a[q];
     } else if constexpr (rows_layout<E>()) {
-      // positions o + q L of one row (L = 1) or of rows L / E apart
-      static_assert(L == 1 || L % E == 0, "row layout needs L = 1 or a multiple of E");
-      constexpr int STEP = (L == 1) ? 1 : (L / E) * (E + 1);
+      // positions o + q L, o = (b - l) R + l: one row (L = 1; o is a
+      // multiple of E) or one point of each of R rows (L = E; o = l modulo
+      // 2 E, as (b - l) R is a multiple of 2 E), so position q lies
+      // q L + floor(q L / 2 E) slots after o's
+      static_assert(L == 1 || (L == E && ((E * R) % (2 * E)) == 0), "block layout: L = 1, or L = E with R even");
       const int a0 = xaddr<E>((b - l) * R + l);
 #pragma unroll
-      for (int q = 0; q < R; ++q) sb[a0 + q * STEP] = a[q];
+      for (int q = 0; q < R; ++q) sb[a0 + q * L + (q * L) / (2 * E)] = a[q];
     } else {
       const int o = (b - l) * R + l;
 #pragma unroll
@@ -214,10 +221,10 @@ __device__ __forceinline__ void wfft_stage(float2 (&v)[E], float2* sb, const flo
     __syncwarp();
     if constexpr (rows_layout<E>()) {
       // natural order, read per butterfly of the next stage: positions
-      // lane + 32 m + r 32 M2 lie 32 M2 / E rows apart
+      // lane + 32 m + r 32 M2 lie 32 M2 / 2 E whole blocks apart
       constexpr int R2 = WPlan<E>::r(S + 1), M2 = E / R2;
-      static_assert((32 * M2) % E == 0, "row layout needs 32 E / R2 to be a multiple of E");
-      constexpr int RSTEP = (32 * M2 / E) * (E + 1);
+      static_assert((32 * M2) % (2 * E) == 0, "block layout needs 32 M2 to be a multiple of 2 E");
+      constexpr int RSTEP = 32 * M2 + (32 * M2) / (2 * E);
 #pragma unroll
       for (int m = 0; m < M2; ++m) {
         const int base = xaddr<E>(lane + 32 * m);
