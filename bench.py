@@ -125,7 +125,7 @@ def workload(small=False, small_shots=8):
 # profiles/kw_born_adj2_e24_c3_small16.md): the traffic of a launch scales
 # with the rows it carries, so a full launch is this figure x rows x depths.
 TRAFFIC_PER_ROW_DEPTH = {
-    "k_born_adj": (1948976e3 + 2011706e3) / (336 * 300),
+    "k_born_adj": (1948216e3 + 2011339e3) / (336 * 300),
 }
 # warp instructions per (row, depth) of the pass kernels (smsp__inst_executed
 # of the same captures; profiles/kw_wem_e24_c3_small16.md for k_wem): the
@@ -133,8 +133,8 @@ TRAFFIC_PER_ROW_DEPTH = {
 # issue rate they reach against one warp instruction per SM sub-partition
 # per cycle
 INST_PER_ROW_DEPTH = {
-    "k_born_adj": 1392862707 / (336 * 300),
-    "k_wem": 420063462 / (336 * 300),
+    "k_born_adj": 1387956947 / (336 * 300),
+    "k_wem": 418853610 / (336 * 300),
 }
 
 
