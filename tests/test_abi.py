@@ -61,3 +61,12 @@ def test_invalid_parameters_are_rejected_on_host(lib, bad):
     with pytest.raises(WemError) as e:
         call("wem_create", ctypes.byref(p), wav.ctypes.data_as(ctypes.c_void_p), ctypes.byref(h))
     assert e.value.code == 1  # WEM_EINVAL, before any device call
+
+
+@pytest.mark.parametrize("fn,bad", [("wem_set_kernel_path", 3), ("wem_set_row_ctas", 3), ("wem_set_row_ctas", -1)])
+def test_launch_shape_knobs_validate_on_host(lib, fn, bad):
+    from wemgpu._lib import WemError, call
+    with pytest.raises(WemError) as e:
+        call(fn, bad)
+    assert e.value.code == 1  # WEM_EINVAL
+    call(fn, 0)  # the automatic choice is always accepted
