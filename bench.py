@@ -13,8 +13,11 @@ linearised pass of the reference's call sequence (2 passes for WEM forward,
 10 for the Born adjoint), so the figure is comparable with the reference's
 own work; ``s_per_iter`` = seconds per gradient; ``e2e`` = the same through
 the C ABI with host buffers (copies inside the timed region); ``roofline``
-for the dominant kernel from CUDA events on its launch stream;
-``cpu_baseline`` = the CPU restatement on the host cores on a bounded sample.
+for the dominant kernel from CUDA events on its launch stream, against HBM
+bandwidth and (``roofline.issue``) against the SM instruction issue rate
+that bounds it; ``cpu_baseline`` = the CPU restatement on the host cores on
+a bounded sample.  ``--workload c1|c2`` prints timings of the other
+configurations instead (not the benchmark line).
 
 ``--impl reference`` times the CPU restatement of the reference (the
 reference itself cannot be built: FFTW, TBB, Boost, SEP I/O and ISPC are
