@@ -150,6 +150,37 @@ def config_of(p, nf, world, small):
             "small": bool(small)}
 
 
+def rank_workload(cfg, rank, world):
+    """Rank's block of the weak-scaling survey: the workload's shots shifted
+    by rank / world of the shot interval (wemgpu.shard.interleave_par)."""
+    from wemgpu.shard import interleave_par
+    if world == 1:
+        return cfg
+    return dict(cfg, par=interleave_par(cfg["par"], world, rank))
+
+
+def reduce_gradients(g0, g1, world):
+    """The one exchange of a multi-rank gradient: both model gradients summed
+    over ranks (NCCL on the GPU arm; any backend the tensors' device has)."""
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(g0, op=dist.ReduceOp.SUM)
+        dist.all_reduce(g1, op=dist.ReduceOp.SUM)
+
+
+def relaunch(args):
+    """`--gpus N` outside torchrun: run the same command as N ranks under
+    torch.distributed.run on this node and return its exit status."""
+    import socket
+    sock = socket.socket()
+    sock.bind(("127.0.0.1", 0))
+    port = sock.getsockname()[1]
+    sock.close()
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__), *sys.argv[1:]]
+    return subprocess.call(cmd)
+
+
 def row_steps(p, nfreq):
     return (PASSES_WEM + PASSES_BORN_ADJ) * p.ns * nfreq * (p.nz - 1)
 
@@ -184,9 +215,10 @@ def run_gpu(args, rank, world):
     lib = _lib.load()
     dev = torch.device(f"cuda:{int(os.environ.get('LOCAL_RANK', 0))}")
     torch.cuda.set_device(dev)
-    cfg = workload(args.small, args.small_shots)
+    # weak scaling: every rank runs a block of the workload's size, its own
+    # shots of one survey of world x 32 shots
+    cfg = rank_workload(workload(args.small, args.small_shots), rank, world)
     p = S.params_of(cfg)
-    # weak scaling: every rank owns its own block of shots of the same size
     nf = WemOp(p, cfg["wavelet"]).nfreq()
     wav = cfg["wavelet"]
     s_true = torch.from_numpy(cfg["slow_true"]).to(dev)
@@ -203,8 +235,7 @@ def run_gpu(args, rank, world):
 
     def step():
         fwi.gradient(s0, rho, d_obs, g0, g1)
-        if world > 1:
-            torch.distributed.all_reduce(g0)
+        reduce_gradients(g0, g1, world)
         return g0
 
     for _ in range(args.warmup):
@@ -525,6 +556,12 @@ def main():
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.gpus < 1:
+        sys.exit("bench.py: --gpus must be at least 1")
+    if "WORLD_SIZE" not in os.environ and args.gpus > 1:
+        sys.exit(relaunch(args))
+    if args.gpus != world:
+        sys.exit(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={world}; launch one rank per GPU")
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if args.impl == "gpu" else "gloo")

@@ -344,15 +344,18 @@ int wem_dreflect(const void* slow2, const void* rho, int nx, int nz, int adj, vo
  * the library holds on every GPU that loads it, until the process exits.
  *   slow_row  padded slowness^2 of the depth, complex [nxg]
  *   sref      reference slownesses of the depth, complex [nref]
- *   refidx    reference of each point [nxg] (-1: none), e.g. one row of
- *             wemop_refsampler's table
+ *   refidx    reference of each point [nxg] in [-1, nref) (-1: none),
+ *             e.g. one row of wemop_refsampler's table; any other entry
+ *             counts as -1 (the point gets no reference)
  *   in, out   complex [nrow][nxg]; adj and add as wemop_onestep
+ * All five arrays must be memory of the current device (or managed).
  * Limits: N = nxg + 2 tap <= 4096 and nref <= 16 (WEM_EINVAL otherwise).
  * Every call reuses the same array, so calls that overlap on the GPU race:
  * serialise them.  The first call on a device looks the array up with
- * cudaGetSymbolAddress: make it before any stream capture.  The work is
- * queued on `stream` (a cudaStream_t, NULL for the default stream) and the
- * call returns without waiting for it. */
+ * cudaGetSymbolAddress: make it before any stream capture (and the first
+ * call after the device's context was reset, which looks it up again).
+ * The work is queued on `stream` (a cudaStream_t, NULL for the default
+ * stream) and the call returns without waiting for it. */
 int wemop_onestep_noalloc(const wem_params* p, const void* slow_row, const void* sref,
                           const signed char* refidx, int nxg, float freq, int adj,
                           const void* in, void* out, int nrow, int add, void* stream);

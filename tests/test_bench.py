@@ -52,3 +52,14 @@ def test_measured_per_row_constants(bench, c3):
     assert abs(traffic / bench.algorithmic_bytes("k_born_adj", p, 96, 8) - 1) < 0.05
     for k in ("k_born_adj", "k_wem"):
         assert bench.INST_PER_ROW_DEPTH[k] > 1000
+
+
+def test_gpus_flag_must_match_the_ranks():
+    """--gpus N under a launcher with another world size is refused, not
+    silently run as one rank."""
+    import subprocess
+    import sys
+    env = dict(os.environ, WORLD_SIZE="2", RANK="0")
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "1"], env=env,
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode != 0 and "WORLD_SIZE=2" in r.stderr

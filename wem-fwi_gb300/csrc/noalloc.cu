@@ -14,7 +14,13 @@
 // previous call left there, so two calls that overlap on the GPU (on
 // different streams, or from different host threads) race on it: serialise
 // them.  The first call on a device looks the array up with
-// cudaGetSymbolAddress; make that first call before any stream capture.
+// cudaGetSymbolAddress; make that first call before any stream capture.  The
+// address is kept per device together with the id of the context it was
+// looked up in, and looked up again only when the device's context has
+// changed (after cudaDeviceReset, say), which a later call then also must
+// not do under capture.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -38,12 +44,43 @@ constexpr size_t kScratchBytes = (size_t)1 << 20;  // 1 MiB per device
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 64;
-void* g_scratch_addr[kMaxDevices] = {};
+// per device: the array's address and the id of the context it belongs to
+struct ScratchSlot {
+  void* addr = nullptr;
+  unsigned long long ctx = 0;
+};
+ScratchSlot g_slot[kMaxDevices];
 std::mutex g_scratch_mutex;
+
+// id of the calling thread's current context (0: none, or the driver does
+// not say), through the driver entry points the runtime hands out, so the
+// library does not link the driver library itself
+unsigned long long current_context_id() {
+  static PFN_cuCtxGetCurrent_v4000 get_current = nullptr;
+  static PFN_cuCtxGetId_v12000 get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(f);
+    cudaGetLastError();
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
 
 // byte layout of the scratch for one call
 struct Layout {
-  size_t tw, kx, taper, omega, q, fac, ph, end;
+  size_t tw, kx, taper, omega, q, fac, ph, ref, end;
 };
 
 size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -58,16 +95,18 @@ Layout layout_of(int N, int nxg, int nref) {
   L.q = o;     o += al256((size_t)nxg * 8);
   L.fac = o;   o += al256((size_t)nxg * 8);
   L.ph = o;    o += al256((size_t)nref * N * 8);
+  L.ref = o;   o += al256((size_t)nxg);
   L.end = o;
   return L;
 }
 
 // twiddles, k grid (Phshift_cmplx.cpp:13,21-24), taper / N (Taper.h:11-23),
 // omega, and the split-step argument q = (s - s_ref)/sqrt(s_ref) of each
-// point's reference (SplitStep.cpp:12-13), all in double
+// point's reference (SplitStep.cpp:12-13), all in double; the caller's
+// reference indices are copied with every entry outside [-1, nref) made -1
 __global__ void k_noalloc_setup(int N, int nxg, int pad, double dx, float freq, int nref,
                                 const float2* slow, const float2* sref, const signed char* ref, float2* tw, float* kx,
-                                float* taper, float* omega, float2* q) {
+                                float* taper, float* omega, float2* q, signed char* ref_ok) {
   const double pi = 3.14159265358979323846;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
   for (int t = tid; t < N; t += nth) {
@@ -85,7 +124,8 @@ __global__ void k_noalloc_setup(int N, int nxg, int pad, double dx, float freq, 
     const int i = x < nxg - 1 - x ? x : nxg - 1 - x;
     if (i < pad) tp = .5 * (1 - cos(pi * i / (pad - 1)));
     taper[x] = (float)(tp / N);
-    const int j = ref[x];
+    const int j = ref[x] >= -1 && ref[x] < nref ? ref[x] : -1;
+    ref_ok[x] = (signed char)j;
     float2 v = make_float2(0.f, 0.f);
     if (j >= 0 && j < nref) {
       const double sr = sref[j].x, si = sref[j].y;
@@ -102,14 +142,16 @@ __global__ void k_noalloc_setup(int N, int nxg, int pad, double dx, float freq, 
   if (tid == 0) omega[0] = (float)(2 * pi * (double)freq);
 }
 
-bool device_ptr(const void* p) {
+// device memory of GPU `dev` (the current one), or managed memory
+bool device_ptr(const void* p, int dev) {
   if (!p) return false;
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 int fail(int code, const char* msg) {
@@ -149,30 +191,34 @@ extern "C" int wemop_onestep_noalloc(const wem_params* p, const void* slow_row, 
     return fail(WEM_EINVAL, "wemop_onestep_noalloc: rows are limited to N = nxg + 2 tap <= 4096 and nref <= 16");
   const Layout L = layout_of(N, nxg, p->nref);
   if (L.end > kScratchBytes) return fail(WEM_EINVAL, "wemop_onestep_noalloc: tables exceed the 1 MiB scratch");
-  if (!device_ptr(slow_row) || !device_ptr(sref) || !device_ptr(refidx) || !device_ptr(in) || !device_ptr(out))
-    return fail(WEM_EINVAL, "wemop_onestep_noalloc: every array must be device memory");
-  if (nrow == 0) return WEM_OK;
-  wg::FftPlan plan;
-  if (!plan_of(N, plan)) return fail(WEM_EINVAL, "FFT length has too many factors");
-
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     cudaGetLastError();
     return fail(WEM_EDEVICE, "wemop_onestep_noalloc: no usable current device");
   }
+  if (!device_ptr(slow_row, dev) || !device_ptr(sref, dev) || !device_ptr(refidx, dev) || !device_ptr(in, dev) ||
+      !device_ptr(out, dev))
+    return fail(WEM_EINVAL, "wemop_onestep_noalloc: every array must be device memory of the current device");
+  if (nrow == 0) return WEM_OK;
+  wg::FftPlan plan;
+  if (!plan_of(N, plan)) return fail(WEM_EINVAL, "FFT length has too many factors");
+
   unsigned char* base = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_addr[dev]) {
+    ScratchSlot& slot = g_slot[dev];
+    const unsigned long long ctx = slot.addr ? current_context_id() : 0;
+    if (!slot.addr || ctx == 0 || ctx != slot.ctx) {
       void* a = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&a, g_scratch);
       if (e != cudaSuccess || !a) {
         cudaGetLastError();
         return fail(WEM_EDEVICE, "wemop_onestep_noalloc: cannot get the scratch address");
       }
-      g_scratch_addr[dev] = a;
+      slot.addr = a;
+      slot.ctx = current_context_id();
     }
-    base = static_cast<unsigned char*>(g_scratch_addr[dev]);
+    base = static_cast<unsigned char*>(slot.addr);
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   float2* tw = reinterpret_cast<float2*>(base + L.tw);
@@ -182,10 +228,11 @@ extern "C" int wemop_onestep_noalloc(const wem_params* p, const void* slow_row, 
   float2* q = reinterpret_cast<float2*>(base + L.q);
   float2* fac = reinterpret_cast<float2*>(base + L.fac);
   float2* ph = reinterpret_cast<float2*>(base + L.ph);
+  signed char* ref_ok = reinterpret_cast<signed char*>(base + L.ref);
 
   k_noalloc_setup<<<8, 256, 0, st>>>(N, nxg, p->pad, (double)p->dx, freq, p->nref,
                                      static_cast<const float2*>(slow_row), static_cast<const float2*>(sref), refidx,
-                                     tw, kx, taper, omega, q);
+                                     tw, kx, taper, omega, q, ref_ok);
   wg::note_launch();
   // one depth, one frequency: the depth-step kernels index the tables at (f, z) = (0, 0)
   wg::DevCtx c{};
@@ -207,7 +254,7 @@ extern "C" int wemop_onestep_noalloc(const wem_params* p, const void* slow_row, 
   c.kx = kx;
   c.taperN = taper;
   c.omega = omega;
-  c.ref = refidx;
+  c.ref = ref_ok;
   wg::launch_phase_tables(c, static_cast<const float2*>(sref), p->eps, ph, st);
   c.ph = ph;
   if (p->prop == WEM_PROP_SSF) {

@@ -37,6 +37,28 @@ def block_par(par: Mapping, world: int, rank: int) -> dict:
     return p
 
 
+def interleave_par(par: Mapping, world: int, rank: int) -> dict:
+    """Weak-scaling survey: rank r keeps the block's shot count and spacing
+    but shifts the regular shot line by r / world of the shot interval, so
+    that the ranks together hold world x ns distinct, evenly spaced shots of
+    one survey (shot interval dsx / world)."""
+    if not 0 <= rank < world:
+        raise ValueError("rank out of range")
+    if "sx" in par and par["sx"] is not None:
+        raise ValueError("interleaving needs the regular shot geometry (ns, osx, dsx)")
+    p = dict(par)
+    p["osx"] = float(p.get("osx", 0.0)) + rank * float(p.get("dsx", 0.0)) / world
+    return p
+
+
+def survey_par(par: Mapping, world: int) -> dict:
+    """The whole survey of interleave_par's ranks as one shot line."""
+    p = dict(par)
+    p["ns"] = int(p["ns"]) * world
+    p["dsx"] = float(p.get("dsx", 0.0)) / world
+    return p
+
+
 def allreduce_sum(x, group=None):
     """Sum a gradient (torch tensor, any device the backend supports) over
     ranks in place."""
