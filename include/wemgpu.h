@@ -239,6 +239,34 @@ void fwi_destroy(fwi_handle* h);
 int fwi_gradient(fwi_handle* h, const void* slow2, const void* rho, const void* d_obs,
                  void* g_slow2, void* g_rho, double* loss);
 
+/* ---------------------------------- exact gradient of the nonlinear modelling
+ * No reference counterpart: the reference's FWI gradient is the Born adjoint
+ * above (a Taylor-scatter linearisation that holds the reference slownesses
+ * fixed and scales dReflect as dReflect.h:18-24 codes it), which is not the
+ * derivative of its modelled data.  These differentiate WEM::forward
+ * (wem_prop.cpp:9-78, WEMnl.cpp:11-82) exactly: through Reflect
+ * (Reflect.h:12-48), the split step (SplitStep.cpp:5-29), the phase shift
+ * (phase_shift.ispc:2-32, or the exact-kz law) and the reference slowness
+ * that RefSampler samples from the model (RefSampler.cpp:28-39).  The
+ * gradient of a real function L of the data is returned as
+ * dL/dRe + i dL/dIm for each complex model value.
+ * Requires one reference (nref = 1, SSF or PSPI), no conformal map, and
+ * N = nx + 2 pad + 2 tap = 32 E with E in {8, 12, 16, 24, 32}
+ * (WEM_ENOTIMPL otherwise).  checkpoint: 0 or 1 keeps every depth's
+ * wavefields on the device; k > 1 keeps every k-th depth and recomputes the
+ * k depths between from it (the same numbers, bit for bit; about 4/10 more
+ * work), which divides the stored bytes by about k.
+ *
+ * fwi_gradient_exact: loss = 1/2 ||WEM(s2, rho) - d_obs||^2 (d_obs float
+ * [ns][nr][nt]) and its exact gradient.
+ * wem_gradient: (g_slow2, g_rho) (+)= J^H g for the derivative J of
+ * wem_forward at (slow2, rho) and a data gradient g (data_kind as
+ * wem_forward: float time traces or complex bins). */
+int fwi_gradient_exact(fwi_handle* h, const void* slow2, const void* rho, const void* d_obs,
+                       void* g_slow2, void* g_rho, double* loss, int checkpoint);
+int wem_gradient(wem_handle* h, const void* slow2, const void* rho, const void* data_grad,
+                 int data_kind, void* g_slow2, void* g_rho, int add, int checkpoint);
+
 /* ------------------------------------- frequency-extended operators (ext*) */
 typedef struct extwem_handle extwem_handle;
 typedef struct extborn_handle extborn_handle;

@@ -5,7 +5,6 @@
 // schedule and the workspaces.  Every public call validates its arguments
 // on the host, turns every failure into a status code and never throws
 // across the boundary.
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -64,59 +63,6 @@ bool is_device_ptr(const void* p) {
   return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
-// cuBLAS handles for the time <-> frequency GEMMs: a per-device pool, one
-// handle lent to a caller for the length of a call (host threads that run
-// engines side by side each hold their own); handles are created on first
-// need and kept for the life of the process
-class BlasLease {
- public:
-  BlasLease() {
-    cuda_check(cudaGetDevice(&dev_), "cudaGetDevice");
-    require(dev_ >= 0 && dev_ < kMaxDev, "device index out of range");
-    {
-      std::lock_guard<std::mutex> lock(mu());
-      auto& f = pool()[dev_];
-      if (!f.empty()) {
-        h_ = f.back();
-        f.pop_back();
-      }
-    }
-    if (!h_ && cublasCreate(&h_) != CUBLAS_STATUS_SUCCESS) throw Fail(WEM_EDEVICE, "cublasCreate failed");
-    // the calling thread's default stream, where its engine's kernels run
-    if (cublasSetStream(h_, cudaStreamPerThread) != CUBLAS_STATUS_SUCCESS) {
-      give_back();
-      throw Fail(WEM_EDEVICE, "cublasSetStream failed");
-    }
-  }
-  ~BlasLease() { give_back(); }
-  BlasLease(const BlasLease&) = delete;
-  BlasLease& operator=(const BlasLease&) = delete;
-  cublasHandle_t get() const { return h_; }
-
- private:
-  static constexpr int kMaxDev = 64;
-  static std::mutex& mu() {
-    static std::mutex m;
-    return m;
-  }
-  static std::vector<cublasHandle_t>* pool() {
-    static std::vector<cublasHandle_t> p[kMaxDev];
-    return p;
-  }
-  void give_back() {
-    if (!h_) return;
-    std::lock_guard<std::mutex> lock(mu());
-    pool()[dev_].push_back(h_);
-    h_ = nullptr;
-  }
-  int dev_ = 0;
-  cublasHandle_t h_ = nullptr;
-};
-
-void blas_check(cublasStatus_t st, const char* what) {
-  if (st != CUBLAS_STATUS_SUCCESS) throw Fail(WEM_EDEVICE, std::string(what) + ": cuBLAS status " + std::to_string((int)st));
-}
-
 // growable device buffer
 struct Buf {
   void* p = nullptr;
@@ -136,6 +82,25 @@ struct Buf {
     return p;
   }
   template <class T> T* as(size_t n) { return reinterpret_cast<T*>(get(n * sizeof(T))); }
+};
+
+// page-locked host memory for the values a call reads back when it ends:
+// the loss (double at byte 0) and the background status (int at byte 8,
+// kNoBad when every reference slowness was positive)
+constexpr int kNoBad = 0x7f7f7f7f;
+struct Pinned {
+  void* p = nullptr;
+  ~Pinned() {
+    if (p) cudaFreeHost(p);
+  }
+  char* get() {
+    if (!p) {
+      cuda_check(cudaMallocHost(&p, 64), "cudaMallocHost");
+      std::memset(p, 0, 64);
+      *reinterpret_cast<int*>(static_cast<char*>(p) + 8) = kNoBad;
+    }
+    return static_cast<char*>(p);
+  }
 };
 
 template <class T>
@@ -225,32 +190,6 @@ std::vector<float> host_floats(const void* p, size_t nfloat) {
   return h;
 }
 
-// FFT1_r over time (FFT1_r.cpp:74-96) restricted to the propagated bins
-// (consecutive, PropParam.h:75-78): unitary DFT matrices in double, rounded
-// once; the forward takes e^{-i a}, the inverse keeps Re(B e^{i a})
-struct DftMatrices {
-  std::vector<float> wf, wi;  // [nt][2F], [2F][nt]
-};
-
-DftMatrices dft_matrices(const Geometry& g, int nt) {
-  const int n = g.nt_pad, F = g.nfreq(), F2 = 2 * F;
-  DftMatrices m;
-  m.wf.resize((size_t)nt * F2);
-  m.wi.resize((size_t)F2 * nt);
-  const long double pi = 3.14159265358979323846264338327950288L;
-  const double sc = 1.0 / std::sqrt((double)n);
-  for (int k = 0; k < nt; ++k)
-    for (int f = 0; f < F; ++f) {
-      const long double a = 2 * pi * (long double)((long long)g.bin[f] * k % n) / n;
-      const float cs = (float)(std::cos(a) * sc), sn = (float)(std::sin(a) * sc);
-      m.wf[(size_t)k * F2 + 2 * f] = cs;
-      m.wf[(size_t)k * F2 + 2 * f + 1] = -sn;
-      m.wi[(size_t)(2 * f) * nt + k] = cs;
-      m.wi[(size_t)(2 * f + 1) * nt + k] = -sn;
-    }
-  return m;
-}
-
 class Engine {
  public:
   // kind: 0 BornFull / WEM, 1 BornRefl, 2 BornTomo (propagator/src/ext_born_refl.cpp,
@@ -274,10 +213,8 @@ class Engine {
     int dev = 0;
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     if (!maps.empty()) {
-      // the shots share the time <-> frequency matrices; they run on
-      // `workers_` host threads (shot s on thread s mod workers_, in order),
-      // each thread with its own large buffers
-      dft_ = std::make_shared<const DftMatrices>(dft_matrices(geo_, p.nt));
+      // the shots run on `workers_` host threads (shot s on thread s mod
+      // workers_, in order), each thread with its own large buffers
       workers_ = std::max(1, std::min(geo_.ns, kShotWorkers));
       for (int w = 0; w < workers_; ++w) worker_ws_.push_back(std::make_shared<Scratch>());
       acc_.resize(workers_);
@@ -297,7 +234,7 @@ class Engine {
         gs.sptr = {0, (int)m.src_x.size()};
         gs.rx = m.rec_x;
         gs.rz = m.rec_z;
-        shots_.push_back(std::unique_ptr<Engine>(new Engine(ps, gs, m, born, dft_, worker_ws_[s % workers_])));
+        shots_.push_back(std::unique_ptr<Engine>(new Engine(ps, gs, m, born, worker_ws_[s % workers_])));
       }
       return;
     }
@@ -415,15 +352,12 @@ class Engine {
     wem_pass();
     // residual r = WEM(m) - d_obs in time, loss = 1/2 |r|^2, r back to bins
     const size_t nd = (size_t)geo_.ns * geo_.nr * p_.nt;
-    float* syn = dsyn_.as<float>(nd);
-    bins_to_time(syn, 0);
     Staged obs;
     obs.in(dobs, nd * 4);
-    const double loss = residual_loss(syn, (const float*)obs.dev, nd);
-    time_to_bins(syn);
+    double* loss_h = residual_bins((const float*)obs.dev);
     adj_pass();
-    grad_out(g_s2, g_rho, 0);
-    return loss;
+    grad_out(g_s2, g_rho, 0);  // ends with the stream synchronised
+    return *loss_h;
   }
 
   void born_forward(const void* ds2, const void* drho, void* data, int kind, int add) {
@@ -538,6 +472,7 @@ class Engine {
     cuda_check(cudaGetLastError(), "image launch");
     cuda_check(cudaStreamSynchronize(0), "image");
     o.finish(out);
+    check_background();
   }
 
   void born_adjoint(void* ds2, void* drho, const void* data, int kind, int add) {
@@ -627,6 +562,119 @@ class Engine {
     cuda_check(cudaStreamSynchronize(0), "born_adjoint");
     o0.finish(ds2);
     o1.finish(drho);
+    check_background();
+  }
+
+  // ---------------------------------- exact gradient of the modelling
+  // (kernels_wg.cuh, grad.cu): the adjoint-state derivative of the modelled
+  // data (wem_prop.cpp:9-78) through Reflect, the split step, the phase
+  // shift and the reference slowness; ck > 1 stores every ck-th depth and
+  // recomputes the segments between
+  void require_exact(bool tables) const {
+    if (!shots_.empty() || ext_ || kind_ != 0)
+      throw Fail(WEM_ENOTIMPL, "the exact gradient covers WEM without conformal maps or per-frequency models");
+    if (p_.nref != 1) throw Fail(WEM_ENOTIMPL, "the exact gradient needs one reference slowness (nref = 1)");
+    if (tables && !grad_warp_supported(ctx_))
+      throw Fail(WEM_ENOTIMPL, "the exact gradient runs on the warp kernels: N = 32 E, E in {8, 12, 16, 24, 32}, "
+                               "ntaylor <= 1, and its tables in shared memory");
+  }
+
+  // the images IR, IL and the per-depth reference sums of the data
+  // gradient held in the internal bins
+  void exact_pass(int ck) {
+    require(ck >= 0 && ck < p_.nz, "checkpoint interval must be in [0, nz)");
+    const int nz = p_.nz, nxg = geo_.nxg, N = geo_.N;
+    const size_t plane = (size_t)nz * nxg, splane = (size_t)nz * N;
+    if (!gam_ok_) {
+      float2* gam = gam_.as<float2>((size_t)F_ * nz * N);
+      launch_phase_grad_tables(ctx_, ctx_.sref, p_.eps, gam, 0);
+      ctx_.gam = gam;
+      gam_ok_ = true;
+    }
+    const int cke = ck > 1 ? ck : 0;
+    const int ncp = cke ? (nz - 1) / cke + 1 : nz;
+    const size_t segl = (size_t)(cke + 1) * (2 * nxg + 2 * N) + N;
+    const int G = std::min(geo_.ns, grad_rows_per_group());
+    const size_t row_store = cke ? (2 * (size_t)ncp * nxg + segl) * 8 : (2 * plane + 2 * splane) * 8;
+    float2* IR = ir_.as<float2>(plane);
+    float2* IL = is_.as<float2>(plane);
+    float2* qsum = qsum_.as<float2>(nz);
+    cuda_check(cudaMemsetAsync(IR, 0, plane * 8, 0), "memset");
+    cuda_check(cudaMemsetAsync(IL, 0, plane * 8, 0), "memset");
+    cuda_check(cudaMemsetAsync(qsum, 0, (size_t)nz * 8, 0), "memset");
+    ctx_.one_row = 0;
+    for_chunks(G, row_store + (2 * plane * 8 + G - 1) / G + 2 * (size_t)nz * 8, [&](const Group* gd, int ng, int rows) {
+      GradArgs a{};
+      a.bg = ws_->store1.as<float2>((size_t)rows * ncp * nxg);
+      a.t = ws_->store2.as<float2>((size_t)rows * ncp * nxg);
+      if (cke) {
+        a.seg = ws_->store3.as<float2>((size_t)rows * segl);
+      } else {
+        a.sw = ws_->store3.as<float2>((size_t)rows * splane);
+        a.sg = ws_->store4.as<float2>((size_t)rows * splane);
+      }
+      a.ir = ws_->part1.as<float2>((size_t)ng * plane);
+      a.il = ws_->part2.as<float2>((size_t)ng * plane);
+      if (!ctx_.fac) cuda_check(cudaMemsetAsync(a.il, 0, (size_t)ng * plane * 8, 0), "memset");
+      a.qs = qsbuf_.as<float2>((size_t)2 * rows * nz);
+      cuda_check(cudaMemsetAsync(a.qs, 0, (size_t)2 * rows * nz * 8, 0), "memset");
+      a.bins = bins_;
+      a.ck = cke;
+      a.rows_total = rows;
+      timed("k_wem_grad", [&] { launch_grad_warp(ctx_, gd, ng, a, 0); });
+      cuda_check(cudaGetLastError(), "k_wem_grad launch");
+      int* dbeg = upload(begbuf_, std::vector<int>{0, ng});
+      launch_reduce_images(a.ir, dbeg, 1, plane, IR, 0);
+      launch_reduce_images(a.il, dbeg, 1, plane, IL, 0);
+      launch_qs_reduce(a.qs, rows, nz, 1, qsum, 0);
+      cuda_check(cudaGetLastError(), "reduce launch");
+    }, true);
+  }
+
+  void exact_grad_out(void* g_s2, void* g_rho, int add) {
+    const size_t plane = (size_t)p_.nz * geo_.nxg;
+    const size_t nm = (size_t)p_.nz * p_.nx;
+    Staged o0, o1;
+    o0.out(g_s2, nm * 8, add != 0);
+    o1.out(g_rho, nm * 8, add != 0);
+    launch_exact_assemble(ctx_, p_.nx, p_.eps, static_cast<const float2*>(sp_.p), static_cast<const float2*>(dp_.p),
+                          ir_.as<float2>(plane), is_.as<float2>(plane), qsum_.as<float2>(p_.nz),
+                          gref_.as<float2>(p_.nz), (float2*)o0.dev, (float2*)o1.dev, add, 0);
+    cuda_check(cudaGetLastError(), "gradient launch");
+    cuda_check(cudaStreamSynchronize(0), "gradient");
+    o0.finish(g_s2);
+    o1.finish(g_rho);
+    check_background();
+  }
+
+  // the FWI objective and its exact gradient in one call
+  double fwi_gradient_exact(const void* s2, const void* rho, const void* dobs, void* g_s2, void* g_rho, int ck) {
+    require(s2 && rho && dobs && g_s2 && g_rho, "NULL argument");
+    require_exact(false);
+    set_background(s2, rho);
+    require_exact(true);
+    zero_bins();
+    wem_pass();
+    const size_t nd = (size_t)geo_.ns * geo_.nr * p_.nt;
+    Staged obs;
+    obs.in(dobs, nd * 4);
+    double* loss_h = residual_bins((const float*)obs.dev);
+    exact_pass(ck);
+    exact_grad_out(g_s2, g_rho, 0);
+    return *loss_h;
+  }
+
+  // (g_s2, g_rho) (+)= J^H g: the adjoint of the modelling's derivative at
+  // (s2, rho) applied to the data gradient g (time traces or bins)
+  void wem_gradient(const void* s2, const void* rho, const void* data, int kind, void* g_s2, void* g_rho, int add,
+                    int ck) {
+    require(s2 && rho && data && g_s2 && g_rho, "NULL argument");
+    require_exact(false);
+    set_background(s2, rho);
+    require_exact(true);
+    absorb(data, kind);
+    exact_pass(ck);
+    exact_grad_out(g_s2, g_rho, add);
   }
 
   // a model-grid field of this shot's mapped grid back onto the model grid
@@ -643,15 +691,14 @@ class Engine {
   // operator run one after another and rebuild their tables before every
   // pass, so they share one set.
   struct Scratch {
-    Buf store1, store2, store3, part1, part2, ph, fac;
+    Buf store1, store2, store3, store4, part1, part2, ph, fac;
   };
   std::shared_ptr<Scratch> ws_ = std::make_shared<Scratch>();
 
   // one shot of a conformal-map operator: its mapped grid (p.dx, p.dz) and
   // devices (g) and the gather tables of its map
-  Engine(const wem_params& p, const Geometry& g, const ShotMap& m, bool born,
-         std::shared_ptr<const DftMatrices> dft, std::shared_ptr<Scratch> ws)
-      : p_(p), ext_(false), born_(born), kind_(0), dft_(std::move(dft)) {
+  Engine(const wem_params& p, const Geometry& g, const ShotMap& m, bool born, std::shared_ptr<Scratch> ws)
+      : p_(p), ext_(false), born_(born), kind_(0) {
     ws_ = std::move(ws);
     geo_ = g;
     F_ = geo_.nfreq();
@@ -749,20 +796,24 @@ class Engine {
   wem_params p_;
   bool ext_, born_;
   int kind_ = 0;
-  std::shared_ptr<const DftMatrices> dft_;
   int M_img_ = 1;  // image slices: per frequency for the extended operators and BornRefl
   bool have_bg_ = false;
   Geometry geo_;
   int F_ = 0, M_ = 1;
   DevCtx ctx_{};
   // static tables
-  Buf tw_, kx_, taper_, omega_, bin_, wave_, sx_, sz_, gs_, gr_, rptr_, rid_, rxs_, wfwd_, winv_;
+  Buf tw_, kx_, taper_, omega_, bin_, wave_, sx_, sz_, gs_, gr_, rptr_, rid_, rxs_, tftw_, tfwn_;
+  TimeFreq tf_{};  // the traces' time <-> frequency transform (timefreq.cu)
+  TfShape tfs_{};
   // background tables
-  Buf sref_, ref_, q_, sc_, rc_, a0b_, b0b_, a1b_, b1b_, sp_, dp_;
+  Buf sref_, ref_, q_, sc_, rc_, a0b_, b0b_, a1b_, b1b_, sp_, dp_, badbuf_, refscr_;
   float2 *a0_ = nullptr, *b0_ = nullptr, *a1_ = nullptr, *b1_ = nullptr;
   // workspaces
   std::vector<Group> chunk_;  // host copy of the groups of the current launch
-  Buf rcf_, binsbuf_, groups_, dsyn_, lossbuf_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
+  Buf rcf_, binsbuf_, groups_, lossbuf_, dm0_, dm1_, drm_, ir_, is_, begbuf_, stage_;
+  Buf gam_, qsum_, qsbuf_, gref_;  // exact gradient: phase-factor derivatives and reference sums
+  bool gam_ok_ = false;
+  Pinned pinned_;
   float2* bins_ = nullptr;
 
   void build_static() {
@@ -818,9 +869,9 @@ class Engine {
     ctx_.rptr = upload(rptr_, rptr);
     ctx_.rid = upload(rid_, ord);
     ctx_.rxs = upload(rxs_, rxs);
-    if (!dft_) dft_ = std::make_shared<const DftMatrices>(dft_matrices(g, p_.nt));
-    upload(wfwd_, dft_->wf);
-    upload(winv_, dft_->wi);
+    // time <-> frequency over n = nt + tpad samples; the propagated bins are
+    // the window [bin[0], bin[0] + F)
+    build_timefreq(g.nt_pad);
     bins_ = binsbuf_.as<float2>((size_t)g.ns * g.nr * F_);
   }
 
@@ -860,35 +911,17 @@ class Engine {
     }
     float2* dsref = sref_.as<float2>((size_t)M_ * nz * nref);
     signed char* dref = ref_.as<signed char>((size_t)M_ * plane);
-    const bool device_refs = nref == 1 && (p_.refs_mode == WEM_REFS_NEAREST || nz <= nxg - 2);
-    if (device_refs) {
-      launch_sref(sp, dsref, M_, nz, nxg, nref, 0);
-      cuda_check(cudaMemsetAsync(dref, 0, (size_t)M_ * plane, 0), "memset");
-      std::vector<float2> h((size_t)M_ * nz * nref);
-      cuda_check(cudaMemcpy(h.data(), dsref, h.size() * 8, cudaMemcpyDeviceToHost), "D2H sref");
-      for (size_t i = 0; i < h.size(); ++i)
-        if (!(h[i].x > 0))
-          throw Fail(WEM_EINVAL, "Ref velocity " + std::to_string(h[i].x) + " at the layer " +
-                                     std::to_string((i / nref) % nz));
-    } else {
-      std::vector<float2> hs((size_t)M_ * plane);
-      cuda_check(cudaMemcpy(hs.data(), sp, hs.size() * 8, cudaMemcpyDeviceToHost), "D2H slowness");
-      std::vector<float2> sref((size_t)M_ * nz * nref);
-      std::vector<signed char> ref((size_t)M_ * plane);
-      for (int m = 0; m < M_; ++m) {
-        std::vector<cd> spm(plane);
-        for (size_t i = 0; i < plane; ++i) spm[i] = cd(hs[(size_t)m * plane + i].x, hs[(size_t)m * plane + i].y);
-        std::vector<cd> sr_m;
-        std::vector<signed char> ref_m;
-        refsampler(p_, spm, nxg, nz, sr_m, ref_m);
-        for (size_t i = 0; i < sr_m.size(); ++i)
-          sref[(size_t)m * nz * nref + i] = make_float2((float)sr_m[i].real(), (float)sr_m[i].imag());
-        std::copy(ref_m.begin(), ref_m.end(), ref.begin() + (size_t)m * plane);
-      }
-      cuda_check(cudaMemcpy(dsref, sref.data(), sref.size() * 8, cudaMemcpyHostToDevice), "H2D sref");
-      cuda_check(cudaMemcpy(dref, ref.data(), ref.size(), cudaMemcpyHostToDevice), "H2D ref");
-    }
+    // RefSampler on the device; a reference slowness <= 0 is reported when
+    // the call ends (check_background), not by a copy in mid-call
+    int* bad = badbuf_.as<int>(1);
+    cuda_check(cudaMemsetAsync(bad, 0x7f, sizeof(int), 0), "memset");
+    launch_sref(sp, dsref, M_, nz, nxg, nref, bad, 0);
+    cuda_check(cudaMemcpyAsync(pinned_bad(), bad, sizeof(int), cudaMemcpyDeviceToHost, 0), "D2H status");
+    launch_refsampler(p_.refs_mode == WEM_REFS_NEAREST ? 1 : 0, sp, dsref, M_, nz, nxg, nref,
+                      refscr_.as<float>(refs_scratch_floats(M_, nz, nref)), dref, 0);
     ctx_.ref = dref;
+    ctx_.sref = dsref;
+    gam_ok_ = false;
     const bool ssf = p_.prop == WEM_PROP_SSF;
     float2* q = ssf ? q_.as<float2>((size_t)M_ * plane) : nullptr;
     float2* rc = rc_.as<float2>((size_t)M_ * plane);
@@ -1028,47 +1061,101 @@ class Engine {
     cuda_check(cudaStreamSynchronize(0), "pad");
   }
 
-  // internal bins [ns][nr][F] -> time traces [ns][nr][nt] on the device: one
-  // GEMM with the inverse DFT matrix of the propagated bins
+  // internal bins [ns][nr][F] -> time traces [ns][nr][nt] on the device
   void bins_to_time(float* t, int add) {
-    const int ntr = geo_.ns * geo_.nr;
-    BlasLease lease;
-    cublasHandle_t h = lease.get();
-    const float one = 1.f, beta = add ? 1.f : 0.f;
-    blas_check(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, p_.nt, ntr, 2 * F_, &one, (const float*)winv_.p, p_.nt,
-                           (const float*)bins_, 2 * F_, &beta, t, p_.nt),
-               "bins to time");
-    note_launch();
+    launch_timefreq(0, tf_, tfs_, bins_, t, nullptr, geo_.ns * geo_.nr, add, nullptr, 0);
   }
 
   // time traces on the device -> internal bins
   void time_to_bins(const float* t) {
-    const int ntr = geo_.ns * geo_.nr;
-    BlasLease lease;
-    cublasHandle_t h = lease.get();
-    const float one = 1.f, zero = 0.f;
-    blas_check(cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, 2 * F_, ntr, p_.nt, &one, (const float*)wfwd_.p, 2 * F_, t,
-                           p_.nt, &zero, (float*)bins_, 2 * F_),
-               "time to bins");
-    note_launch();
+    launch_timefreq(1, tf_, tfs_, bins_, const_cast<float*>(t), nullptr, geo_.ns * geo_.nr, 0, nullptr, 0);
   }
 
-  // syn <- syn - obs; returns 1/2 |syn - obs|^2 (per-block partial sums in
-  // double, added in block order on the host)
-  double residual_loss(float* syn, const float* obs, size_t n) {
-    const int nblk = residual_blocks();
-    double* part = lossbuf_.as<double>(nblk);
-    launch_residual(syn, obs, n, part, nblk, 0);
+  int* pinned_bad() { return reinterpret_cast<int*>(pinned_.get() + 8); }
+
+ public:
+  // once the stream has passed the last background build: a reference
+  // slowness whose real part is not > 0 fails the call as the reference's
+  // RefSampler does (RefSampler.cpp:35-36)
+  void check_background() {
+    if (have_bg_ && shots_.empty()) cuda_check(cudaStreamSynchronize(0), "background");
+    if (!shots_.empty() || !pinned_.p) return;
+    const int i = *pinned_bad();
+    if (i == kNoBad) return;
+    float2 v{};
+    cuda_check(cudaMemcpy(&v, static_cast<const float2*>(sref_.p) + i, sizeof v, cudaMemcpyDeviceToHost), "D2H sref");
+    throw Fail(WEM_EINVAL, "Ref velocity " + std::to_string(v.x) + " at the layer " +
+                               std::to_string((i / p_.nref) % p_.nz));
+  }
+
+ private:
+  // the FFT plan with its per-stage twiddle tables ([r - 1][l] per stage, in
+  // double rounded once) and the natural table of the restricted DFT
+  void build_timefreq(int n) {
+    TimeFreq& t = tf_;
+    t = TimeFreq{};
+    t.n = n;
+    t.nt = p_.nt;
+    t.nf = F_;
+    t.b0 = geo_.bin[0];
+    t.sc = (float)(1.0 / std::sqrt((double)n));
+    t.wn = upload(tfwn_, to_f2(twiddles(n)));
+    // radices, largest first: 16, 12, 8, 6 (in-register DFTs), then 4, 3, 2, 5, 7
+    std::vector<int> rad;
+    int m = n;
+    for (int r : {16, 12, 8, 6, 4, 3, 2, 5, 7})
+      while (m % r == 0) {
+        rad.push_back(r);
+        m /= r;
+      }
+    t.fft = m == 1 && (int)rad.size() <= kMaxStages && n <= 16384;
+    if (t.fft) {
+      const long double pi = 3.14159265358979323846264338327950288L;
+      std::vector<float2> tws;
+      t.plan.n = n;
+      t.plan.nstage = (int)rad.size();
+      int L = 1;
+      for (size_t s = 0; s < rad.size(); ++s) {
+        TfStage& S = t.st[s];
+        S.R = rad[s];
+        t.plan.radix[s] = S.R;
+        S.L = L;
+        S.nb = n / S.R;
+        S.ld = n + (n >> 4) + 1;
+        S.twoff = (int)tws.size();
+        S.mag_nb = (unsigned)((((unsigned long long)1 << 32) + S.nb - 1) / S.nb);
+        S.mag_L = (unsigned)((((unsigned long long)1 << 32) + L - 1) / L);
+        for (int k = 0; k < 7; ++k)
+          S.w7[k] = make_float2((float)std::cos(-2 * pi * k / 7), (float)std::sin(-2 * pi * k / 7));
+        for (int r = 1; r < S.R; ++r)
+          for (int l = 0; l < L; ++l) {
+            const long double a = -2 * pi * (long double)(r * l) / ((long double)L * S.R);
+            tws.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
+          }
+        L *= S.R;
+      }
+      t.tw_len = (int)tws.size();
+      t.tws = upload(tftw_, tws);
+    }
+    tfs_ = timefreq_shape(t, geo_.ns * geo_.nr);
+    require(tfs_.ok, "time axis too long for the time-frequency kernels' shared memory");
+  }
+
+  // bins <- bins of (the bins' time traces - obs); the loss 1/2 |residual|^2
+  // lands in page-locked host memory once the stream has reached it (the
+  // per-CTA sums added in a fixed order)
+  double* residual_bins(const float* obs) {
+    double* part = lossbuf_.as<double>((size_t)tfs_.grid + 1);
+    launch_timefreq(2, tf_, tfs_, bins_, nullptr, obs, geo_.ns * geo_.nr, 0, part, 0);
+    launch_half_sum(part, tfs_.grid, part + tfs_.grid, 0);
     cuda_check(cudaGetLastError(), "residual launch");
-    std::vector<double> h(nblk);
-    cuda_check(cudaMemcpy(h.data(), part, nblk * sizeof(double), cudaMemcpyDeviceToHost), "D2H loss");
-    double sum = 0;
-    for (double v : h) sum += v;
-    return 0.5 * sum;
+    double* h = reinterpret_cast<double*>(pinned_.get());
+    cuda_check(cudaMemcpyAsync(h, part + tfs_.grid, sizeof(double), cudaMemcpyDeviceToHost, 0), "D2H loss");
+    return h;
   }
 
-  // internal bins -> caller data: time traces by one GEMM, frequency data by
-  // a window copy
+  // internal bins -> caller data: time traces by the inverse transform,
+  // frequency data by a window copy
   void emit(void* data, int kind, int add) {
     require(data != nullptr, "data is NULL");
     const int ntr = geo_.ns * geo_.nr;
@@ -1084,6 +1171,7 @@ class Engine {
     cuda_check(cudaGetLastError(), "emit launch");
     cuda_check(cudaStreamSynchronize(0), "operator");
     o.finish(data);
+    check_background();
   }
 
   // caller data -> internal bins
@@ -1104,6 +1192,35 @@ class Engine {
 };
 
 // ------------------------------------------------------------ wemop
+// RefSampler tables of one padded slowness grid [nz][nxg] on the device,
+// brought back to the host (the row-level operators build their other
+// tables there)
+void device_refsampler(const wem_params& p, const float2* slow_d, int nxg, std::vector<cd>& sref,
+                       std::vector<signed char>& ref) {
+  require(p.nref >= 1 && p.nref <= 127 && p.nref <= nxg, "nref must be in [1, min(127, nxg)]");
+  const int nz = p.nz, nref = p.nref;
+  Buf sb, rb, bb, scr;
+  float2* dsref = sb.as<float2>((size_t)nz * nref);
+  signed char* dref = rb.as<signed char>((size_t)nz * nxg);
+  int* bad = bb.as<int>(1);
+  cuda_check(cudaMemsetAsync(bad, 0x7f, sizeof(int), 0), "memset");
+  launch_sref(slow_d, dsref, 1, nz, nxg, nref, bad, 0);
+  launch_refsampler(p.refs_mode == WEM_REFS_NEAREST ? 1 : 0, slow_d, dsref, 1, nz, nxg, nref,
+                    scr.as<float>(refs_scratch_floats(1, nz, nref)), dref, 0);
+  cuda_check(cudaGetLastError(), "refsampler kernels");
+  std::vector<float2> hs((size_t)nz * nref);
+  int hbad = 0;
+  cuda_check(cudaMemcpy(hs.data(), dsref, hs.size() * 8, cudaMemcpyDeviceToHost), "D2H sref");
+  cuda_check(cudaMemcpy(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost), "D2H status");
+  if (hbad != kNoBad)
+    throw Fail(WEM_EINVAL, "Ref velocity " + std::to_string(hs[hbad].x) + " at the layer " +
+                               std::to_string(hbad / nref));
+  ref.resize((size_t)nz * nxg);
+  cuda_check(cudaMemcpy(ref.data(), dref, ref.size(), cudaMemcpyDeviceToHost), "D2H ref");
+  sref.resize(hs.size());
+  for (size_t i = 0; i < hs.size(); ++i) sref[i] = cd(hs[i].x, hs[i].y);
+}
+
 class RowOps {
  public:
   RowOps(const wem_params& p, const void* slow, int nxg) : p_(p), nxg_(nxg) {
@@ -1115,7 +1232,14 @@ class RowOps {
     std::vector<float> hs = host_floats(slow, 2 * (size_t)p.nz * nxg);
     std::vector<cd> sp((size_t)p.nz * nxg), dp(sp.size(), cd(1.0, 0.0));
     for (size_t i = 0; i < sp.size(); ++i) sp[i] = cd(hs[2 * i], hs[2 * i + 1]);
-    t_ = make_slice_tables(p, sp, dp, nxg, true);
+    std::vector<float2> sf(sp.size());
+    for (size_t i = 0; i < sp.size(); ++i) sf[i] = make_float2(hs[2 * i], hs[2 * i + 1]);
+    slow_d_ = upload(slow_, sf);
+    // the partition from the operators' own device RefSampler
+    std::vector<cd> sref;
+    std::vector<signed char> ref;
+    device_refsampler(p, slow_d_, nxg, sref, ref);
+    t_ = make_slice_tables(p, sp, dp, nxg, true, sref, ref);
     N_ = nxg + 2 * p.tap;
     std::vector<double> k = k_grid(N_, p.dx), tp = taper(nxg, p.pad);
     std::vector<float> kf(k.begin(), k.end()), tpf(nxg);
@@ -1137,9 +1261,6 @@ class RowOps {
     c_.tw = upload(tw_, to_f2(twiddles(N_)));
     c_.kx = upload(kx_, kf);
     c_.taperN = upload(taper_, tpf);
-    std::vector<float2> sf(sp.size());
-    for (size_t i = 0; i < sp.size(); ++i) sf[i] = make_float2(hs[2 * i], hs[2 * i + 1]);
-    slow_d_ = upload(slow_, sf);
     c_.ref = upload(ref_, t_.ref);
     c_.sc = upload(sc_, to_f2(t_.sc));
     c_.rc = upload(rc_, to_f2(t_.rc));
@@ -1366,12 +1487,17 @@ int born_create(const wem_params* p, const float* wavelet, const void* s2, const
     auto h = std::make_unique<born_handle>();
     h->e = std::make_unique<Engine>(*p, wavelet, false, true);
     h->e->set_background(s2, rho);
+    h->e->check_background();
     *out = h.release();
   });
 }
 void born_destroy(born_handle* h) { delete h; }
 int born_set_background(born_handle* h, const void* s2, const void* rho) {
-  return guard([&] { require(h != nullptr, "NULL handle"); h->e->set_background(s2, rho); });
+  return guard([&] {
+    require(h != nullptr, "NULL handle");
+    h->e->set_background(s2, rho);
+    h->e->check_background();
+  });
 }
 int born_forward(born_handle* h, const void* ds2, const void* drho, void* data, int kind, int add) {
   return guard([&] { require(h != nullptr, "NULL handle"); h->e->born_forward(ds2, drho, data, kind, add); });
@@ -1399,6 +1525,7 @@ static void set_bg_unit_rho(Engine& e, const wem_params& p, const void* s2) {
   std::vector<float> ones((size_t)2 * p.nz * p.nx, 0.f);
   for (size_t i = 0; i < ones.size(); i += 2) ones[i] = 1.f;
   e.set_background(s2, ones.data());
+  e.check_background();
 }
 
 int bornrefl_create(const wem_params* p, const float* wavelet, const void* s2, bornrefl_handle** out) {
@@ -1461,6 +1588,22 @@ int fwi_gradient(fwi_handle* h, const void* s2, const void* rho, const void* d_o
   });
 }
 
+int fwi_gradient_exact(fwi_handle* h, const void* s2, const void* rho, const void* d_obs, void* g_s2, void* g_rho,
+                       double* loss, int checkpoint) {
+  return guard([&] {
+    require(h != nullptr && loss != nullptr, "NULL argument");
+    *loss = h->e->fwi_gradient_exact(s2, rho, d_obs, g_s2, g_rho, checkpoint);
+  });
+}
+
+int wem_gradient(wem_handle* h, const void* s2, const void* rho, const void* data_grad, int kind, void* g_s2,
+                 void* g_rho, int add, int checkpoint) {
+  return guard([&] {
+    require(h != nullptr, "NULL handle");
+    h->e->wem_gradient(s2, rho, data_grad, kind, g_s2, g_rho, add, checkpoint);
+  });
+}
+
 int extborn_create(const wem_params* p, const float* wavelet, const void* s2, const void* rho,
                    extborn_handle** out) {
   return guard([&] {
@@ -1468,12 +1611,17 @@ int extborn_create(const wem_params* p, const float* wavelet, const void* s2, co
     auto h = std::make_unique<extborn_handle>();
     h->e = std::make_unique<Engine>(*p, wavelet, true, true);
     h->e->set_background(s2, rho);
+    h->e->check_background();
     *out = h.release();
   });
 }
 void extborn_destroy(extborn_handle* h) { delete h; }
 int extborn_set_background(extborn_handle* h, const void* s2, const void* rho) {
-  return guard([&] { require(h != nullptr, "NULL handle"); h->e->set_background(s2, rho); });
+  return guard([&] {
+    require(h != nullptr, "NULL handle");
+    h->e->set_background(s2, rho);
+    h->e->check_background();
+  });
 }
 int extborn_forward(extborn_handle* h, const void* ds2, const void* drho, void* data, int kind, int add) {
   return guard([&] { require(h != nullptr, "NULL handle"); h->e->born_forward(ds2, drho, data, kind, add); });

@@ -45,13 +45,22 @@ __host__ __device__ inline float2 c_sub(float2 a, float2 b) {
   return make_float2(a.x - b.x, a.y - b.y);
 #endif
 }
-__host__ __device__ inline float2 c_mul(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+// Complex products with their roundings written out (one product rounded,
+// the other fused into it), so that every inlined copy of a transform or a
+// depth step computes the same bits whatever the surrounding code: a
+// checkpointed recompute reproduces the stored wavefields exactly.
+#ifdef __CUDA_ARCH__
+__device__ inline float2 c_mul(float2 a, float2 b) {
+  return make_float2(__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)), __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
 }
 // a * conj(b)
-__host__ __device__ inline float2 c_mulc(float2 a, float2 b) {
-  return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+__device__ inline float2 c_mulc(float2 a, float2 b) {
+  return make_float2(__fmaf_rn(a.x, b.x, __fmul_rn(a.y, b.y)), __fmaf_rn(a.y, b.x, -__fmul_rn(a.x, b.y)));
 }
+#else
+inline float2 c_mul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+inline float2 c_mulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
+#endif
 // acc + a b and acc + a conj(b) as four fused multiply-adds (the paired add
 // above would otherwise stop the accumulation from contracting)
 __host__ __device__ inline float2 c_fma(float2 acc, float2 a, float2 b) {
@@ -61,7 +70,11 @@ __host__ __device__ inline float2 c_fmac(float2 acc, float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, fmaf(a.y, b.y, acc.x)), fmaf(a.y, b.x, fmaf(-a.x, b.y, acc.y)));
 }
 __host__ __device__ inline float2 c_conj(float2 a) { return make_float2(a.x, -a.y); }
-__host__ __device__ inline float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+#ifdef __CUDA_ARCH__
+__device__ inline float2 c_scale(float2 a, float s) { return make_float2(__fmul_rn(a.x, s), __fmul_rn(a.y, s)); }
+#else
+inline float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+#endif
 // multiply by -i (fwd) or +i (inv)
 __device__ inline float2 c_rot(float2 a, bool inv) {
   return inv ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);

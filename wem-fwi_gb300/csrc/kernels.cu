@@ -814,24 +814,6 @@ __global__ void k_bin_window(const float2* src, float2* dst, int nrows, int ldu,
   }
 }
 
-// r <- syn - obs in place; each CTA leaves the sum of its r^2 (in double)
-__global__ void k_residual(float* syn, const float* obs, size_t n, double* part) {
-  __shared__ double red[256];
-  double acc = 0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const float r = syn[i] - obs[i];
-    syn[i] = r;
-    acc += (double)r * r;
-  }
-  red[threadIdx.x] = acc;
-  __syncthreads();
-  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
-}
-
 __global__ void k_copy_rows(const float2* src, int lds, float2* dst, int ldd, int nrows, int ncopy, int add) {
   const size_t total = (size_t)nrows * ldd;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
@@ -986,13 +968,6 @@ void launch_bin_window(const float2* src, float2* dst, int nrows, int ldu, int n
                        cudaStream_t st) {
   const size_t n = (size_t)nrows * (to_user ? ldu : nf);
   k_bin_window<<<grid_for(n), 256, 0, st>>>(src, dst, nrows, ldu, nf, off, to_user, add);
-  note_launch();
-}
-
-int residual_blocks() { return 152 * 4; }
-
-void launch_residual(float* syn, const float* obs, size_t n, double* part, int nblk, cudaStream_t st) {
-  k_residual<<<nblk, 256, 0, st>>>(syn, obs, n, part);
   note_launch();
 }
 

@@ -46,6 +46,9 @@ struct DevCtx {
   const int* rptr;              // [nz + 1] receivers by depth (CSR over rid)
   const int* rid;               // receiver ids sorted by (depth, x)
   const int* rxs;               // x of rid[k] (sorted within a depth)
+  // exact gradient of the modelling (kernels_wg.cuh)
+  const float2* gam;            // [F][nz][N] -i dz ph / (2 kz), the phase factor's derivative
+  const float2* sref;           // [M][nz][nref] reference slownesses
 };
 
 // group g: frequency f, first shot s0, row count n, first storage row
@@ -118,9 +121,41 @@ void launch_pass_warp(int which, const DevCtx& c, const Group* g, int ng, const 
 // then needs s3: [rows][nz][nxg] filtered spectra of the stored T
 bool warp_adj_reuse(const DevCtx& c, int compat);
 
+// exact gradient of the modelling (kernels_wg.cuh), two warps per row, one
+// reference; storage per row: full (ck <= 1) bg, t [nz][nxg] and sw, sg
+// [nz][N]; checkpoints (ck > 1) bg, t [(nz - 1)/ck + 1][nxg] and seg
+// [(ck + 1)(2 nxg + 2 N) + N]; per group: il, ir [nz][nxg]; qs [2][rows][nz]
+struct GradArgs {
+  float2 *bg, *t, *sw, *sg, *seg, *il, *ir, *qs;
+  const float2* bins;
+  int ck, rows_total;
+};
+bool grad_warp_supported(const DevCtx& c);
+int grad_rows_per_group();
+void launch_grad_warp(const DevCtx& c, const Group* g, int ng, const GradArgs& a, cudaStream_t st);
+// Gamma = -i dz ph / (2 kz) of every phase-table entry (one reference)
+void launch_phase_grad_tables(const DevCtx& c, const float2* sref, float eps, float2* gam, cudaStream_t st);
+// out[z] (+)= sum over rows r of qs[0][r][z] + qs[1][r][z], rows in order
+void launch_qs_reduce(const float2* qs, int rows, int nz, int add, float2* out, cudaStream_t st);
+// gradient of the modelling on the model grid [nz][nx] from the images IR,
+// IL [nz][nxg] and the per-depth reference sums qsum [nz] (exact derivatives
+// of Reflect, the split-step and reference terms; edge-extended padding
+// summed back onto the edge columns)
+void launch_exact_assemble(const DevCtx& c, int nx, float eps, const float2* sp, const float2* dp, const float2* IR,
+                           const float2* IL, const float2* qsum, float2* gref, float2* g0, float2* g1, int add,
+                           cudaStream_t st);
+
 // ---- background tables on the device (tables.cu)
 void launch_pad_edge(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st);
-void launch_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref, cudaStream_t st);
+// reference slownesses [M][nz][nref]; bad (may be null): atomicMin of the
+// flat index of any entry whose real part is not > 0
+void launch_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref, int* bad, cudaStream_t st);
+// RefSampler partition (as coded, or nearest): reference index [M][nz][nxg]
+// of every point from the padded slowness and the reference slownesses;
+// scratch holds refs_scratch_floats(M, nz, nref) floats
+size_t refs_scratch_floats(int M, int nz, int nref);
+void launch_refsampler(int nearest, const float2* sp, const float2* sref, int M, int nz, int nxg, int nref,
+                       float* scratch, signed char* ref, cudaStream_t st);
 // q (SSF split step, may be null), rc, and for the Born operators sc and the
 // dReflect pairs (null to skip) of every padded point
 // sp_refl: the slowness of the Reflect/dReflect coefficients when it differs
@@ -145,10 +180,37 @@ void launch_reduce_images(const float2* parts, const int* slice_beg, int M, size
 void launch_grad_assemble(const DevCtx& c, int M, const float2* a0, const float2* b0, const float2* a1,
                           const float2* b1, const float2* IR, const float2* IS, float2* g0, float2* g1, int nx,
                           int add, cudaStream_t st);
-// traces: time [ntr][nt] <-> bins [ntr][n]
-// syn <- syn - obs; part[nblk] per-CTA sums of the squares (double)
-int residual_blocks();
-void launch_residual(float* syn, const float* obs, size_t n, double* part, int nblk, cudaStream_t st);
+// ---- time <-> frequency (timefreq.cu): real traces [ntr][nt] <-> compact
+// bins [ntr][nf] at the consecutive FFT bins b0 .. b0 + nf - 1 of length n
+struct TfStage {
+  int R, L, nb, twoff, ld;   // radix, product of the earlier radices, n / R, offset in tws, padded row length
+  unsigned mag_nb, mag_L;    // ceil(2^32 / nb), ceil(2^32 / L) (unused when 1)
+  float2 w7[7];              // exp(-2 pi i m / 7) (radix 7)
+};
+struct TimeFreq {
+  FftPlan plan;              // radices of n = nt + tpad
+  TfStage st[kMaxStages];
+  const float2* tws;         // per-stage twiddles [(R - 1) L] in stage order
+  int tw_len;
+  const float2* wn;          // [n] exp(-2 pi i j / n) (the restricted DFT)
+  int n, nt, nf, b0;
+  int fft;                   // every prime factor of n is <= 7
+  float sc;                  // 1/sqrt(n)
+};
+// launch shape: the FFT path with R traces per CTA, or the restricted DFT
+// (use_fft 0); ok 0 when the DFT's traces do not fit in shared memory
+struct TfShape {
+  int R, grid, use_fft, ok;
+  size_t smem;
+};
+TfShape timefreq_shape(const TimeFreq& t, int ntr);
+// mode 0: time (+)= Re IFFT(bins) sc (add), 1: bins = FFT(time) sc,
+// 2: bins <- FFT(Re IFFT(bins) sc - obs) sc and part[grid] the per-CTA sums
+// of the squared residual (double)
+void launch_timefreq(int mode, const TimeFreq& t, const TfShape& s, float2* bins, float* time, const float* obs,
+                     int ntr, int add, double* part, cudaStream_t st);
+// out[0] = 1/2 sum part[0..n) in a fixed order
+void launch_half_sum(const double* part, int n, double* out, cudaStream_t st);
 // caller bins [nrows][ldu] <-> compact propagated bins [nrows][nf] (window at off)
 void launch_bin_window(const float2* src, float2* dst, int nrows, int ldu, int nf, int off, int to_user, int add,
                        cudaStream_t st);

@@ -77,6 +77,37 @@ void launch_pass_warp(int which, const DevCtx& c, const Group* g, int ng, const 
   }
 }
 
+template <int E>
+void launch_grad_w(const DevCtx& c, const Group* g, int ng, const GradArgs& a, cudaStream_t st);
+template <int E>
+bool grad_fits_w(const DevCtx& c);
+
+bool grad_warp_supported(const DevCtx& c) {
+  if (!warp_path_supported(c)) return false;
+  switch (c.N / 32) {
+    case 8: return grad_fits_w<8>(c);
+    case 12: return grad_fits_w<12>(c);
+    case 16: return grad_fits_w<16>(c);
+    case 24: return grad_fits_w<24>(c);
+    case 32: return grad_fits_w<32>(c);
+    default: return false;
+  }
+}
+
+// rows per CTA of the gradient kernel (kRowsAdj2 of kernels_w.cuh)
+int grad_rows_per_group() { return 8; }
+
+void launch_grad_warp(const DevCtx& c, const Group* g, int ng, const GradArgs& a, cudaStream_t st) {
+  switch (c.N / 32) {
+    case 8: launch_grad_w<8>(c, g, ng, a, st); break;
+    case 12: launch_grad_w<12>(c, g, ng, a, st); break;
+    case 16: launch_grad_w<16>(c, g, ng, a, st); break;
+    case 24: launch_grad_w<24>(c, g, ng, a, st); break;
+    case 32: launch_grad_w<32>(c, g, ng, a, st); break;
+    default: break;
+  }
+}
+
 bool warp_adj_reuse(const DevCtx& c, int compat) {
   switch (c.N / 32) {
     case 8: return adj_reuse_w<8>(c, compat);

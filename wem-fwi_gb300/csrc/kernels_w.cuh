@@ -1323,10 +1323,12 @@ constexpr int kRowsAdj2 = 8;
 constexpr int kRowsWem = 16;
 
 // which: 4 is WEM with kRowsWem rows per CTA, 5 WEM with one row, 6 the
-// two-warp Born adjoint with one row; exchange buffers per CTA
+// two-warp Born adjoint with one row, 7 the exact modelling gradient
+// (kernels_wg.cuh); exchange buffers per CTA
 inline int nbuf_of(int which) {
   switch (which) {
     case 3: return 2 * kRowsAdj2;
+    case 7: return 2 * kRowsAdj2;
     case 4: return kRowsWem;
     case 5: return 1;
     case 6: return 2;
@@ -1334,7 +1336,9 @@ inline int nbuf_of(int which) {
   }
 }
 // the tables a pass reads: as WEM (0), Born forward (1) or Born adjoint (2)
-inline int tables_of(int which) { return (which == 4 || which == 5) ? 0 : ((which == 3 || which == 6) ? 2 : which); }
+inline int tables_of(int which) {
+  return (which == 4 || which == 5 || which == 7) ? 0 : ((which == 3 || which == 6) ? 2 : which);
+}
 // one-row CTAs leave the taper out of shared memory when the split-step table
 // carries it (SSF)
 inline bool taper_of(const DevCtx& c, int which) { return !((which == 5 || which == 6) && c.fac); }
@@ -1374,7 +1378,7 @@ SlotLayout slot_layout(const DevCtx& c, int pass, int limit) {
   L.nslots = 3;
   // one-row WEM CTAs read the stored row through L2 (prefetched a depth
   // ahead) so that three of them fit on an SM
-  L.row_bytes = (which == 0 && pass != 5) ? rowb : 0;
+  L.row_bytes = (which == 0 && pass != 5 && pass != 7) ? rowb : 0;
   auto total = [&]() {
     return base_bytes<E>(c, pass) + (size_t)L.nslots * L.bytes + (size_t)2 * nbuf_of(pass) * L.row_bytes;
   };

@@ -173,73 +173,16 @@ std::vector<double> taper(int nxg, int pad) {
   return t;
 }
 
-// RefSampler (propagator/src/RefSampler.cpp:28-84).  The as-coded partition
-// keeps the nx-long reference buffer across depths exactly as the
-// reference's member array does; the one deviation is that the scans stop
-// at nx where the reference reads past the end (possible only for nref == 1
-// once nz >= nx - 1).
-void refsampler(const wem_params& p, const std::vector<cd>& s, int nx, int nz, std::vector<cd>& sref,
-                std::vector<signed char>& ref) {
-  const int nref = p.nref;
-  sref.assign((size_t)nz * nref, 0);
-  ref.assign((size_t)nz * nx, -1);
-  const int o = nx / (2 * nref);
-  for (int iz = 0; iz < nz; ++iz)
-    for (int j = 0; j < nref; ++j) {
-      cd v = s[(size_t)iz * nx + o + j * nx / nref];
-      if (!((float)v.real() > 0))
-        throw Fail(WEM_EINVAL, "Ref velocity " + std::to_string(v.real()) + " at the layer " + std::to_string(iz));
-      sref[(size_t)iz * nref + j] = v;
-    }
-  if (p.refs_mode == WEM_REFS_NEAREST) {
-    for (int iz = 0; iz < nz; ++iz)
-      for (int ix = 0; ix < nx; ++ix) {
-        double v = s[(size_t)iz * nx + ix].real();
-        int best = 0;
-        double bd = std::abs(v - sref[(size_t)iz * nref].real());
-        for (int j = 1; j < nref; ++j) {
-          double d = std::abs(v - sref[(size_t)iz * nref + j].real());
-          if (d < bd) { bd = d; best = j; }
-        }
-        ref[(size_t)iz * nx + ix] = (signed char)best;
-      }
-    return;
-  }
-  // the comparisons run on float values, like the reference's float1D buffers
-  std::vector<float> slice(nx), hist(nx, 0.f);
-  std::vector<int> order(nx), rorder(nref);
-  for (int iz = 0; iz < nz; ++iz) {
-    for (int ix = 0; ix < nx; ++ix) slice[ix] = (float)s[(size_t)iz * nx + ix].real();
-    for (int j = 0; j < nref; ++j) hist[j] = (float)sref[(size_t)iz * nref + j].real();
-    std::iota(order.begin(), order.end(), 0);
-    std::iota(rorder.begin(), rorder.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return slice[a] < slice[b]; });
-    std::stable_sort(rorder.begin(), rorder.end(), [&](int a, int b) { return hist[a] < hist[b]; });
-    std::sort(slice.begin(), slice.end());
-    std::sort(hist.begin(), hist.end());
-    std::vector<int> group_of(nx, -1);
-    int off = 0;
-    while (off < nx && slice[off] - hist[0] < hist[1] - slice[off]) off++;
-    for (int i = 0; i < off; ++i) group_of[i] = rorder[0];
-    int beg = off;
-    for (int j = 1; j < nref - 1; ++j) {
-      while (off < nx && slice[off] - hist[j] < hist[j + 1] - slice[off]) off++;
-      for (int i = beg; i < off; ++i) group_of[i] = rorder[j];
-      beg = off;
-    }
-    if (nref == 1) std::fill(group_of.begin(), group_of.end(), -1);  // the last block overwrites the first
-    for (int i = off; i < nx; ++i) group_of[i] = rorder[nref - 1];
-    for (int i = 0; i < nx; ++i) ref[(size_t)iz * nx + order[i]] = (signed char)group_of[i];
-  }
-}
-
 SliceTables make_slice_tables(const wem_params& p, const std::vector<cd>& sp, const std::vector<cd>& dp,
-                              int nxg, bool need_born) {
+                              int nxg, bool need_born, const std::vector<cd>& sref,
+                              const std::vector<signed char>& ref) {
   const int nz = p.nz;
   const size_t ng = (size_t)nz * nxg;
   require(p.nref <= 127, "nref must be <= 127");
+  require(sref.size() == (size_t)nz * p.nref && ref.size() == ng, "RefSampler tables of the wrong size");
   SliceTables t;
-  refsampler(p, sp, nxg, nz, t.sref, t.ref);
+  t.sref = sref;
+  t.ref = ref;
   // SplitStep (SplitStep.cpp:11-15): q = (s - sref)/sqrt(sref) of the point's reference
   t.q.assign(ng, 0);
   for (int iz = 0; iz < nz; ++iz)

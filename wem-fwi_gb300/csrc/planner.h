@@ -56,14 +56,11 @@ struct SliceTables {
   std::vector<cd> a0, b0, a1, b1;  // [nz][nxg] dReflect coefficient pairs
 };
 
-// sp, dp: padded [nz][nxg] slowness^2 and density.
+// sp, dp: padded [nz][nxg] slowness^2 and density; sref [nz][nref] and ref
+// [nz][nxg]: the RefSampler tables of sp (from the device RefSampler)
 SliceTables make_slice_tables(const wem_params& p, const std::vector<cd>& sp, const std::vector<cd>& dp,
-                              int nxg, bool need_born);
-
-// RefSampler of one padded slowness [nz][nx]: reference slownesses [nz][nref]
-// and the reference index of every point [nz][nx] (-1 none)
-void refsampler(const wem_params& p, const std::vector<cd>& s, int nx, int nz, std::vector<cd>& sref,
-                std::vector<signed char>& ref);
+                              int nxg, bool need_born, const std::vector<cd>& sref,
+                              const std::vector<signed char>& ref);
 
 // edge- or zero-pad [nz][nx] complex floats to [nz][nx+2pad] doubles
 std::vector<cd> pad_model(const float* m, int nz, int nx, int pad, bool extend);

@@ -49,14 +49,143 @@ __global__ void k_pad_edge(const float2* in, float2* out, int M, int nz, int nx,
   }
 }
 
-// reference slownesses sampled at x = nxg/(2 nref) + j nxg/nref (RefSampler.cpp:28-39)
-__global__ void k_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref) {
+// reference slownesses sampled at x = nxg/(2 nref) + j nxg/nref
+// (RefSampler.cpp:28-39); the reference refuses a real part <= 0, so the
+// smallest flat index of such an entry goes to *bad (atomicMin)
+__global__ void k_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref, int* bad) {
   const size_t total = (size_t)M * nz * nref;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
     int j = (int)(i % nref);
     size_t mz = i / nref;
     int off = nxg / (2 * nref) + j * nxg / nref;
-    sref[i] = sp[mz * nxg + off];
+    const float2 v = sp[mz * nxg + off];
+    sref[i] = v;
+    if (bad && !(v.x > 0.f)) atomicMin(bad, (int)i);
+  }
+}
+
+// RefSampler partition (RefSampler.cpp:41-84) on the device, one CTA per
+// model slice.  The reference keeps its reference values in an nx-long
+// buffer that survives across depths: every depth overwrites the buffer's
+// first nref entries (after the previous depth's sort, its nref smallest)
+// with the depth's references and sorts the whole buffer again, so the
+// thresholds of depth z are the K = max(nref, 2) smallest values of a
+// multiset that starts as nx zeros and, per depth, loses its nref smallest
+// values and gains the depth's references.  One thread replays that multiset
+// as a zero count plus a binary min-heap in shared memory and writes the K
+// thresholds of every depth; when the zeros cannot run out (nx - nz nref >=
+// K) every threshold is 0 and the replay is skipped.  Every thread also
+// writes, per depth, the references' indices in ascending order of their
+// real part (stable, as the float comparisons of the reference).
+__global__ void k_refs_hist(const float2* sref, int nz, int nxg, int nref, int K, int replay, float* thr,
+                            signed char* rord) {
+  extern __shared__ float heap[];
+  const int m = blockIdx.x;
+  for (int z = threadIdx.x; z < nz; z += blockDim.x) {
+    const float2* r = sref + ((size_t)m * nz + z) * nref;
+    signed char* o = rord + ((size_t)m * nz + z) * nref;
+    for (int j = 0; j < nref; ++j) o[j] = (signed char)j;
+    for (int i = 1; i < nref; ++i) {
+      const signed char key = o[i];
+      const float kv = r[key].x;
+      int k = i - 1;
+      while (k >= 0 && r[o[k]].x > kv) {
+        o[k + 1] = o[k];
+        --k;
+      }
+      o[k + 1] = key;
+    }
+  }
+  float* t = thr + (size_t)m * nz * K;
+  if (!replay) {
+    for (int i = threadIdx.x; i < nz * K; i += blockDim.x) t[i] = 0.f;
+    return;
+  }
+  if (threadIdx.x != 0) return;
+  int zeros = nxg, sz = 0;
+  auto push = [&](float v) {
+    int i = sz++;
+    while (i > 0) {
+      const int p = (i - 1) >> 1;
+      if (heap[p] <= v) break;
+      heap[i] = heap[p];
+      i = p;
+    }
+    heap[i] = v;
+  };
+  // the smallest value of the multiset (zeros counted apart), removed
+  auto pop = [&]() -> float {
+    if (zeros > 0 && (sz == 0 || !(heap[0] < 0.f))) {
+      --zeros;
+      return 0.f;
+    }
+    const float top = heap[0];
+    const float v = heap[--sz];
+    int i = 0;
+    for (;;) {
+      int c = 2 * i + 1;
+      if (c >= sz) break;
+      if (c + 1 < sz && heap[c + 1] < heap[c]) ++c;
+      if (!(heap[c] < v)) break;
+      heap[i] = heap[c];
+      i = c;
+    }
+    if (sz > 0) heap[i] = v;
+    return top;
+  };
+  for (int j = 0; j < nref; ++j) pop();  // depth 0 overwrites nref of the initial zeros
+  for (int z = 0; z < nz; ++z) {
+    const float2* r = sref + ((size_t)m * nz + z) * nref;
+    for (int j = 0; j < nref; ++j) push(r[j].x);
+    // the K smallest are the thresholds; the nref smallest are also the
+    // entries the next depth overwrites, so only the rest go back
+    for (int k = 0; k < K; ++k) t[(size_t)z * K + k] = pop();
+    for (int k = nref; k < K; ++k) push(t[(size_t)z * K + k]);
+  }
+}
+
+// reference index of every point: in the as-coded partition the sorted
+// slowness is cut where `s - h_j < h_{j+1} - s` (float differences) first
+// fails, so a point belongs to the first j < nref - 1 whose test it passes,
+// else to the last, and group j is the j-th reference in ascending order
+// (nref = 1: points passing the test get none, -1).  The nearest partition
+// takes the reference of smallest |s - s_ref| (real parts, double, first of
+// equals).
+__global__ void k_refs_assign(const float2* sp, const float2* sref, const float* thr, const signed char* rord,
+                              int M, int nz, int nxg, int nref, int K, int nearest, signed char* ref) {
+  const size_t plane = (size_t)nz * nxg, total = (size_t)M * plane;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+    const size_t mz = i / nxg;
+    const float v = sp[i].x;
+    int out;
+    if (nearest) {
+      const float2* r = sref + mz * nref;
+      const double dv = (double)v;
+      int best = 0;
+      double bd = fabs(dv - (double)r[0].x);
+      for (int j = 1; j < nref; ++j) {
+        const double d = fabs(dv - (double)r[j].x);
+        if (d < bd) {
+          bd = d;
+          best = j;
+        }
+      }
+      out = best;
+    } else {
+      const float* h = thr + mz * K;
+      if (nref == 1) {
+        out = __fsub_rn(v, h[0]) < __fsub_rn(h[1], v) ? -1 : 0;
+      } else {
+        int g = nref - 1;
+        for (int j = 0; j < nref - 1; ++j)
+          if (__fsub_rn(v, h[j]) < __fsub_rn(h[j + 1], v)) {
+            g = j;
+            break;
+          }
+        out = rord[mz * nref + g];
+      }
+    }
+    ref[i] = (signed char)out;
   }
 }
 
@@ -134,9 +263,32 @@ void launch_pad_edge(const float2* in, float2* out, int M, int nz, int nx, int p
   note_launch();
 }
 
-void launch_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref, cudaStream_t st) {
+void launch_sref(const float2* sp, float2* sref, int M, int nz, int nxg, int nref, int* bad, cudaStream_t st) {
   size_t n = (size_t)M * nz * nref;
-  k_sref<<<grid_of(n), 256, 0, st>>>(sp, sref, M, nz, nxg, nref);
+  k_sref<<<grid_of(n), 256, 0, st>>>(sp, sref, M, nz, nxg, nref, bad);
+  note_launch();
+}
+
+size_t refs_scratch_floats(int M, int nz, int nref) {
+  const int K = nref > 2 ? nref : 2;
+  return (size_t)M * nz * K + ((size_t)M * nz * nref + 3) / 4;
+}
+
+void launch_refsampler(int nearest, const float2* sp, const float2* sref, int M, int nz, int nxg, int nref,
+                       float* scratch, signed char* ref, cudaStream_t st) {
+  const int K = nref > 2 ? nref : 2;
+  float* thr = scratch;
+  signed char* rord = reinterpret_cast<signed char*>(scratch + (size_t)M * nz * K);
+  if (!nearest) {
+    const int replay = (long long)nxg - (long long)nz * nref >= K ? 0 : 1;
+    const size_t smem = replay ? (size_t)nxg * sizeof(float) : 0;
+    if (smem > 48 * 1024)
+      cudaFuncSetAttribute(k_refs_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_refs_hist<<<M, 128, smem, st>>>(sref, nz, nxg, nref, K, replay, thr, rord);
+    note_launch();
+  }
+  const size_t n = (size_t)M * nz * nxg;
+  k_refs_assign<<<grid_of(n), 256, 0, st>>>(sp, sref, thr, rord, M, nz, nxg, nref, K, nearest, ref);
   note_launch();
 }
 

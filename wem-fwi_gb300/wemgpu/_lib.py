@@ -64,6 +64,8 @@ _SIGS = {
     "fwi_create": (_i, [_pp, _v, ctypes.POINTER(_h)]),
     "fwi_destroy": (None, [_h]),
     "fwi_gradient": (_i, [_h, _v, _v, _v, _v, _v, ctypes.POINTER(ctypes.c_double)]),
+    "fwi_gradient_exact": (_i, [_h, _v, _v, _v, _v, _v, ctypes.POINTER(ctypes.c_double), _i]),
+    "wem_gradient": (_i, [_h, _v, _v, _v, _i, _v, _v, _i, _i]),
     "wemop_create": (_i, [_pp, _v, _i, ctypes.POINTER(_h)]),
     "wemop_destroy": (None, [_h]),
     "wemop_onestep": (_i, [_h, _i, _f, _i, _v, _v, _i, _i]),

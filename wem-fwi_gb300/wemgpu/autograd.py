@@ -20,9 +20,17 @@ leaves get the reference's Born-linearised gradient:
 For a real loss and complex leaves, torch's gradient is dL/dRe + i dL/dIm.
 That is B^H r for real time data r, which is what the Born adjoint returns.
 
+``WEMGradient`` is the same forward with the exact derivative as its
+backward: the adjoint-state gradient of the modelled data itself (through
+Reflect, the split step, the phase shift and the reference slowness; the
+library's ``wem_gradient``), which a finite-difference check of the
+modelling pins.  Its ``checkpoint`` k > 1 keeps every k-th depth's
+wavefields and recomputes the depths between (same numbers, bit for bit).
+
 Memory: the Born adjoint stores two or three wavefields per (shot,
-frequency) row.  The library bounds that storage by running the rows in
-chunks sized to free HBM, so no depth checkpointing is needed.
+frequency) row, the exact gradient four (or two every k depths with
+checkpointing).  The library also bounds the storage by running the rows
+in chunks sized to free HBM.
 """
 from __future__ import annotations
 
@@ -57,8 +65,35 @@ class FWIGradient(torch.autograd.Function):
         return g_s2, g_rho, None, None
 
 
-def modelled_data(s2, rho, wem: WemOp, born: BornOp):
-    """Synthetic data of (s2, rho) that backpropagates through the Born adjoint."""
+class WEMGradient(torch.autograd.Function):
+    """d = WEM(s2, rho); backward: (g_s2, g_rho) = J^H(dL/dd), J the exact
+    derivative of the modelling at (s2, rho)."""
+
+    @staticmethod
+    def forward(ctx, s2, rho, wem: WemOp, checkpoint: int = 0):
+        if not (s2.is_cuda and rho.is_cuda):
+            raise ValueError("WEMGradient works on CUDA tensors")
+        s2c, rhoc = s2.detach().contiguous(), rho.detach().contiguous()
+        d = torch.empty(wem.data_shape(0), dtype=torch.float32, device=s2.device)
+        wem.forward(s2c, rhoc, d)
+        ctx.save_for_backward(s2c, rhoc)
+        ctx.wem, ctx.checkpoint = wem, int(checkpoint)
+        return d
+
+    @staticmethod
+    def backward(ctx, grad_d):
+        s2, rho = ctx.saved_tensors
+        g_s2, g_rho = torch.zeros_like(s2), torch.zeros_like(rho)
+        ctx.wem.gradient(s2, rho, grad_d.contiguous(), g_s2, g_rho, checkpoint=ctx.checkpoint)
+        return g_s2, g_rho, None, None
+
+
+def modelled_data(s2, rho, wem: WemOp, born: BornOp = None, exact: bool = False, checkpoint: int = 0):
+    """Synthetic data of (s2, rho) that backpropagates through the Born
+    adjoint (the reference's gradient) or, with exact=True, through the
+    exact derivative of the modelling."""
+    if exact:
+        return WEMGradient.apply(s2, rho, wem, checkpoint)
     return FWIGradient.apply(s2, rho, wem, born)
 
 
@@ -76,8 +111,9 @@ class FwiObjective:
     gradients are returned as new CUDA tensors).
     """
 
-    def __init__(self, p: WemParams, wavelet, d_obs, device=None):
+    def __init__(self, p: WemParams, wavelet, d_obs, device=None, exact=False, checkpoint=0):
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.exact, self.checkpoint = bool(exact), int(checkpoint)
         self.op = FwiOp(p, wavelet)
         self.d_obs = torch.as_tensor(d_obs).to(self.device, torch.float32).contiguous()
         if tuple(self.d_obs.shape) != tuple(self.op.data_shape(0)):
@@ -101,7 +137,7 @@ class FwiObjective:
         rho_d, _ = self._to_device(rho, 1)
         g0 = torch.empty_like(s2_d)
         g1 = torch.empty_like(rho_d)
-        loss = self.op.gradient(s2_d, rho_d, self.d_obs, g0, g1)
+        loss = self.op.gradient(s2_d, rho_d, self.d_obs, g0, g1, exact=self.exact, checkpoint=self.checkpoint)
         if not host:
             return loss, g0, g1
         self._pin_out[0].copy_(g0)

@@ -21,8 +21,8 @@ LIB = os.path.join(OUT_DIR, "libwemgpu.so")
 OBJ_DIR = os.path.join(OUT_DIR, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels.cu", "kernels_w.cu", "tables.cu", "noalloc.cu", "interp.cu", "rowops.cu", "api.cpp", "planner.cpp", "cmap.cpp"] + [
-    f"kw_e{e}_{p}.cu" for e in (32, 24, 16, 12, 8) for p in ("adj", "adj1", "wem", "fwd")]
+SOURCES = ["kernels.cu", "kernels_w.cu", "tables.cu", "timefreq.cu", "grad.cu", "noalloc.cu", "interp.cu", "rowops.cu", "api.cpp", "planner.cpp", "cmap.cpp"] + [
+    f"kw_e{e}_{p}.cu" for e in (32, 24, 16, 12, 8) for p in ("adj", "adj1", "wem", "fwd", "grad")]
 
 # host code whose float results must not depend on the machine: the
 # conformal maps turn float coordinates into grid indices, so no multiply-add
@@ -76,7 +76,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcublas", "-lcudart"]
+    cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -110,6 +110,17 @@ class WemOp(_Base):
                   ptr(rho, np.complex64, self.model_shape, "density"), d, kind, int(bool(add)))
         return data
 
+    def gradient(self, s2, rho, data_grad, g_s2, g_rho, add=False, checkpoint=0):
+        """(g_s2, g_rho) (+)= J^H data_grad: the exact derivative of the
+        modelling at (s2, rho), transposed (wem_gradient); checkpoint k > 1
+        keeps every k-th depth and recomputes between."""
+        d, kind = self._data_ptr(data_grad, False)
+        _lib.call("wem_gradient", self.h, ptr(s2, np.complex64, self.model_shape, "slowness"),
+                  ptr(rho, np.complex64, self.model_shape, "density"), d, kind,
+                  ptr(g_s2, np.complex64, self.model_shape, "g_slowness", True),
+                  ptr(g_rho, np.complex64, self.model_shape, "g_density", True), int(bool(add)), int(checkpoint))
+        return g_s2, g_rho
+
 
 class BornOp(_Base):
     """Born operator (BornFull, propagator/src/BornFull.cpp:13-117)."""
@@ -152,13 +163,19 @@ class FwiOp(_Base):
         _lib.call("fwi_create", ctypes.byref(self.p), self.wavelet.ctypes.data_as(ctypes.c_void_p),
                   ctypes.byref(self.h))
 
-    def gradient(self, s2, rho, d_obs, g_s2, g_rho) -> float:
+    def gradient(self, s2, rho, d_obs, g_s2, g_rho, exact=False, checkpoint=0) -> float:
+        """Loss and gradient; exact=True differentiates the modelling itself
+        (fwi_gradient_exact) instead of the reference's Born adjoint."""
         loss = ctypes.c_double()
-        _lib.call("fwi_gradient", self.h, ptr(s2, np.complex64, self.model_shape, "slowness"),
-                  ptr(rho, np.complex64, self.model_shape, "density"),
-                  ptr(d_obs, np.float32, self.data_shape(WEM_DATA_TIME), "d_obs"),
-                  ptr(g_s2, np.complex64, self.model_shape, "g_slowness", True),
-                  ptr(g_rho, np.complex64, self.model_shape, "g_density", True), ctypes.byref(loss))
+        args = [self.h, ptr(s2, np.complex64, self.model_shape, "slowness"),
+                ptr(rho, np.complex64, self.model_shape, "density"),
+                ptr(d_obs, np.float32, self.data_shape(WEM_DATA_TIME), "d_obs"),
+                ptr(g_s2, np.complex64, self.model_shape, "g_slowness", True),
+                ptr(g_rho, np.complex64, self.model_shape, "g_density", True), ctypes.byref(loss)]
+        if exact:
+            _lib.call("fwi_gradient_exact", *args, int(checkpoint))
+        else:
+            _lib.call("fwi_gradient", *args)
         return loss.value
 
 
