@@ -359,9 +359,13 @@ def run_gpu(args, rank, world):
         plain = {"s_per_iter": plain_s, "sample": f"{ns_p} shots x {nf} freqs, scaled to {p.ns} shots",
                  "batched_speedup": plain_s / s_per_iter}
 
-    cpu = None
+    cpu, cpu_fft = None, None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_sample(cfg, seconds=args.cpu_seconds)
+        cpu_fft = cpu_fft_bound(p, nf)
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = parity_sample(cfg, p, wem, s0, rho, d_obs)
 
     line = {
         "metric": METRIC, "value": value, "unit": "depth-steps/s", "n_gpus": world, "steps": args.steps,
@@ -383,10 +387,84 @@ def run_gpu(args, rank, world):
         "gpu_launches": gpu_launches,
         "plain_gpu": plain,
         "cpu_baseline": cpu,
+        "cpu_fft_bound": cpu_fft,
+        "parity": parity,
         "clocks": clocks,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def parity_sample(cfg, p, wem, s0, rho, d_obs):
+    """rel-L2 of the benchmarked kernels' results against the oracle (fp32
+    restatement and fp64 twin), outside the timed region: the first two
+    shots of the full batch's modelling (the timed step's WEM pass), and the
+    FWI gradient of a two-shot block (the timed call on 2 of the 32 shots;
+    the tests hold the full call to the sum of its blocks)."""
+    import torch
+    from oracle import oracle as O
+    from wemgpu import synthetic as S
+    from wemgpu.core import FwiOp
+    from wemgpu.params import WEM_DATA_TIME
+    O.build()
+    t0 = time.perf_counter()
+    wav = cfg["wavelet"]
+    d = torch.zeros_like(d_obs)
+    wem.forward(s0, rho, d)
+    cfg2 = dict(cfg, par=dict(cfg["par"], ns=2))
+    p2 = S.params_of(cfg2)
+    obs2 = d_obs[:2].contiguous()
+    g0, g1 = torch.zeros_like(s0), torch.zeros_like(s0)
+    FwiOp(p2, wav).gradient(s0, rho, obs2, g0, g1)
+    torch.cuda.synchronize()
+    d2 = d[:2].cpu().numpy()
+    # the oracle's gradient of the block's own residual (a small difference
+    # of two modelled data sets: each side's modelling error would be
+    # amplified by |syn| / |res| were the oracle to form it itself)
+    res = d2 - obs2.cpu().numpy()
+    g0h, g1h = g0.cpu().numpy(), g1.cpu().numpy()
+
+    def rel(a, b):
+        a, b = np.asarray(a, np.complex128), np.asarray(b, np.complex128)
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    out = {"tolerance": 1e-4}
+    for prec in (32, 64):
+        syn = O.wem_forward(p2, wav, cfg["slow"], cfg["rho"], kind=WEM_DATA_TIME, prec=prec)
+        o0, o1 = O.born_adjoint(p2, wav, cfg["slow"], cfg["rho"], res, kind=WEM_DATA_TIME, prec=prec)
+        out[f"wem_vs_fp{prec}"] = rel(d2, syn)
+        out[f"gradient_vs_fp{prec}"] = max(rel(g0h, o0), rel(g1h, o1))
+    out["sample"] = ("shots 0-1 of the full-batch modelling; fwi_gradient of a 2-shot block against the "
+                     f"oracle's Born adjoint of its residual (oracle {time.perf_counter() - t0:.0f} s on the host)")
+    return out
+
+
+def cpu_fft_bound(p, nfreq, seconds=5.0):
+    """A bound on how fast a tuned CPU code could take the workload's depth
+    steps on the host cores: the bare split-step depth step of the rows of
+    one shot (forward FFT, phase-shift multiply, inverse FFT, split-step
+    multiply; no injection, recording, tables or imaging) with torch.fft
+    (pocketfft, vectorised) on every host thread.  Every depth-step of the
+    reference costs at least this, so the GPU's ratio to this figure bounds
+    from below its speed-up over any CPU implementation of the path on this
+    host."""
+    import torch
+    nthreads = os.cpu_count() or 1
+    torch.set_num_threads(nthreads)
+    n = p.nx + 2 * (p.pad + p.tap)
+    rows = nfreq  # one shot's rows
+    g = torch.Generator().manual_seed(0)
+    x = torch.randn(rows, n, dtype=torch.complex64, generator=g)
+    ph = torch.exp(1j * torch.rand(rows, n, generator=g)).to(torch.complex64)
+    fac = torch.exp(1j * torch.rand(rows, n, generator=g)).to(torch.complex64) / n
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        for _ in range(10):
+            x = torch.fft.ifft(torch.fft.fft(x) * ph, norm="forward") * fac
+        steps += 10
+    dt = time.perf_counter() - t0
+    return {"value": rows * steps / dt, "unit": "depth-steps/s", "cores": nthreads, "kind": "fft-bound",
+            "sample": f"{rows} rows of N = {n}, {steps} bare split-step depth steps with torch.fft, {dt:.1f} s"}
 
 
 def cpu_sample(cfg, seconds=15.0, nthreads=0, nshots=0):
@@ -430,19 +508,24 @@ def run_reference(args, rank, world):
     per_step = min(10.0, max(1.0, 120.0 / (args.warmup + args.steps)))
     first = cpu_sample(cfg, seconds=per_step)
     nshots = int(first["sample"].split()[0])
-    res = []
+    res, durs = [], []
     for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
         r = cpu_sample(cfg, nshots=nshots) if i else first
         if i >= args.warmup:
             res.append(r["value"])
+            durs.append(time.perf_counter() - t0)
     v = float(np.median(res))
     from oracle import oracle as O
     from wemgpu import synthetic as S
     p = S.params_of(cfg)
     nf = O.count_freqs(p)[0]
     per_iter = row_steps(p, nf) / v
+    # a step is one timed sample of the workload (its duration); s_per_iter
+    # is the whole gradient at the measured rate
     line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "depth-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_iter * 1e3, "s_per_iter": per_iter,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.median(durs)) * 1e3,
+            "s_per_iter": per_iter,
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c64", "data": "synthetic (seeded c3 model, see wemgpu/synthetic.py)",
             "config": config_of(p, nf, 1, args.small),
@@ -547,6 +630,7 @@ def main():
     ap.add_argument("--small-shots", type=int, default=8, help="shots of the reduced case")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the results")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3"],
                     help="c3 is the benchmark line; c1 and c2 print their own timings for the record")

@@ -18,11 +18,18 @@ TOL_OP = 1e-4
 TOL_STEP = 1e-5
 
 
-@pytest.mark.parametrize("prop,nref,mode", [("ssf", 1, "ascoded"), ("pspi", 3, "ascoded"),
-                                            ("ssf", 3, "ascoded"), ("pspi", 3, "nearest")])
-def test_refsampler_tables_bit_exact(gpu_lib, oracle, prop, nref, mode):
+@pytest.mark.parametrize("prop,nref,mode,nx,nz", [("ssf", 1, "ascoded", 52, 24), ("pspi", 3, "ascoded", 52, 24),
+                                                  ("ssf", 3, "ascoded", 52, 24), ("pspi", 3, "nearest", 52, 24),
+                                                  ("pspi", 4, "ascoded", 52, 24), ("pspi", 4, "nearest", 52, 24),
+                                                  # the zero history runs out (nz nref > nxg - nref)
+                                                  ("pspi", 4, "ascoded", 60, 40), ("pspi", 3, "ascoded", 20, 30),
+                                                  ("ssf", 1, "ascoded", 20, 40)])
+def test_refsampler_tables_bit_exact(gpu_lib, oracle, prop, nref, mode, nx, nz):
+    """The device RefSampler (the operators' own partition kernels, through
+    the row-level handle) equals the oracle's line-faithful restatement of
+    RefSampler.cpp:41-84 point for point."""
     from wemgpu.core import RowOps
-    p, par, wav, s, rho = small_case(prop=prop, nref=nref)
+    p, par, wav, s, rho = small_case(prop=prop, nref=nref, nx=nx, nz=nz)
     p.refs_mode = 1 if mode == "nearest" else 0
     sp = pad_edge(s, p.pad)
     ops = RowOps(p, sp)
@@ -30,6 +37,41 @@ def test_refsampler_tables_bit_exact(gpu_lib, oracle, prop, nref, mode):
     sref_o, idx_o = oracle.refsampler(p, sp)
     assert np.array_equal(idx_g, idx_o)
     assert np.array_equal(sref_g, sref_o)
+
+
+@pytest.mark.parametrize("name,nref", [("c2", 4), ("c2", 3), ("c3", 1)])
+def test_refsampler_full_size_models(gpu_lib, oracle, name, nref):
+    """The partition of the benchmark configurations' own models (c2: 1024 x
+    500, c3: 768 x 300) and a history that runs out; bit-exact."""
+    from wemgpu import synthetic as S
+    from wemgpu.core import RowOps
+    cfg = S.CONFIGS[name]()
+    cfg["par"] = dict(cfg["par"], nref=nref, prop="pspi")
+    p = S.params_of(cfg)
+    sp = np.ascontiguousarray(cfg["slow"])
+    sref_g, idx_g = RowOps(p, sp).refsampler()
+    sref_o, idx_o = oracle.refsampler(p, sp)
+    assert np.array_equal(sref_g, sref_o)
+    assert np.array_equal(idx_g, idx_o)
+
+
+def test_refsampler_rejects_nonpositive_reference(gpu_lib):
+    """A reference slowness whose real part is not positive fails the call
+    with the reference's message (RefSampler.cpp:35-36), on the operators'
+    device path as on the row-level one."""
+    from wemgpu._lib import WemError
+    from wemgpu.core import BornOp, RowOps
+    p, par, wav, s, rho = small_case(prop="pspi", nref=2)
+    bad = s.copy()
+    bad[5, :] = -1e-7
+    with pytest.raises(WemError, match="Ref velocity .* at the layer 5"):
+        BornOp(p, wav, bad, rho)
+    op = BornOp(p, wav, s, rho)
+    with pytest.raises(WemError, match="at the layer 5"):
+        op.set_background(bad, rho)
+    op.set_background(s, rho)
+    with pytest.raises(WemError, match="at the layer 5"):
+        RowOps(p, pad_edge(bad, p.pad))
 
 
 @pytest.mark.parametrize("prop,nref", [("ssf", 1), ("pspi", 1), ("pspi", 3), ("ssf", 2)])
@@ -330,8 +372,8 @@ def test_warp_path_is_deterministic(gpu_lib, case):
 
 def test_refsampler_history_exhausted(gpu_lib, oracle):
     """nref = 1 with nz > nxg - 2: the reference's zero history runs out and
-    the as-coded partition drops points (RefSampler.cpp:63-81); the library
-    then builds the partition on the host exactly as the oracle does."""
+    the as-coded partition drops points (RefSampler.cpp:63-81); the device
+    RefSampler replays that history as the oracle does."""
     from wemgpu.core import WemOp
     p, par, wav, s, rho = small_case(nx=20, nz=24, pad=0, tap=6, ns=1)
     d = np.zeros((p.ns, p.nr, p.nt), np.float32)
@@ -514,3 +556,31 @@ def test_born_dot_reference_setup(gpu_lib):
             assert ratio < 1e-5, ratio
         else:
             assert np.isfinite(ratio)
+
+
+# time axes n = nt + tpad: the FFT path (every prime factor <= 7: 1536 =
+# 2^9 3 as the benchmark's, 960 with a radix 5, 1176 with radix 7, and a
+# time pad) and the restricted DFT (1018 = 2 x 509, 824 = 8 x 103 with a
+# time pad, 10010 = 2 5 7 11 13)
+@pytest.mark.parametrize("nt,tpad,dt", [(1536, 0, 0.004), (960, 0, 0.005), (1000, 176, 0.004), (1018, 0, 0.004),
+                                        (700, 124, 0.005), (10010, 0, 0.0005)])
+def test_time_axis_lengths(gpu_lib, oracle, nt, tpad, dt):
+    from wemgpu.core import BornOp, FwiOp, WemOp
+    p, par, wav, s, rho = small_case(nz=10, nt=nt, dt=dt)
+    p.tpad = tpad
+    d = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    WemOp(p, wav).forward(s, rho, d)
+    o32 = oracle.wem_forward(p, wav, s, rho, kind=WEM_DATA_TIME, prec=32)
+    o64 = oracle.wem_forward(p, wav, s, rho, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(d, o32) < TOL_OP and rel_l2(d, o64) < TOL_OP, (rel_l2(d, o32), rel_l2(d, o64))
+    rng = np.random.default_rng(8)
+    obs = (o32 * (1 + 0.1 * rng.standard_normal(o32.shape))).astype(np.float32)
+    g0, g1 = np.zeros_like(s), np.zeros_like(s)
+    loss = FwiOp(p, wav).gradient(s, rho, obs, g0, g1)
+    res = (d - obs).astype(np.float32)
+    assert loss == pytest.approx(0.5 * float(np.sum(res.astype(np.float64) ** 2)), rel=1e-5)
+    q0, q1 = oracle.born_adjoint(p, wav, s, rho, res, kind=WEM_DATA_TIME, prec=64)
+    assert rel_l2(g0, q0) < TOL_OP and rel_l2(g1, q1) < TOL_OP
+    a0, a1 = np.zeros_like(s), np.zeros_like(s)
+    BornOp(p, wav, s, rho).adjoint(a0, a1, res)
+    assert rel_l2(g0, a0) < 1e-6 and rel_l2(g1, a1) < 1e-6
