@@ -440,14 +440,14 @@ def parity_sample(cfg, p, wem, s0, rho, d_obs):
 
 
 def cpu_fft_bound(p, nfreq, seconds=5.0):
-    """A bound on how fast a tuned CPU code could take the workload's depth
-    steps on the host cores: the bare split-step depth step of the rows of
-    one shot (forward FFT, phase-shift multiply, inverse FFT, split-step
-    multiply; no injection, recording, tables or imaging) with torch.fft
-    (pocketfft, vectorised) on every host thread.  Every depth-step of the
-    reference costs at least this, so the GPU's ratio to this figure bounds
-    from below its speed-up over any CPU implementation of the path on this
-    host."""
+    """The bare split-step depth step of the rows of one shot (forward FFT,
+    phase-shift multiply, inverse FFT, split-step multiply; no injection,
+    recording, tables or imaging) with torch.fft (pocketfft, vectorised) on
+    every host thread: what a library FFT gives on the host cores for the
+    transform pair that every depth-step of the reference's SSF passes
+    takes.  It is a second CPU figure beside the oracle's, not a proven
+    bound: a code tuned for these cores (FFTW with ISPC, one row per thread)
+    may run faster."""
     import torch
     nthreads = os.cpu_count() or 1
     torch.set_num_threads(nthreads)

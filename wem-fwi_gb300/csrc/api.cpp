@@ -593,7 +593,7 @@ class Engine {
     }
     const int cke = ck > 1 ? ck : 0;
     const int ncp = cke ? (nz - 1) / cke + 1 : nz;
-    const size_t segl = (size_t)(cke + 1) * (2 * nxg + 2 * N) + N;
+    const size_t segl = (size_t)(cke + 1) * (2 * nxg + 2 * N) + 2 * N;
     const int G = std::min(geo_.ns, grad_rows_per_group());
     const size_t row_store = cke ? (2 * (size_t)ncp * nxg + segl) * 8 : (2 * plane + 2 * splane) * 8;
     float2* IR = ir_.as<float2>(plane);

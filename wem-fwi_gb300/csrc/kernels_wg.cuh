@@ -65,7 +65,7 @@ __device__ __forceinline__ float2 warp_csum(float2 v) {
 // every ck depths plus a segment of ck + 1 recomputed depths per row
 struct GradStore {
   float2 *bg, *t, *sw, *sg;  // full: [rows][nz][nxg] x 2, [rows][nz][N] x 2; checkpoints: bg, t [rows][ncp][nxg]
-  float2* seg;               // [rows][(ck + 1)(2 nxg + 2 N) + N] (checkpoints only)
+  float2* seg;               // [rows][(ck + 1)(2 nxg + 2 N) + 2 N] (checkpoints only)
   float2* il;                // [groups][nz][nxg] split-step image
   float2* ir;                // [groups][nz][nxg] Reflect image
   float2* qs;                // [2][rows][nz] reference terms (source side, receiver side)
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_wem_grad(DevCtx c, SlotLayou
   float2* TT = gs.t + rid * (size_t)ncp * nxg;
   float2* SW = ck > 1 ? nullptr : gs.sw + rid * splane;
   float2* SG = ck > 1 ? nullptr : gs.sg + rid * splane;
-  float2* SEG = ck > 1 ? gs.seg + rid * ((size_t)(ck + 1) * (2 * nxg + 2 * N) + N) : nullptr;
+  float2* SEG = ck > 1 ? gs.seg + rid * ((size_t)(ck + 1) * (2 * nxg + 2 * N) + 2 * N) : nullptr;
   float2* IR = gs.ir + (size_t)blockIdx.x * plane;
   float2* IL = gs.il + (size_t)blockIdx.x * plane;
   float2* QS = gs.qs + rid * nz;                               // source side
@@ -204,12 +204,14 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_wem_grad(DevCtx c, SlotLayou
 
   // ---------------- segment recompute (checkpoints): depths z0 .. z1 of
   // bg, T and their spectra from the checkpoint at z0; tables from global.
-  // The recompute runs in S: the up sweep's state waits in the segment's
-  // last slot meanwhile.
+  // The recompute runs in S: the up sweep's state waits in one of the
+  // segment's two last slots meanwhile (one per warp of the row).  Each
+  // side reads rows the other side recomputes, so the caller synchronises
+  // the block after it.
   auto recompute = [&](int z0, bool keep_state) {
     zs = z0;
     if (!act) return;
-    float2* save = SEG + (size_t)(ck + 1) * (2 * nxg + 2 * N);
+    float2* save = SEG + (size_t)(ck + 1) * (2 * nxg + 2 * N) + (recv ? N : 0);
     if (keep_state) store_spec(save, S);
     const int z1 = min(z0 + ck, nz - 1);
     if (!recv) {
@@ -277,7 +279,10 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_wem_grad(DevCtx c, SlotLayou
     __syncthreads();  // the image buffers are summed; slot (z - 2) % 3 is free
     ring.issue(z - 2);
     cp_commit();
-    if (ck > 1 && z - 1 < zs) recompute(((z - 1) / ck) * ck, true);
+    if (ck > 1 && z - 1 < zs) {
+      recompute(((z - 1) / ck) * ck, true);
+      __syncthreads();  // bg rows for the receiver sides, T rows for the source sides
+    }
     if (act) {
       const float2* gam = c.gam + ((size_t)f * nz + (recv ? z - 1 : z)) * N;
       if (!recv) {
