@@ -620,6 +620,109 @@ def run_config(args):
     print(json.dumps(out), flush=True)
 
 
+def run_c4(args):
+    """The subsurface-offset extended Born (c4: nh = 21 lags, 64 shots of
+    uneven aperture), timed for the record: forward (reflectivity -> time
+    traces) and adjoint (traces -> lag image), CUDA events around each call
+    on resident inputs, with the per-kernel times, a full-size dot test, and
+    the first shot against the oracle (fp32 and fp64, the oracle also timed
+    on it with every host thread)."""
+    import torch
+    import wemgpu
+    from wemgpu import _lib, synthetic as S
+    from wemgpu.core import BornOffsetOp
+    from oracle import oracle as O
+
+    wemgpu.build()
+    dev = torch.device("cuda:0")
+    cfg = S.c4()
+    if args.small:  # a reduced case of the same kernels for profiling captures
+        ns = min(cfg["par"]["ns"], args.small_shots)
+        cfg["par"] = dict(cfg["par"], ns=ns, dsx=cfg["par"]["dsx"], fmax=cfg["par"]["fmin"] + 2.0)
+        cfg["apertures"] = cfg["apertures"][:ns]
+    p = S.params_of(cfg)
+    wav, nh, ap = cfg["wavelet"], cfg["nh"], cfg["apertures"]
+    op = BornOffsetOp(p, wav, cfg["slow"], nh, ap)
+    nf = op.nfreq()
+    r = torch.from_numpy(cfg["refl"]).to(dev)
+    d = torch.zeros((p.ns, p.nr, p.nt), dtype=torch.float32, device=dev)
+    img = torch.zeros_like(r)
+    n_rows, _ = op.rows()
+    rows = p.ns * nf
+    lib = _lib.load()
+    out = {"workload": "c4 extended Born (subsurface offset): forward and adjoint", "small": bool(args.small),
+           "nx": p.nx, "nz": p.nz, "shots": p.ns, "freqs": nf, "nh": nh, "aperture_cells": [int(ap[:, 1].min()),
+           int(ap[:, 1].max())], "row_lengths": {str(n): int((n_rows == n).sum()) for n in sorted(set(n_rows))},
+           "prop": "ssf", "ops": {}}
+    for name, fn in (("forward", lambda: op.forward(r, d)), ("adjoint", lambda: op.adjoint(img, d))):
+        for _ in range(max(args.warmup, 1)):
+            fn()
+        torch.cuda.synchronize()
+        lib.wem_stats_reset()
+        lib.wem_stats_enable(1)
+        fn()
+        lib.wem_stats_enable(0)
+        kern = {k: round(_lib.kernel_stats(k)[0], 3) for k in ("k_off_down", "k_off_up", "k_off_upadj",
+                                                                "k_off_source", "k_off_image")}
+        kern = {k: v for k, v in kern.items() if v > 0}
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(args.steps):
+            fn()
+        b.record()
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b) / args.steps
+        steps = 2 * rows * (p.nz - 1)  # two sweeps per row
+        out["ops"][name] = {"ms": ms, "depth_steps_per_s": steps / (ms / 1e3), "sweeps": 2, "kernels_ms": kern}
+    # algorithmic bytes of the lag kernels: each reads two fields and writes
+    # at most one, 8 bytes a point of every row's aperture
+    pts = float(sum(nf * p.nz * (int(w) + 2 * p.pad) for w in ap[:, 1]))
+    hbm = peaks()[0]
+    for k, op_name, nbytes in (("k_off_source", "forward", 16 * pts), ("k_off_image", "adjoint", 16 * pts)):
+        ms = out["ops"][op_name]["kernels_ms"].get(k)
+        if ms:
+            out["ops"][op_name][k + "_gbs"] = nbytes / (ms / 1e3) / 1e9
+            out["ops"][op_name][k + "_frac_of_measured_hbm"] = nbytes / (ms / 1e3) / 1e9 / hbm
+    # dot test at full size: <L r, g> = <r, L^H g> with complex bins
+    rng = np.random.default_rng(7)
+    nb = p.nt + p.tpad
+    df = torch.zeros((p.ns, p.nr, nb), dtype=torch.complex64, device=dev)
+    op.forward(r, df)
+    g = torch.from_numpy((rng.standard_normal(df.shape) + 1j * rng.standard_normal(df.shape)).astype(np.complex64)).to(dev)
+    im2 = torch.zeros_like(img)
+    op.adjoint(im2, g)
+    lhs = complex(torch.vdot(df.flatten().to(torch.complex128), g.flatten().to(torch.complex128)))
+    rhs = complex(torch.vdot(r.flatten().to(torch.complex128), im2.flatten().to(torch.complex128)))
+    out["dot_ratio"] = abs(lhs - rhs) / abs(lhs)
+    if not args.no_parity:
+        one = dict(cfg, par=dict(cfg["par"], ns=1))
+        p1 = S.params_of(one)
+        op1 = BornOffsetOp(p1, wav, cfg["slow"], nh, ap[:1])
+        taps = list(op1.rows()[1])
+        d1 = d[:1].cpu().numpy()  # the full batch's first shot
+        gd = rng.standard_normal(d1.shape).astype(np.float32)
+        i1 = np.zeros((nh, p.nz, p.nx), np.complex64)
+        op1.adjoint(i1, gd)
+        nt = os.cpu_count() or 1
+        par = {}
+        t0 = time.perf_counter()
+        for prec in (32, 64):
+            o = O.offborn_forward(p1, wav, cfg["slow"], cfg["refl"], ap[:1], taps, kind=0, prec=prec, nthreads=nt)
+            if prec == 32:
+                t1 = time.perf_counter()
+            oi = O.offborn_adjoint(p1, wav, cfg["slow"], nh, gd, ap[:1], taps, kind=0, prec=prec, nthreads=nt)
+            if prec == 32:
+                t2 = time.perf_counter()
+            par[f"forward_vs_fp{prec}"] = float(np.linalg.norm(d1 - o) / np.linalg.norm(o))
+            par[f"adjoint_vs_fp{prec}"] = float(np.linalg.norm(i1 - oi) / np.linalg.norm(oi))
+        out["parity"] = dict(par, tolerance=1e-4, sample="shot 0 at full size (the full batch's forward; "
+                             "a one-shot operator's adjoint)")
+        w0 = int(ap[0, 1]) + 2 * p.pad
+        out["cpu_oracle"] = {"s_one_shot_forward": t1 - t0, "s_one_shot_adjoint": t2 - t1, "cores": nt, "kind": "port",
+                             "depth_steps_per_s": 4 * nf * (p.nz - 1) / (t2 - t0), "aperture_cells": w0}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -632,9 +735,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the results")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3"],
-                    help="c3 is the benchmark line; c1 and c2 print their own timings for the record")
+    ap.add_argument("--workload", default="c3", choices=["c1", "c2", "c3", "c4"],
+                    help="c3 is the benchmark line; c1, c2 and c4 print their own timings for the record")
     args = ap.parse_args()
+    if args.workload == "c4":
+        run_c4(args)
+        return
     if args.workload != "c3":
         run_config(args)
         return

@@ -136,7 +136,9 @@ const char* wem_version(void);
 /* Kernel timing (no counterpart in the reference: measurement support).
  * While enabled, every pass kernel is bracketed by CUDA events on the stream
  * it is launched on; per-kernel totals accumulate until reset.  Kernel names:
- * "k_wem", "k_born_fwd", "k_born_adj". */
+ * "k_wem", "k_born_fwd", "k_born_adj", "k_wem_grad"; the offset Born's
+ * "k_off_down", "k_off_up", "k_off_upadj" (one sweep over every row, all its
+ * launches), "k_off_source", "k_off_image". */
 int wem_stats_enable(int on);
 int wem_stats_get(const char* kernel, double* total_ms, long long* launches);
 int wem_stats_reset(void);
@@ -213,6 +215,34 @@ void bornrefl_destroy(bornrefl_handle* h);
 int bornrefl_set_background(bornrefl_handle* h, const void* bg_slow2);
 int bornrefl_forward(bornrefl_handle* h, const void* model, void* data, int data_kind, int add);
 int bornrefl_adjoint(bornrefl_handle* h, void* model, const void* data, int data_kind, int add);
+
+/* Subsurface-offset extended reflectivity Born (no reference counterpart;
+ * the extension the reference's BornRefl, propagator/src/ext_born_refl.cpp:
+ * 8-105, and IC, propagator/src/ic.cpp:5-29, reduce from at one lag).
+ * Model r [nh][nz][nx] complex64: the reflectivity at horizontal lag
+ * l = i - (nh - 1)/2 grid cells (nh odd, <= 41).  Per (shot, frequency):
+ *   forward  bg = Down(src); sc(x) = sum_l r_l(x - l) bg(x - 2l); record Up(sc)
+ *   adjoint  bg = Down(src); a = Up^H(data); image_l(x) += conj(bg(x - l)) a(x + l)
+ * Shot s propagates on its aperture, model columns [ap_x0[s], ap_x0[s] +
+ * ap_w[s]) (even widths; NULL: the whole model for every shot), edge-padded
+ * by pad and zero-padded to the row length N_s, the smallest of 256, 384,
+ * 512, 768, 1024 with N_s >= ap_w[s] + 2 pad + 2 tap, equally on both sides
+ * (bornoff_rows reports N_s and the leading zero pad).  The aperture is a
+ * cropped model as WEM.from_subspace builds it (propagator/src/python/
+ * WEM.py:24-30): the reference slowness comes from the aperture, receivers
+ * outside it record zero and are ignored by the adjoint.  One reference
+ * slowness (nref = 1), SSF or PSPI; background slowness^2 with unit
+ * density.  With nh = 1 and full apertures the operator is BornRefl with
+ * the same reflectivity at every frequency, summed over frequencies in the
+ * adjoint. */
+typedef struct bornoff_handle bornoff_handle;
+int bornoff_create(const wem_params* p, const float* wavelet, const void* bg_slow2, int nh, const int* ap_x0,
+                   const int* ap_w, bornoff_handle** out);
+void bornoff_destroy(bornoff_handle* h);
+int bornoff_set_background(bornoff_handle* h, const void* bg_slow2);
+int bornoff_forward(bornoff_handle* h, const void* model, void* data, int data_kind, int add);
+int bornoff_adjoint(bornoff_handle* h, void* model, const void* data, int data_kind, int add);
+int bornoff_rows(bornoff_handle* h, int* row_len, int* tap);
 
 typedef struct borntomo_handle borntomo_handle;
 int borntomo_create(const wem_params* p, const float* wavelet, const void* bg_slow2, borntomo_handle** out);

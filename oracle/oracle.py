@@ -164,6 +164,36 @@ def bornrefl_adjoint(p, wavelet, bs2, data, kind=WEM_DATA_TIME, add=False, prec=
     return model
 
 
+def _apertures(p, apertures, taps):
+    ap = np.ascontiguousarray(np.asarray(apertures, dtype=np.int32).reshape(p.ns, 2))
+    x0, w = np.ascontiguousarray(ap[:, 0]), np.ascontiguousarray(ap[:, 1])
+    return x0, w, np.ascontiguousarray(np.asarray(taps, dtype=np.int32).reshape(p.ns))
+
+
+def offborn_forward(p, wavelet, bs2, model, apertures, taps, kind=WEM_DATA_TIME, data=None, add=False, prec=32,
+                    nthreads=0):
+    """Subsurface-offset extended reflectivity Born (no reference counterpart):
+    model [nh][nz][nx]; shot s on the aperture (x0, w) = apertures[s] with
+    the row's leading zero pad taps[s]."""
+    out = _data_out(p, kind, data)
+    m = _c64(model)
+    x0, w, t = _apertures(p, apertures, taps)
+    _call("oracle_offborn_forward", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(bs2)), m.shape[0], _ptr(x0), _ptr(w), _ptr(t), _ptr(m), _ptr(out), kind, int(add), prec,
+          nthreads)
+    return out
+
+
+def offborn_adjoint(p, wavelet, bs2, nh, data, apertures, taps, kind=WEM_DATA_TIME, add=False, prec=32,
+                    nthreads=0):
+    model = np.zeros((nh, p.nz, p.nx), np.complex64)
+    d = np.ascontiguousarray(data, np.float32 if kind == WEM_DATA_TIME else np.complex64)
+    x0, w, t = _apertures(p, apertures, taps)
+    _call("oracle_offborn_adjoint", ctypes.byref(p), _ptr(np.ascontiguousarray(wavelet, np.float32)),
+          _ptr(_c64(bs2)), nh, _ptr(x0), _ptr(w), _ptr(t), _ptr(model), _ptr(d), kind, int(add), prec, nthreads)
+    return model
+
+
 def borntomo_forward(p, wavelet, bs2, refl, dm, kind=WEM_DATA_TIME, data=None, add=False, prec=32, nthreads=0):
     """BornTomo (ext_born_tomo.cpp:9-57): dm [nz][nx], refl [nfreq][nz][nx]."""
     out = _data_out(p, kind, data)

@@ -716,6 +716,144 @@ void bornrefl_adjoint(const wem_params& p, const float* wavelet, const float* bs
   store(model, out.data(), nm * nf, add);
 }
 
+// ------------------------------- subsurface-offset extended Born (C4)
+// No reference counterpart.  Per shot, BornRefl (ext_born_refl.cpp:8-105) on
+// the cropped model of the shot's aperture, as WEM.from_subspace builds a
+// sub-propagator (propagator/src/python/WEM.py:24-30): the aperture's model
+// columns [x0, x0 + w), padded by pad (edge-extended), a row of nxg + 2 tap_s
+// points, its own RefSampler; the shot's devices inside the aperture.  The
+// imaging condition IC (ic.cpp:5-29) is extended over horizontal lags
+// l = -hm .. hm:  forward sc(x) = sum_l r_l(x - l) bg(x - 2l),
+// adjoint image_l(y) += conj(bg(y - l)) a(y + l), r and the image zero off
+// the aperture's model cells, bg and a zero off the padded row.
+template <class R>
+struct Aperture {
+  wem_params ps;             // the cropped problem: nx = w, tap = tap_s
+  int x0 = 0, w = 0, nxg = 0;
+  std::vector<C<R>> sp;      // padded aperture slowness [nz][nxg]
+  std::vector<int> rec;      // receivers inside the aperture
+  Inject<R> src, recinj;
+};
+
+template <class R>
+Aperture<R> make_aperture(const Problem<R>& P, const float* bs2, int is, int x0, int w, int tap) {
+  const wem_params& p = P.p;
+  check(x0 >= 0 && w >= 2 && x0 + w <= p.nx, "aperture outside the model");
+  Aperture<R> a;
+  a.ps = p;
+  a.ps.nx = w;
+  a.ps.tap = tap;
+  a.x0 = x0;
+  a.w = w;
+  a.nxg = w + 2 * p.pad;
+  std::vector<float> crop((size_t)2 * p.nz * w);
+  for (int z = 0; z < p.nz; ++z)
+    for (int x = 0; x < w; ++x) {
+      crop[2 * ((size_t)z * w + x)] = bs2[2 * ((size_t)z * p.nx + x0 + x)];
+      crop[2 * ((size_t)z * w + x) + 1] = bs2[2 * ((size_t)z * p.nx + x0 + x) + 1];
+    }
+  a.sp = pad_field<R>(a.ps, crop.data(), 1, true);
+  const int sx = P.src.ix[is];
+  check(sx >= x0 && sx < x0 + w, "source outside its aperture");
+  a.src = Inject<R>({sx - x0}, {P.src.iz[is]}, p.ngs, p.pad);
+  std::vector<int> ix, iz;
+  for (size_t i = 0; i < P.rec.ix.size(); ++i)
+    if (P.rec.ix[i] >= x0 && P.rec.ix[i] < x0 + w) {
+      a.rec.push_back((int)i);
+      ix.push_back(P.rec.ix[i] - x0);
+      iz.push_back(P.rec.iz[i]);
+    }
+  a.recinj = Inject<R>(ix, iz, p.ngr, p.pad);
+  return a;
+}
+
+template <class R>
+void offborn_forward(const wem_params& p, const float* wavelet, const float* bs2, int nh, const int* ax0,
+                     const int* aw, const int* atap, const float* model, void* data, int kind, bool add,
+                     int nthreads) {
+  check(nh >= 1 && nh % 2 == 1, "nh must be odd");
+  check(p.nref == 1, "one reference slowness");
+  Problem<R> P(p, wavelet);
+  const int nz = p.nz, nf = P.nfreq(), hm = (nh - 1) / 2;
+  const size_t nm = (size_t)p.nx * nz;
+  std::vector<C<R>> r = load<R>(model, nm * nh);
+  DataF<R> D = new_dataf(P);
+  for (int is = 0; is < p.ns; ++is) {
+    Aperture<R> A = make_aperture(P, bs2, is, ax0[is], aw[is], atap[is]);
+    const int nxg = A.nxg;
+    Core<R> core(A.ps, A.sp.data(), nxg, nz);
+    const size_t ng = (size_t)nxg * nz;
+    parallel_for(nf, nthreads, [&](int f, int) {
+      const int bin = P.F.bin[f];
+      const R w = Core<R>::omega(P.F.freq[f]);
+      std::vector<C<R>> bg(ng, C<R>(0)), sc(ng, C<R>(0)), vals(A.rec.size(), C<R>(0));
+      Work<R> wk(core.N, nxg);
+      C<R> wv = P.wave_f[bin];
+      A.src.spread(bg.data(), nxg, &wv);
+      down_fwd(core, w, bg.data(), bg.data(), true, wk);
+      for (int z = 0; z < nz; ++z)
+        for (int x = 0; x < nxg; ++x) {
+          C<R> acc(0);
+          for (int l = -hm; l <= hm; ++l) {
+            const int y = x - l, xb = x - 2 * l;
+            if (y < p.pad || y >= p.pad + A.w || xb < 0 || xb >= nxg) continue;
+            acc += r[(size_t)(l + hm) * nm + (size_t)z * p.nx + A.x0 + y - p.pad] * bg[(size_t)z * nxg + xb];
+          }
+          sc[(size_t)z * nxg + x] = acc;
+        }
+      up_fwd(core, w, sc.data(), sc.data(), true, wk);
+      A.recinj.gather(sc.data(), nxg, vals.data());
+      for (size_t i = 0; i < vals.size(); ++i) *D.at(is, A.rec[i], bin) += vals[i];
+    });
+  }
+  emit_data(P, D, data, kind, add, nthreads);
+}
+
+template <class R>
+void offborn_adjoint(const wem_params& p, const float* wavelet, const float* bs2, int nh, const int* ax0,
+                     const int* aw, const int* atap, float* model, const void* data, int kind, bool add,
+                     int nthreads) {
+  check(nh >= 1 && nh % 2 == 1, "nh must be odd");
+  check(p.nref == 1, "one reference slowness");
+  Problem<R> P(p, wavelet);
+  const int nz = p.nz, nf = P.nfreq(), hm = (nh - 1) / 2;
+  const size_t nm = (size_t)p.nx * nz;
+  DataF<R> D = absorb_data(P, data, kind, nthreads);
+  // per-frequency images, summed in frequency order at the end
+  std::vector<std::vector<C<R>>> img(nf, std::vector<C<R>>(nm * nh, C<R>(0)));
+  for (int is = 0; is < p.ns; ++is) {
+    Aperture<R> A = make_aperture(P, bs2, is, ax0[is], aw[is], atap[is]);
+    const int nxg = A.nxg;
+    Core<R> core(A.ps, A.sp.data(), nxg, nz);
+    const size_t ng = (size_t)nxg * nz;
+    parallel_for(nf, nthreads, [&](int f, int) {
+      const int bin = P.F.bin[f];
+      const R w = Core<R>::omega(P.F.freq[f]);
+      std::vector<C<R>> bg(ng, C<R>(0)), a(ng, C<R>(0)), vals(A.rec.size());
+      Work<R> wk(core.N, nxg);
+      C<R> wv = P.wave_f[bin];
+      A.src.spread(bg.data(), nxg, &wv);
+      down_fwd(core, w, bg.data(), bg.data(), true, wk);
+      for (size_t i = 0; i < vals.size(); ++i) vals[i] = *D.at(is, A.rec[i], bin);
+      A.recinj.spread(a.data(), nxg, vals.data());
+      up_adj(core, w, a.data(), a.data(), true, wk);
+      std::vector<C<R>>& I = img[f];
+      for (int z = 0; z < nz; ++z)
+        for (int y = p.pad; y < p.pad + A.w; ++y)
+          for (int l = -hm; l <= hm; ++l) {
+            const int yb = y - l, ya = y + l;
+            if (yb < 0 || yb >= nxg || ya < 0 || ya >= nxg) continue;
+            I[(size_t)(l + hm) * nm + (size_t)z * p.nx + A.x0 + y - p.pad] +=
+                std::conj(bg[(size_t)z * nxg + yb]) * a[(size_t)z * nxg + ya];
+          }
+    });
+  }
+  std::vector<C<R>> out(nm * nh, C<R>(0));
+  for (int f = 0; f < nf; ++f)
+    for (size_t i = 0; i < out.size(); ++i) out[i] += img[f][i];
+  store(model, out.data(), out.size(), add);
+}
+
 // BornTomo::fwd_propagate (ext_born_tomo.cpp:9-57): Born_down (LinDown,
 // Down, reflectivity, Up, record; Born_down.cpp:14-27) and Born_up on the
 // up background Up(refl_f bg) (Born_up.cpp:14-22)
@@ -956,6 +1094,22 @@ int oracle_bornrefl_adjoint(const wem_params* p, const float* wavelet, const flo
   return run_guarded([&] {
     if (prec == 64) bornrefl_adjoint<double>(*p, wavelet, bs2, model, data, kind, add, nthreads);
     else bornrefl_adjoint<float>(*p, wavelet, bs2, model, data, kind, add, nthreads);
+  });
+}
+int oracle_offborn_forward(const wem_params* p, const float* wavelet, const float* bs2, int nh, const int* ax0,
+                           const int* aw, const int* atap, const float* model, void* data, int kind, int add, int prec,
+                           int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) offborn_forward<double>(*p, wavelet, bs2, nh, ax0, aw, atap, model, data, kind, add, nthreads);
+    else offborn_forward<float>(*p, wavelet, bs2, nh, ax0, aw, atap, model, data, kind, add, nthreads);
+  });
+}
+int oracle_offborn_adjoint(const wem_params* p, const float* wavelet, const float* bs2, int nh, const int* ax0,
+                           const int* aw, const int* atap, float* model, const void* data, int kind, int add, int prec,
+                           int nthreads) {
+  return run_guarded([&] {
+    if (prec == 64) offborn_adjoint<double>(*p, wavelet, bs2, nh, ax0, aw, atap, model, data, kind, add, nthreads);
+    else offborn_adjoint<float>(*p, wavelet, bs2, nh, ax0, aw, atap, model, data, kind, add, nthreads);
   });
 }
 int oracle_borntomo_forward(const wem_params* p, const float* wavelet, const float* bs2, const float* refl,

@@ -257,6 +257,8 @@ class Engine {
       b.in(rho, nm);
       cuda_check(cudaMemcpy(cm_bg0_.get(nm), a.dev, nm, cudaMemcpyDeviceToDevice), "copy background");
       cuda_check(cudaMemcpy(cm_bg1_.get(nm), b.dev, nm, cudaMemcpyDeviceToDevice), "copy background");
+    } else if (kind_ == 3) {
+      off_background(s2);
     } else {
       build_background(s2, rho);
     }
@@ -423,6 +425,187 @@ class Engine {
     absorb(data, kind);
     adj_pass();
     image_out(ir_, model, add);
+  }
+
+  // ---- subsurface-offset extended reflectivity Born (kind 3; no reference
+  // counterpart).  BornRefl with the imaging condition extended over nh
+  // horizontal lags, every shot on its own aperture of model columns [x0, x0
+  // + w) (the cropped-model mechanism of WEM.from_subspace,
+  // propagator/src/python/WEM.py:24-30), padded by pad (edge-extended) and
+  // zero-padded to the row length N = 32 E >= w + 2 pad + 2 tap of the warp
+  // kernels, equally on both sides.  Receivers outside a shot's aperture
+  // record zero and are ignored by the adjoint.  One reference slowness.
+  void off_init(int nh, const int* ax0, const int* aw) {
+    require(kind_ == 3, "not an offset-Born engine");
+    require(nh >= 1 && nh % 2 == 1 && nh <= 41, "nh must be odd and at most 41");
+    require(p_.nref == 1, "the offset Born operator takes one reference slowness (nref = 1)");
+    require(p_.cmap == WEM_CMAP_NONE, "the offset Born operator has no conformal maps");
+    const Geometry& g = geo_;
+    const int ns = g.ns, nz = p_.nz, pad = p_.pad;
+    onh_ = nh;
+    osh_.assign(ns, OffShot{});
+    for (int s = 0; s < ns; ++s) {
+      OffShot& o = osh_[s];
+      o.x0 = ax0 ? ax0[s] : 0;
+      o.w = aw ? aw[s] : p_.nx;
+      require(o.x0 >= 0 && o.w >= 2 && o.x0 + o.w <= p_.nx, "aperture of shot " + std::to_string(s) +
+                                                                 " outside the model");
+      require(o.w % 2 == 0, "aperture widths must be even (shot " + std::to_string(s) + ")");
+      const int p0 = g.sptr.empty() ? s : g.sptr[s], p1 = g.sptr.empty() ? s + 1 : g.sptr[s + 1];
+      for (int pt = p0; pt < p1; ++pt)
+        require(g.sx[pt] >= o.x0 && g.sx[pt] < o.x0 + o.w,
+                "source of shot " + std::to_string(s) + " outside its aperture");
+      const int nxg = o.w + 2 * pad;
+      o.N = off_row_length(nxg + 2 * p_.tap);
+      require(o.N > 0, "aperture of shot " + std::to_string(s) + " too wide: w + 2 pad + 2 tap must be <= 1024");
+      o.tap = (o.N - nxg) / 2;
+    }
+    // rows: shots by row length, then shot, then frequency
+    std::vector<int> order(ns);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return osh_[a].N < osh_[b].N; });
+    std::vector<int> rowbase(ns), tpo(ns), x0(ns), w(ns), tap(ns);
+    std::vector<long long> toff(ns), roff;
+    std::vector<float> tpr;
+    long long t = 0, r = 0;
+    onxg_max_ = 0;
+    for (int s = 0; s < ns; ++s) {
+      const OffShot& o = osh_[s];
+      const int nxg = o.w + 2 * pad;
+      x0[s] = o.x0;
+      w[s] = o.w;
+      tap[s] = o.tap;
+      toff[s] = t;
+      t += (long long)nz * nxg;
+      tpo[s] = (int)tpr.size();
+      const std::vector<double> tp = taper(nxg, pad);
+      for (int i = 0; i < nxg; ++i) tpr.push_back((float)(tp[i] / o.N));
+      onxg_max_ = std::max(onxg_max_, nxg);
+    }
+    otab_elems_ = (size_t)t;
+    t = 0;
+    obuckets_.clear();
+    for (int s : order) {
+      const OffShot& o = osh_[s];
+      rowbase[s] = (int)r;
+      for (int f = 0; f < F_; ++f) {
+        roff.push_back(t);  // t: running offset of the rows' fields
+        t += (long long)nz * (o.w + 2 * pad);
+        ++r;
+      }
+      if (obuckets_.empty() || obuckets_.back().E != o.N / 32) {
+        obuckets_.emplace_back();
+        obuckets_.back().E = o.N / 32;
+      }
+      for (int f0 = 0; f0 < F_; f0 += kOffRows)
+        obuckets_.back().groups.push_back(OffGroup{s, f0, std::min(kOffRows, F_ - f0), rowbase[s] + f0});
+    }
+    ostore_elems_ = (size_t)t;
+    // receivers of each shot inside its aperture, by (depth, column, id)
+    std::vector<int> rptr((size_t)ns * (nz + 1), 0), rid, rxc;
+    for (int s = 0; s < ns; ++s) {
+      const OffShot& o = osh_[s];
+      std::vector<int> in;
+      for (int i = 0; i < g.nr; ++i)
+        if (g.rx[i] >= o.x0 && g.rx[i] < o.x0 + o.w) in.push_back(i);
+      std::stable_sort(in.begin(), in.end(), [&](int a, int b) {
+        return g.rz[a] != g.rz[b] ? g.rz[a] < g.rz[b] : g.rx[a] < g.rx[b];
+      });
+      int* rp = rptr.data() + (size_t)s * (nz + 1);
+      const int base = (int)rid.size();
+      for (int i : in) {
+        rp[g.rz[i] + 1]++;
+        rid.push_back(i);
+        rxc.push_back(g.rx[i]);
+      }
+      rp[0] = base;
+      for (int z = 0; z < nz; ++z) rp[z + 1] += rp[z];
+    }
+    OffCtx& c = octx_;
+    c = OffCtx{};
+    c.nz = nz;
+    c.nx = p_.nx;
+    c.pad = pad;
+    c.prop = p_.prop;
+    c.phase_law = p_.phase_law;
+    c.nh = nh;
+    c.nfreq = F_;
+    c.ns = ns;
+    c.nr = g.nr;
+    c.ngs = p_.ngs;
+    c.ngr = p_.ngr;
+    c.dz = p_.dz;
+    c.eps = p_.eps;
+    c.omega = ctx_.omega;
+    c.wave = ctx_.wave;
+    c.x0 = upload(ox0_, x0);
+    c.w = upload(ow_, w);
+    c.tap = upload(otap_, tap);
+    c.toff = upload(otoff_, toff);
+    c.taperN = upload(otaper_, tpr);
+    c.tpo = upload(otpo_, tpo);
+    c.sx = ctx_.sx;
+    c.sptr = ctx_.sptr;
+    c.sz = ctx_.sz;
+    c.gs = ctx_.gs;
+    c.gr = ctx_.gr;
+    c.rptr = upload(orptr_, rptr);
+    c.rid = upload(orid_, rid.empty() ? std::vector<int>{0} : rid);
+    c.rxc = upload(orxc_, rxc.empty() ? std::vector<int>{0} : rxc);
+    c.rowbase = upload(orowbase_, rowbase);
+    c.roff = upload(oroff_, roff);
+    // per row length: k grid, twiddles and the groups on the device
+    for (OffBucket& b : obuckets_) {
+      const int N = 32 * b.E;
+      std::vector<double> k = k_grid(N, p_.dx);
+      b.kx = upload(*b.kxb, std::vector<float>(k.begin(), k.end()));
+      b.tw = upload(*b.twb, to_f2(twiddles(N)));
+      b.dg = upload(*b.gb, b.groups);
+      require(off_smem_bytes(b.E, onxg_max_) <= (size_t)max_smem_per_block(),
+              "aperture rows do not fit one CTA's shared memory");
+    }
+  }
+
+  // row length and leading zero pad of every shot's aperture row
+  void off_rows(int* row_len, int* tap) const {
+    require(kind_ == 3 && !osh_.empty(), "not an offset-Born engine");
+    for (size_t s = 0; s < osh_.size(); ++s) {
+      if (row_len) row_len[s] = osh_[s].N;
+      if (tap) tap[s] = osh_[s].tap;
+    }
+  }
+
+  void off_forward(const void* model, void* data, int kind, int add) {
+    require(have_bg_, "background not set");
+    require(model && data, "NULL argument");
+    Staged m;
+    m.in(model, (size_t)onh_ * p_.nz * p_.nx * 8);
+    float2* A = ostoreA_.as<float2>(ostore_elems_);
+    float2* B = ostoreB_.as<float2>(ostore_elems_);
+    zero_bins();
+    off_sweeps(0, A);
+    timed("k_off_source", [&] { launch_off_source(octx_, (const float2*)m.dev, A, B, onxg_max_, 0); });
+    off_sweeps(1, B);
+    cuda_check(cudaGetLastError(), "offset Born launches");
+    emit(data, kind, add);
+  }
+
+  void off_adjoint(void* model, const void* data, int kind, int add) {
+    require(have_bg_, "background not set");
+    require(model && data, "NULL argument");
+    absorb(data, kind);
+    float2* A = ostoreA_.as<float2>(ostore_elems_);
+    float2* B = ostoreB_.as<float2>(ostore_elems_);
+    off_sweeps(0, A);
+    off_sweeps(2, B);
+    Staged o;
+    const size_t nm = (size_t)onh_ * p_.nz * p_.nx;
+    o.out(model, nm * 8, add != 0);
+    timed("k_off_image", [&] { launch_off_image(octx_, A, B, (float2*)o.dev, add, 0); });
+    cuda_check(cudaGetLastError(), "offset Born launches");
+    cuda_check(cudaStreamSynchronize(0), "offset Born adjoint");
+    o.finish(model);
+    check_background();
   }
 
   // BornTomo (ext_born_tomo.cpp:9-119): the model is a slowness perturbation
@@ -816,6 +999,87 @@ class Engine {
   Pinned pinned_;
   float2* bins_ = nullptr;
 
+  // offset Born (kind 3)
+  struct OffShot {
+    int x0 = 0, w = 0, N = 0, tap = 0;
+  };
+  struct OffBucket {
+    int E = 0;
+    std::vector<OffGroup> groups;
+    std::shared_ptr<Buf> kxb = std::make_shared<Buf>(), twb = std::make_shared<Buf>(), gb = std::make_shared<Buf>();
+    const float* kx = nullptr;
+    const float2* tw = nullptr;
+    const OffGroup* dg = nullptr;
+  };
+  std::vector<OffShot> osh_;
+  std::vector<OffBucket> obuckets_;
+  OffCtx octx_{};
+  int onh_ = 1, onxg_max_ = 0;
+  size_t otab_elems_ = 0, ostore_elems_ = 0;
+  Buf ox0_, ow_, otap_, otoff_, otaper_, otpo_, orptr_, orid_, orxc_, orowbase_, oroff_;
+  Buf osp_, osref_, oref_, oq_, obad_, oscr_, ostoreA_, ostoreB_;
+
+  // one sweep over every row, a launch per row length
+  void off_sweeps(int mode, float2* store) {
+    static const char* names[3] = {"k_off_down", "k_off_up", "k_off_upadj"};
+    timed(names[mode], [&] {
+      for (const OffBucket& b : obuckets_) {
+        OffCtx c = octx_;
+        c.kx = b.kx;
+        c.tw = b.tw;
+        launch_off_sweep(mode, b.E, c, b.dg, (int)b.groups.size(), onxg_max_, store, bins_, 0);
+      }
+    });
+  }
+
+  // aperture tables: edge-padded slowness of every aperture, its RefSampler
+  // (RefSampler.cpp:10-91 on the aperture, one reference) and the split-step
+  // exponents; a reference slowness <= 0 is reported when the call ends
+  void off_background(const void* s2) {
+    require(!osh_.empty(), "offset apertures not set");
+    const int nz = p_.nz, ns = geo_.ns, pad = p_.pad;
+    Staged ss;
+    ss.in(s2, (size_t)nz * p_.nx * 8);
+    float2* sp = osp_.as<float2>(otab_elems_);
+    launch_off_crop(octx_, (const float2*)ss.dev, onxg_max_, sp, 0);
+    float2* sref = osref_.as<float2>((size_t)ns * nz);
+    signed char* ref = oref_.as<signed char>(otab_elems_);
+    int* bad = obad_.as<int>(ns);
+    cuda_check(cudaMemsetAsync(bad, 0x7f, (size_t)ns * sizeof(int), 0), "memset");
+    float* scr = oscr_.as<float>(refs_scratch_floats(1, nz, 1));
+    long long t = 0;
+    for (int s = 0; s < ns; ++s) {
+      const int nxg = osh_[s].w + 2 * pad;
+      launch_sref(sp + t, sref + (size_t)s * nz, 1, nz, nxg, 1, bad + s, 0);
+      launch_refsampler(p_.refs_mode == WEM_REFS_NEAREST ? 1 : 0, sp + t, sref + (size_t)s * nz, 1, nz, nxg, 1, scr,
+                        ref + t, 0);
+      t += (long long)nz * nxg;
+    }
+    octx_.sref = sref;
+    float2* q = oq_.as<float2>(otab_elems_);
+    launch_off_q(octx_, sp, ref, p_.prop == WEM_PROP_SSF ? 1 : 0, onxg_max_, q, 0);
+    octx_.q = q;
+    cuda_check(cudaGetLastError(), "aperture table kernels");
+    ss.own.release();
+    cuda_check(cudaStreamSynchronize(0), "aperture tables");
+  }
+
+  void off_check() {
+    if (!have_bg_) return;
+    const int ns = geo_.ns;
+    std::vector<int> bad(ns);
+    cuda_check(cudaMemcpy(bad.data(), obad_.p, (size_t)ns * sizeof(int), cudaMemcpyDeviceToHost), "D2H status");
+    for (int s = 0; s < ns; ++s) {
+      if (bad[s] == kNoBad) continue;
+      float2 v{};
+      cuda_check(cudaMemcpy(&v, static_cast<const float2*>(osref_.p) + (size_t)s * p_.nz + bad[s], sizeof v,
+                            cudaMemcpyDeviceToHost),
+                 "D2H sref");
+      throw Fail(WEM_EINVAL, "Ref velocity " + std::to_string(v.x) + " at the layer " + std::to_string(bad[s]) +
+                                 " (aperture of shot " + std::to_string(s) + ")");
+    }
+  }
+
   void build_static() {
     const Geometry& g = geo_;
     std::vector<cd> tw = twiddles(g.N);
@@ -1078,6 +1342,10 @@ class Engine {
   // slowness whose real part is not > 0 fails the call as the reference's
   // RefSampler does (RefSampler.cpp:35-36)
   void check_background() {
+    if (kind_ == 3) {
+      off_check();
+      return;
+    }
     if (have_bg_ && shots_.empty()) cuda_check(cudaStreamSynchronize(0), "background");
     if (!shots_.empty() || !pinned_.p) return;
     const int i = *pinned_bad();
@@ -1397,6 +1665,7 @@ struct extborn_handle { std::unique_ptr<Engine> e; };
 struct fwi_handle { std::unique_ptr<Engine> e; };
 struct bornrefl_handle { std::unique_ptr<Engine> e; };
 struct borntomo_handle { std::unique_ptr<Engine> e; };
+struct bornoff_handle { std::unique_ptr<Engine> e; };
 struct wemop_handle { std::unique_ptr<RowOps> r; };
 
 extern "C" {
@@ -1546,6 +1815,31 @@ int bornrefl_forward(bornrefl_handle* h, const void* model, void* data, int kind
 }
 int bornrefl_adjoint(bornrefl_handle* h, void* model, const void* data, int kind, int add) {
   return guard([&] { require(h != nullptr, "NULL handle"); h->e->refl_adjoint(model, data, kind, add); });
+}
+
+int bornoff_create(const wem_params* p, const float* wavelet, const void* s2, int nh, const int* ap_x0,
+                   const int* ap_w, bornoff_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<bornoff_handle>();
+    h->e = std::make_unique<Engine>(*p, wavelet, false, false, 3);
+    h->e->off_init(nh, ap_x0, ap_w);
+    set_bg_unit_rho(*h->e, *p, s2);
+    *out = h.release();
+  });
+}
+void bornoff_destroy(bornoff_handle* h) { delete h; }
+int bornoff_set_background(bornoff_handle* h, const void* s2) {
+  return guard([&] { require(h != nullptr, "NULL handle"); set_bg_unit_rho(*h->e, h->e->params(), s2); });
+}
+int bornoff_forward(bornoff_handle* h, const void* model, void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->off_forward(model, data, kind, add); });
+}
+int bornoff_adjoint(bornoff_handle* h, void* model, const void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->off_adjoint(model, data, kind, add); });
+}
+int bornoff_rows(bornoff_handle* h, int* row_len, int* tap) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->off_rows(row_len, tap); });
 }
 
 int borntomo_create(const wem_params* p, const float* wavelet, const void* s2, borntomo_handle** out) {

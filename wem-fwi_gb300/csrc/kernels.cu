@@ -11,6 +11,7 @@
 
 #include "fft.cuh"
 #include "kernels.h"
+#include "phase.cuh"
 #include "wemgpu.h"
 
 namespace wg {
@@ -659,13 +660,8 @@ __global__ void __launch_bounds__(kThreads) k_oneway(DevCtx c, int f, int up, in
 }
 
 // ------------------------------------------------------------- tables
-// phase_shift.ispc:2-16: a = w^2 s_re - k^2, b = w^2 (s_im - eps s_re),
-// c = |a + ib|, re = sqrt((c+a)/2), im = -sqrt((c-a)/2),
-// factor = exp(im dz) exp(-i re dz).
-// FP32 with the cancellation-free form of the complex square root: the part
-// whose square root is taken of c + |a| comes first, the other is |b| / (2
-// that part), so neither c - a (a > 0) nor c + a (a < 0) is formed.  One CTA
-// row per (frequency, depth, reference) table row, threads over the N points.
+// Phase-shift factors (phase_factor, phase.cuh): one CTA row per
+// (frequency, depth, reference) table row, threads over the N points.
 __global__ void k_phase(DevCtx c, const float2* sref, float eps, float2* ph) {
   const int nrow = c.nfreq * c.nz * c.nref;
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -675,38 +671,14 @@ __global__ void k_phase(DevCtx c, const float2* sref, float eps, float2* ph) {
     const int j = r % c.nref, z = (r / c.nref) % c.nz, f = r / (c.nref * c.nz);
     const int m = c.ext ? f : 0;
     const float2 s = sref[((size_t)m * c.nz + z) * c.nref + j];
-    const float w = c.omega[f], w2 = w * w;
-    const float a = fmaf(w2, s.x, -k * k);
-    // ISPC law: b = w^2 (s_im - eps s_re), factor exp(im dz - i re dz) with
-    // re = Re sqrt(a + i b), im = -|Im sqrt(a + i b)|.  EXACT_KZ law
-    // (extPropagator/src/Phshift.cpp:59,81): kz = sqrt(a + i (w^2 s_im + 1e-5)),
-    // factor exp(-i dz conj(kz)) = exp(-dz Im kz - i dz Re kz); Im kz >= 0
-    // for b >= 0, the principal root's sign otherwise.
-    const bool exact = c.phase_law == WEM_PHASE_EXACT_KZ;
-    const float b = exact ? fmaf(w2, s.y, 1e-5f) : w2 * fmaf(-eps, s.x, s.y);
-    const float cc = sqrtf(fmaf(a, a, b * b));
-    float re, im;  // real part and non-positive imaginary part of the root
-    if (a >= 0.f) {
-      re = sqrtf(0.5f * (cc + a));
-      im = re > 0.f ? -fabsf(b) / (2.f * re) : 0.f;
-    } else {
-      const float q = sqrtf(0.5f * (cc - a));
-      im = -q;
-      re = fabsf(b) / (2.f * q);
-    }
-    if (exact && b < 0.f) im = -im;  // principal root: Im kz takes the sign of b
-    const float e = expf(im * c.dz);
-    float sn, cs;
-    sincosf(re * c.dz, &sn, &cs);
-    ph[(size_t)r * c.N + n] = make_float2(e * cs, -e * sn);
+    const float w = c.omega[f];
+    ph[(size_t)r * c.N + n] = phase_factor(w * w, s, k, eps, c.dz, c.phase_law);
   }
 }
 
-// SSF per-point factor: taper / N * exp(-i w dz q) (SplitStep.cpp:13-14).
-// One CTA row per (frequency, depth) table row, threads over the points.
-// w dz is carried as an unevaluated float pair hi + lo (lo the FMA-exact
-// error of the float product), so the phase w dz q is the float rounding of
-// the exact product with FP32 operations only (FP64 issues slowly here).
+// SSF per-point factor taper / N * exp(-i w dz q) (ssf_factor, phase.cuh),
+// zero at points without a reference.  One CTA row per (frequency, depth)
+// table row, threads over the points.
 __global__ void k_fac(DevCtx c, const float2* q, float2* fac) {
   const int nrow = c.nfreq * c.nz;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -716,16 +688,7 @@ __global__ void k_fac(DevCtx c, const float2* q, float2* fac) {
     const int z = r % c.nz, f = r / c.nz;
     const int m = c.ext ? f : 0;
     const size_t qi = ((size_t)m * c.nz + z) * c.nxg + x;
-    float2 out = zero2();
-    if (c.ref[qi] >= 0) {
-      const float2 qq = q[qi];
-      const float w = c.omega[f], hi = w * c.dz, lo = fmaf(w, c.dz, -hi);
-      const float amp = expf(fmaf(hi, qq.y, lo * qq.y)) * tp;
-      float sn, cs;
-      sincosf(fmaf(hi, qq.x, lo * qq.x), &sn, &cs);
-      out = make_float2(amp * cs, -amp * sn);
-    }
-    fac[(size_t)r * c.nxg + x] = out;
+    fac[(size_t)r * c.nxg + x] = c.ref[qi] >= 0 ? ssf_factor(q[qi], c.omega[f], c.dz, tp) : zero2();
   }
 }
 

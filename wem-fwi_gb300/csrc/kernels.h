@@ -145,6 +145,68 @@ void launch_exact_assemble(const DevCtx& c, int nx, float eps, const float2* sp,
                            const float2* IL, const float2* qsum, float2* gref, float2* g0, float2* g1, int add,
                            cudaStream_t st);
 
+// ---- subsurface-offset extended reflectivity Born (kernels_off.cuh,
+// offset.cu).  Every shot propagates on its own aperture: model columns
+// [x0, x0 + w) edge-padded by pad (nxg = w + 2 pad) and zero-padded by tap
+// before and N - nxg - tap after it to a row of N = 32 E points.  A CTA holds
+// up to kOffRows frequencies of one shot.  Per-shot tables are concatenated.
+constexpr int kOffRows = 8;
+struct OffCtx {
+  int nz, nx, pad, prop, phase_law, nh, nfreq, ns, nr, ngs, ngr;
+  float dz, eps;
+  const float2* tw;        // [N] exp(-2 pi i t / N) of this launch's row length
+  const float* kx;         // [N] k grid of this launch's row length
+  const float* omega;      // [F] 2 pi f
+  const float2* wave;      // [F] wavelet spectrum at the propagated bins
+  const int* x0;           // [ns] first model column of the aperture
+  const int* w;            // [ns] aperture width
+  const int* tap;          // [ns] zero pad before the padded aperture in the row
+  const long long* toff;   // [ns] offset of the shot's [nz][nxg] tables
+  const float* taperN;     // [sum nxg] taper / N of each shot
+  const int* tpo;          // [ns] offset of the shot's taper
+  const float2* q;         // [sum nz nxg] split-step exponent (s - s_ref)/sqrt(s_ref);
+                           // (0, kOffNoRef) where the point has no reference
+  const float2* sref;      // [ns][nz] reference slowness
+  const int* sx;           // source points (model columns), sptr as DevCtx
+  const int* sptr;
+  const int* sz;           // [ns] source depth
+  const float* gs;         // [2 ngs + 1]
+  const float* gr;         // [2 ngr + 1]
+  const int* rptr;         // [ns][nz + 1] receivers of shot s at depth z in rid/rxc
+  const int* rid;          // receiver index in the data
+  const int* rxc;          // receiver model column, ascending within a (shot, depth)
+  const int* rowbase;      // [ns] row of (s, f = 0); rows of a shot are consecutive in f
+  const long long* roff;   // [rows] offset of each row's [nz][nxg] field
+};
+// imaginary part of q at points without a reference: the split-step factor
+// exp(w dz Im q) underflows to zero
+constexpr float kOffNoRef = -1e30f;
+struct OffGroup {
+  int s, f0, n, row0;
+};
+// row lengths of the warp kernels: N = 32 E, E in {8, 12, 16, 24, 32}
+int off_row_length(int min_n);  // smallest such N >= min_n, or 0
+size_t off_smem_bytes(int E, int nxg_max);
+// mode 0: down sweep of the source field, stored; 1: up sweep of the stored
+// source rows, recorded into bins [ns][nr][F]; 2: adjoint of the up sweep of
+// the recorded bins, stored
+void launch_off_sweep(int mode, int E, const OffCtx& c, const OffGroup* g, int ng, int nxg_max, float2* store,
+                      float2* bins, cudaStream_t st);
+// scattered source sc(x) = sum_l r_l(x - l) bg(x - 2l) of every row of the
+// shots (rows laid out as the stores), model [nh][nz][nx]
+void launch_off_source(const OffCtx& c, const float2* model, const float2* bg, float2* sc, int nxg_max,
+                       cudaStream_t st);
+// img [nh][nz][nx] (+)= sum over rows of conj(bg(x - l)) a(x + l)
+void launch_off_image(const OffCtx& c, const float2* bg, const float2* a, float2* img, int add, cudaStream_t st);
+// padded apertures [sum nz nxg] of the slowness [nz][nx] (edge-extended,
+// each aperture on its own: operator/src/Pad.h:77-96)
+void launch_off_crop(const OffCtx& c, const float2* s2, int nxg_max, float2* sp, cudaStream_t st);
+// q of every point of the apertures from the padded slowness, the reference
+// slownesses [ns][nz] and the partition [sum nz nxg] (ssf: the split step's
+// (s - s_ref)/sqrt(s_ref), SplitStep.cpp:12-13; else 0)
+void launch_off_q(const OffCtx& c, const float2* sp, const signed char* ref, int ssf, int nxg_max, float2* q,
+                  cudaStream_t st);
+
 // ---- background tables on the device (tables.cu)
 void launch_pad_edge(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st);
 // reference slownesses [M][nz][nref]; bad (may be null): atomicMin of the

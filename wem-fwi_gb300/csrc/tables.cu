@@ -1,6 +1,7 @@
 // Background tables built on the GPU, in double precision: the per-task
 // set-up the reference repeats for every shot (propagator/src/wem_prop.cpp:
 // 26-41, born_prop.cpp:36-58), computed once per background for all rows.
+#include <algorithm>
 #include <cmath>
 
 #include "kernels.h"
@@ -299,6 +300,46 @@ void launch_point_tables(int M, int nz, int nxg, int nref, int ntaylor, float ep
   size_t n = (size_t)M * nz * nxg;
   k_point_tables<<<grid_of(n), 256, 0, st>>>(M, nz, nxg, nref, ntaylor + 1, (double)eps, sp, sp_refl ? sp_refl : sp,
                                              dp, sref, ref, q, rc, sc, a0, b0, a1, b1);
+  note_launch();
+}
+
+// ---- subsurface-offset Born: per-shot apertures
+namespace {
+// grid (nz, ns): aperture row of shot s at depth z, edge-extended by pad
+__global__ void k_off_crop(OffCtx c, const float2* s2, float2* sp) {
+  const int z = blockIdx.x, s = blockIdx.y;
+  const int w = c.w[s], nxg = w + 2 * c.pad, x0 = c.x0[s];
+  float2* o = sp + c.toff[s] + (size_t)z * nxg;
+  const float2* in = s2 + (size_t)z * c.nx + x0;
+  for (int x = threadIdx.x; x < nxg; x += blockDim.x) {
+    int k = x - c.pad;
+    k = k < 0 ? 0 : (k >= w ? w - 1 : k);
+    o[x] = in[k];
+  }
+}
+// q as k_point_tables (double, rounded once), (0, kOffNoRef) without a reference
+__global__ void k_off_q(OffCtx c, const float2* sp, const signed char* ref, int ssf, float2* q) {
+  const int z = blockIdx.x, s = blockIdx.y;
+  const int nxg = c.w[s] + 2 * c.pad;
+  const size_t o = c.toff[s] + (size_t)z * nxg;
+  const cdd sr = mk(c.sref[(size_t)s * c.nz + z]);
+  const cdd rs = csqrt(sr);
+  for (int x = threadIdx.x; x < nxg; x += blockDim.x) {
+    float2 v = make_float2(0.f, kOffNoRef);
+    if (ref[o + x] >= 0) v = ssf ? f2(dvd(sub(mk(sp[o + x]), sr), rs)) : make_float2(0.f, 0.f);
+    q[o + x] = v;
+  }
+}
+}  // namespace
+
+void launch_off_crop(const OffCtx& c, const float2* s2, int nxg_max, float2* sp, cudaStream_t st) {
+  k_off_crop<<<dim3(c.nz, c.ns), std::min(1024, (nxg_max + 31) / 32 * 32), 0, st>>>(c, s2, sp);
+  note_launch();
+}
+
+void launch_off_q(const OffCtx& c, const float2* sp, const signed char* ref, int ssf, int nxg_max, float2* q,
+                  cudaStream_t st) {
+  k_off_q<<<dim3(c.nz, c.ns), std::min(1024, (nxg_max + 31) / 32 * 32), 0, st>>>(c, sp, ref, ssf, q);
   note_launch();
 }
 

@@ -15,11 +15,12 @@ from .vector import Axis, Hypercube, SuperVector, Vector, getSepVector, superVec
 
 def __getattr__(name):
     # operator classes load the CUDA library on first use
-    if name in ("WEM", "Born", "extWEM", "extBorn", "BornRefl", "BornTomo", "Propagator",
+    if name in ("WEM", "Born", "extWEM", "extBorn", "BornRefl", "BornTomo", "BornOffset", "Propagator",
                 "LanczosInterpolation2D", "Spline", "Spline2D"):
         from . import ops
         return getattr(ops, name)
-    if name in ("WemOp", "BornOp", "ExtWemOp", "ExtBornOp", "BornReflOp", "BornTomoOp", "RowOps", "FwiOp",
+    if name in ("WemOp", "BornOp", "ExtWemOp", "ExtBornOp", "BornReflOp", "BornTomoOp", "BornOffsetOp", "RowOps",
+                "FwiOp",
                 "Interp2DOp"):
         from . import core
         return getattr(core, name)

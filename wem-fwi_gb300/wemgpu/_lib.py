@@ -55,6 +55,12 @@ _SIGS = {
     "bornrefl_set_background": (_i, [_h, _v]),
     "bornrefl_forward": (_i, [_h, _v, _v, _i, _i]),
     "bornrefl_adjoint": (_i, [_h, _v, _v, _i, _i]),
+    "bornoff_create": (_i, [_pp, _v, _v, _i, _v, _v, ctypes.POINTER(_h)]),
+    "bornoff_destroy": (None, [_h]),
+    "bornoff_set_background": (_i, [_h, _v]),
+    "bornoff_forward": (_i, [_h, _v, _v, _i, _i]),
+    "bornoff_adjoint": (_i, [_h, _v, _v, _i, _i]),
+    "bornoff_rows": (_i, [_h, _v, _v]),
     "borntomo_create": (_i, [_pp, _v, _v, ctypes.POINTER(_h)]),
     "borntomo_destroy": (None, [_h]),
     "borntomo_set_background": (_i, [_h, _v]),

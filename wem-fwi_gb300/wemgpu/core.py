@@ -212,6 +212,58 @@ class BornReflOp(_Base):
         return model
 
 
+class BornOffsetOp(_Base):
+    """Subsurface-offset extended reflectivity Born with per-shot apertures
+    (no reference counterpart; at one lag it is BornRefl,
+    propagator/src/ext_born_refl.cpp:8-105, with one reflectivity for every
+    frequency).  Model ``[nh][nz][nx]``: the reflectivity at horizontal lag
+    ``i - (nh - 1) // 2`` cells.  ``apertures``: per shot ``(x0, w)`` model
+    columns (even ``w``), or None for the whole model; each shot propagates on
+    its aperture as a cropped model (``WEM.from_subspace``,
+    propagator/src/python/WEM.py:24-30)."""
+
+    _destroy = "bornoff_destroy"
+
+    def __init__(self, p: WemParams, wavelet, bg_s2, nh: int, apertures=None):
+        super().__init__(p, wavelet)
+        self.nh = int(nh)
+        x0 = w = None
+        if apertures is not None:
+            ap = np.ascontiguousarray(np.asarray(apertures, dtype=np.int32).reshape(p.ns, 2))
+            self._x0 = np.ascontiguousarray(ap[:, 0])
+            self._w = np.ascontiguousarray(ap[:, 1])
+            x0, w = self._x0.ctypes.data_as(ctypes.c_void_p), self._w.ctypes.data_as(ctypes.c_void_p)
+        _lib.call("bornoff_create", ctypes.byref(self.p), self.wavelet.ctypes.data_as(ctypes.c_void_p),
+                  ptr(bg_s2, np.complex64, (self.p.nz, self.p.nx), "slowness"), self.nh, x0, w,
+                  ctypes.byref(self.h))
+
+    @property
+    def model_shape(self):
+        return (self.nh, self.p.nz, self.p.nx)
+
+    def rows(self):
+        """(row length, leading zero pad) of every shot's aperture row."""
+        n = np.zeros(self.p.ns, np.int32)
+        t = np.zeros(self.p.ns, np.int32)
+        _lib.call("bornoff_rows", self.h, n.ctypes.data_as(ctypes.c_void_p), t.ctypes.data_as(ctypes.c_void_p))
+        return n, t
+
+    def set_background(self, s2):
+        _lib.call("bornoff_set_background", self.h, ptr(s2, np.complex64, (self.p.nz, self.p.nx), "slowness"))
+
+    def forward(self, model, data, add=False):
+        d, kind = self._data_ptr(data, True)
+        _lib.call("bornoff_forward", self.h, ptr(model, np.complex64, self.model_shape, "model"), d, kind,
+                  int(bool(add)))
+        return data
+
+    def adjoint(self, model, data, add=False):
+        d, kind = self._data_ptr(data, False)
+        _lib.call("bornoff_adjoint", self.h, ptr(model, np.complex64, self.model_shape, "model", True), d, kind,
+                  int(bool(add)))
+        return model
+
+
 class BornTomoOp(_Base):
     """Frequency-extended tomographic Born (BornTomo,
     propagator/src/ext_born_tomo.cpp:9-119): model [nz][nx] is a slowness^2

@@ -245,6 +245,28 @@ class BornTomo(Propagator):
         self.cppMode.adjoint(model.getNdArray(), data.getNdArray(), add)
 
 
+class BornOffset(Propagator):
+    """Subsurface-offset extended reflectivity Born with per-shot apertures
+    (no reference counterpart; BornRefl's operator, ext_born_refl.cpp:8-105,
+    with the imaging condition extended over nh horizontal lags).  model: a
+    vector of shape [nh][nz][nx]; slowness: the background slowness^2;
+    apertures: per shot (x0, w) in model columns, or None (whole model)."""
+
+    def __init__(self, model, slowness, data, wave, par, nh, apertures=None):
+        self.wave, self.par, self.domain, self.range = wave, par, model, data
+        self.params = _grid_params(par, slowness.getHyper(), wave, data)
+        self.cppMode = core.BornOffsetOp(self.params, wave.getNdArray(), slowness.getNdArray(), nh, apertures)
+
+    def set_background(self, slow):
+        self.cppMode.set_background(slow.getNdArray())
+
+    def forward(self, add, model, data):
+        self.cppMode.forward(model.getNdArray(), data.getNdArray(), add)
+
+    def adjoint(self, add, model, data):
+        self.cppMode.adjoint(model.getNdArray(), data.getNdArray(), add)
+
+
 class LanczosInterpolation2D(Propagator):
     """Coarse-to-fine windowed-sinc interpolation of a 2D complex model
     (Operator.py:436-445; operator/src/LanczosInterpolation2D.h), the model

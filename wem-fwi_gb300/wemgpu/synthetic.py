@@ -14,6 +14,9 @@ shapes and value distributions, deterministically from a seed:
   3-18 Hz, SSF; true model of 6 dipping layers (1500-4500 m/s, dips within
   +-15 deg) with a smooth elliptical anomaly; start model = true smoothed
   with sigma 20 cells.
+* ``c4``: extended Born with nh = 21 subsurface-offset lags, 1024x400,
+  dx=dz=10 m, 64 shots, 80 frequencies in 3-20 Hz, uneven per-shot
+  apertures of 256-1024 cells.
 
 Slowness is the complex squared slowness 1/v^2 - i q of the reference
 (propagator/test/test_wem_ops.py:51-52); density is 1.
@@ -111,7 +114,35 @@ def c3(seed=0):
                 wavelet=ricker(nt, dt, 10.0), slow_true=s_true, slow=s0, rho=np.ones_like(s0))
 
 
-CONFIGS = {"c1": c1, "c2": c2, "c3": c3}
+def c4(seed=0, nh=21):
+    """Extended Born (subsurface offset): 1024 x 400, dx = dz = 10 m, 64
+    shots, 80 frequencies in 3-20 Hz, nh = 21 lags; smooth random background
+    (as c1); extended reflectivity of 1 % random spikes N(0, 0.1) spread over
+    the lags with a Gaussian taper (sigma 3 lags); per-shot aperture widths
+    uniform in [256, 1024] cells (even), centred on the source and moved
+    inside the model."""
+    nx, nz, dx = 1024, 400, 10.0
+    rng = np.random.default_rng(seed)
+    v = gradient_velocity(nz, nx, 1500.0, 3500.0, 0.05, 8, rng)
+    nt, dt = 1152, 0.004  # 80 bins from 3 to 20 Hz, a smooth FFT length
+    ns = 64
+    par = dict(_acquisition(nx, dx, ns), prop="ssf", nref=1, tap=0, pad=0, fmin=3.0, fmax=20.0, eps=0.04,
+               ngs=0, ngr=0, ntaylor=1)
+    s = _slow(v)
+    hm = (nh - 1) // 2
+    spikes = (rng.random((nz, nx)) < 0.01) * rng.normal(0, 0.1, (nz, nx))
+    taper = np.exp(-0.5 * ((np.arange(nh) - hm) / 3.0) ** 2)
+    refl = (taper[:, None, None] * spikes[None]).astype(np.complex64)
+    step = nx // ns
+    srcx = step // 2 + step * np.arange(ns)
+    widths = 2 * (rng.integers(256, 1025, ns) // 2)
+    x0 = np.clip(srcx - widths // 2, 0, nx - widths)
+    apertures = np.stack([x0, widths], 1).astype(np.int32)
+    return dict(name="c4", par=par, nx=nx, nz=nz, dx=dx, dz=dx, nt=nt, dt=dt, nh=nh,
+                wavelet=ricker(nt, dt, 10.0), slow=s, rho=np.ones_like(s), refl=refl, apertures=apertures)
+
+
+CONFIGS = {"c1": c1, "c2": c2, "c3": c3, "c4": c4}
 
 
 def params_of(cfg):
