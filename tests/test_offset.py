@@ -232,7 +232,7 @@ def test_offset_rejects_bad_set_ups(gpu_lib):
     from wemgpu._lib import WemError
     p, par, wav, s, ap, taps = offset_case()
     for nh, a, msg in [(4, ap, "odd"), (5, np.array([(0, 41)] + [tuple(x) for x in ap[1:]]), "even"),
-                       (5, np.array([(90, 40)] + [tuple(x) for x in ap[1:]]), "source"),
+                       (5, np.array([(60, 40)] + [tuple(x) for x in ap[1:]]), "source"),
                        (5, np.array([(100, 40)] + [tuple(x) for x in ap[1:]]), "outside the model")]:
         with pytest.raises(WemError) as e:
             _op(p, wav, s, nh, a)

@@ -244,6 +244,11 @@ class Engine {
     ctx_.last_rule = kind == 2 ? 1 : 0;
   }
 
+  ~Engine() {
+    for (cudaStream_t st : ostreams_) cudaStreamDestroy(st);
+    for (cudaEvent_t ev : oevents_) cudaEventDestroy(ev);
+  }
+
   int nfreq() const { return F_; }
   const wem_params& params() const { return p_; }
 
@@ -465,7 +470,8 @@ class Engine {
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return osh_[a].N < osh_[b].N; });
     std::vector<int> rowbase(ns), tpo(ns), x0(ns), w(ns), tap(ns);
-    std::vector<long long> toff(ns), roff;
+    std::vector<long long> toff(ns), roff, poff;
+    std::vector<int> rowshot;
     std::vector<float> tpr;
     long long t = 0, r = 0;
     onxg_max_ = 0;
@@ -484,23 +490,31 @@ class Engine {
     }
     otab_elems_ = (size_t)t;
     t = 0;
+    long long tp = 0;
     obuckets_.clear();
     for (int s : order) {
       const OffShot& o = osh_[s];
       rowbase[s] = (int)r;
-      for (int f = 0; f < F_; ++f) {
-        roff.push_back(t);  // t: running offset of the rows' fields
-        t += (long long)nz * (o.w + 2 * pad);
-        ++r;
-      }
       if (obuckets_.empty() || obuckets_.back().E != o.N / 32) {
         obuckets_.emplace_back();
         obuckets_.back().E = o.N / 32;
+        obuckets_.back().row0 = (int)r;
       }
+      for (int f = 0; f < F_; ++f) {
+        roff.push_back(t);  // t: running offset of the rows' fields
+        t += (long long)nz * (o.w + 2 * pad);
+        poff.push_back(tp);  // tp: running offset of the rows' phase tables
+        tp += (long long)nz * o.N;
+        rowshot.push_back(s);
+        ++r;
+      }
+      obuckets_.back().nrows = (int)r - obuckets_.back().row0;
+      obuckets_.back().nxg_max = std::max(obuckets_.back().nxg_max, o.w + 2 * pad);
       for (int f0 = 0; f0 < F_; f0 += kOffRows)
         obuckets_.back().groups.push_back(OffGroup{s, f0, std::min(kOffRows, F_ - f0), rowbase[s] + f0});
     }
     ostore_elems_ = (size_t)t;
+    oph_elems_ = (size_t)tp;
     // receivers of each shot inside its aperture, by (depth, column, id)
     std::vector<int> rptr((size_t)ns * (nz + 1), 0), rid, rxc;
     for (int s = 0; s < ns; ++s) {
@@ -554,6 +568,8 @@ class Engine {
     c.rxc = upload(orxc_, rxc.empty() ? std::vector<int>{0} : rxc);
     c.rowbase = upload(orowbase_, rowbase);
     c.roff = upload(oroff_, roff);
+    c.poff = upload(opoff_, poff);
+    c.rowshot = upload(orowshot_, rowshot);
     // per row length: k grid, twiddles and the groups on the device
     for (OffBucket& b : obuckets_) {
       const int N = 32 * b.E;
@@ -561,7 +577,7 @@ class Engine {
       b.kx = upload(*b.kxb, std::vector<float>(k.begin(), k.end()));
       b.tw = upload(*b.twb, to_f2(twiddles(N)));
       b.dg = upload(*b.gb, b.groups);
-      require(off_smem_bytes(b.E, onxg_max_) <= (size_t)max_smem_per_block(),
+      require(off_smem_bytes(b.E, b.nxg_max) <= (size_t)max_smem_per_block(),
               "aperture rows do not fit one CTA's shared memory");
     }
   }
@@ -1004,7 +1020,7 @@ class Engine {
     int x0 = 0, w = 0, N = 0, tap = 0;
   };
   struct OffBucket {
-    int E = 0;
+    int E = 0, row0 = 0, nrows = 0, nxg_max = 0;
     std::vector<OffGroup> groups;
     std::shared_ptr<Buf> kxb = std::make_shared<Buf>(), twb = std::make_shared<Buf>(), gb = std::make_shared<Buf>();
     const float* kx = nullptr;
@@ -1015,20 +1031,44 @@ class Engine {
   std::vector<OffBucket> obuckets_;
   OffCtx octx_{};
   int onh_ = 1, onxg_max_ = 0;
-  size_t otab_elems_ = 0, ostore_elems_ = 0;
-  Buf ox0_, ow_, otap_, otoff_, otaper_, otpo_, orptr_, orid_, orxc_, orowbase_, oroff_;
-  Buf osp_, osref_, oref_, oq_, obad_, oscr_, ostoreA_, ostoreB_;
+  size_t otab_elems_ = 0, ostore_elems_ = 0, oph_elems_ = 0;
+  Buf ox0_, ow_, otap_, otoff_, otaper_, otpo_, orptr_, orid_, orxc_, orowbase_, oroff_, opoff_, orowshot_;
+  Buf osp_, osref_, oref_, oq_, obad_, oscr_, ostoreA_, ostoreB_, otph_, otfac_;
+  // one stream per row length: the launches of a sweep run side by side
+  std::vector<cudaStream_t> ostreams_;
+  std::vector<cudaEvent_t> oevents_;
 
-  // one sweep over every row, a launch per row length
+  void off_streams() {
+    while (ostreams_.size() < obuckets_.size()) {
+      cudaStream_t st;
+      cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+      ostreams_.push_back(st);
+    }
+    while (oevents_.size() < obuckets_.size() + 1) {
+      cudaEvent_t ev;
+      cuda_check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+      oevents_.push_back(ev);
+    }
+  }
+
+  // one sweep over every row: a launch per row length, each on its own
+  // stream after the work before it on stream 0, which waits for them all
   void off_sweeps(int mode, float2* store) {
     static const char* names[3] = {"k_off_down", "k_off_up", "k_off_upadj"};
+    off_streams();
     timed(names[mode], [&] {
-      for (const OffBucket& b : obuckets_) {
+      cuda_check(cudaEventRecord(oevents_.back(), 0), "event");
+      for (size_t i = 0; i < obuckets_.size(); ++i) {
+        const OffBucket& b = obuckets_[i];
         OffCtx c = octx_;
         c.kx = b.kx;
         c.tw = b.tw;
-        launch_off_sweep(mode, b.E, c, b.dg, (int)b.groups.size(), onxg_max_, store, bins_, 0);
+        cuda_check(cudaStreamWaitEvent(ostreams_[i], oevents_.back(), 0), "stream wait");
+        launch_off_sweep(mode, b.E, c, b.dg, (int)b.groups.size(), b.nxg_max, store, bins_, ostreams_[i]);
+        cuda_check(cudaEventRecord(oevents_[i], ostreams_[i]), "event");
       }
+      for (size_t i = 0; i < obuckets_.size(); ++i)
+        cuda_check(cudaStreamWaitEvent(0, oevents_[i], 0), "stream wait");
     });
   }
 
@@ -1059,6 +1099,14 @@ class Engine {
     float2* q = oq_.as<float2>(otab_elems_);
     launch_off_q(octx_, sp, ref, p_.prop == WEM_PROP_SSF ? 1 : 0, onxg_max_, q, 0);
     octx_.q = q;
+    // every row's phase and split-step tables
+    octx_.tph = otph_.as<float2>(oph_elems_);
+    octx_.tfac = otfac_.as<float2>(ostore_elems_);
+    for (const OffBucket& b : obuckets_) {
+      OffCtx c = octx_;
+      c.kx = b.kx;
+      launch_off_tables(c, b.row0, b.nrows, 32 * b.E, 0);
+    }
     cuda_check(cudaGetLastError(), "aperture table kernels");
     ss.own.release();
     cuda_check(cudaStreamSynchronize(0), "aperture tables");

@@ -149,7 +149,9 @@ void launch_exact_assemble(const DevCtx& c, int nx, float eps, const float2* sp,
 // offset.cu).  Every shot propagates on its own aperture: model columns
 // [x0, x0 + w) edge-padded by pad (nxg = w + 2 pad) and zero-padded by tap
 // before and N - nxg - tap after it to a row of N = 32 E points.  A CTA holds
-// up to kOffRows frequencies of one shot.  Per-shot tables are concatenated.
+// up to kOffRows frequencies of one shot.  Per-shot tables are concatenated;
+// rows (shot, frequency) are ordered by row length, then shot, then
+// frequency, and each row has its own phase and split-step tables.
 constexpr int kOffRows = 8;
 struct OffCtx {
   int nz, nx, pad, prop, phase_law, nh, nfreq, ns, nr, ngs, ngr;
@@ -176,7 +178,11 @@ struct OffCtx {
   const int* rid;          // receiver index in the data
   const int* rxc;          // receiver model column, ascending within a (shot, depth)
   const int* rowbase;      // [ns] row of (s, f = 0); rows of a shot are consecutive in f
-  const long long* roff;   // [rows] offset of each row's [nz][nxg] field
+  const int* rowshot;      // [rows] shot of each row
+  const long long* roff;   // [rows] offset of each row's [nz][nxg] field and split-step table
+  const long long* poff;   // [rows] offset of each row's [nz][N] phase table
+  const float2* tph;       // phase-shift factors of every row [nz][N] (phase_factor)
+  const float2* tfac;      // split-step factors x taper / N of every row [nz][nxg] (ssf_factor)
 };
 // imaginary part of q at points without a reference: the split-step factor
 // exp(w dz Im q) underflows to zero
@@ -184,6 +190,9 @@ constexpr float kOffNoRef = -1e30f;
 struct OffGroup {
   int s, f0, n, row0;
 };
+// the phase and split-step tables of the rows [row0, row0 + nrows), all of
+// row length N = 32 E (c.kx that length's k grid)
+void launch_off_tables(const OffCtx& c, int row0, int nrows, int N, cudaStream_t st);
 // row lengths of the warp kernels: N = 32 E, E in {8, 12, 16, 24, 32}
 int off_row_length(int min_n);  // smallest such N >= min_n, or 0
 size_t off_smem_bytes(int E, int nxg_max);

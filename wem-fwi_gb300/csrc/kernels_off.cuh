@@ -9,12 +9,11 @@
 //                every depth (OneWay.cpp:82, Injection.cpp:69-80)
 //   mode 2  Up^H: W[0] = rec(0), W[z+1] = P^H_{z+1} W[z] + rec(z+1), stored
 // One warp owns one row in registers (the natural layout of wfft.cuh); the
-// rows of a CTA are frequencies of one shot, so they share the aperture, the
-// reference slowness of each depth and the split-step exponent row q, which a
-// three-slot cp.async ring brings into shared memory two depths ahead.  The
-// frequency-dependent factors are evaluated per row from those:
-// phase_factor (phase_shift.ispc) over the k grid and ssf_factor
-// (SplitStep.cpp) over the aperture, the formulas of the table builders.
+// rows of a CTA are frequencies of one shot.  Every row has its own phase
+// and split-step tables (built once per background by launch_off_tables):
+// each warp copies its next depth's rows into its own shared-memory slots
+// with cp.async as soon as the current depth has read them, so the copy runs
+// under the rest of the step and the next transform.
 #pragma once
 #include "kernels_w.cuh"
 #include "phase.cuh"
@@ -22,18 +21,16 @@
 namespace wg {
 namespace {
 
-// [tw: tw_entries][kx: N][taper: nxg_max][exchange: kOffRows x wbuf][ring: 3 x nxg_max]
+// [tw: tw_entries][exchange: kOffRows x wbuf][table slots: kOffRows x (N + nxg_max)]
 template <int E>
 struct OffCarve {
   float2* tw;
-  float* kx;
-  float* taper;
   float2* sb0;
-  float2* ring;
+  float2* slots;
   __host__ __device__ static size_t up16(size_t b) { return (b + 15) & ~size_t(15); }
   __host__ __device__ static size_t bytes(int nxg_max) {
-    return up16((size_t)tw_entries<E>() * 8) + up16((size_t)32 * E * 4) + up16((size_t)nxg_max * 4) +
-           up16((size_t)kOffRows * wbuf_len<E>() * 8) + up16((size_t)3 * nxg_max * 8);
+    return up16((size_t)tw_entries<E>() * 8) + up16((size_t)kOffRows * wbuf_len<E>() * 8) +
+           up16((size_t)kOffRows * (32 * E + nxg_max) * 8);
   }
   __device__ explicit OffCarve(int nxg_max) {
     extern __shared__ float4 smem4[];
@@ -44,10 +41,8 @@ struct OffCarve {
       return r;
     };
     tw = reinterpret_cast<float2*>(take((size_t)tw_entries<E>() * 8));
-    kx = reinterpret_cast<float*>(take((size_t)32 * E * 4));
-    taper = reinterpret_cast<float*>(take((size_t)nxg_max * 4));
     sb0 = reinterpret_cast<float2*>(take((size_t)kOffRows * wbuf_len<E>() * 8));
-    ring = reinterpret_cast<float2*>(take((size_t)3 * nxg_max * 8));
+    slots = reinterpret_cast<float2*>(take((size_t)kOffRows * (32 * E + nxg_max) * 8));
   }
 };
 
@@ -60,7 +55,7 @@ __global__ void __launch_bounds__(kOffRows * 32, 1) kw_off(OffCtx c, const OffGr
   const OffGroup gp = groups[blockIdx.x];
   const int s = gp.s, nz = c.nz;
   const int x0 = c.x0[s], nxg = c.w[s] + 2 * c.pad, tap = c.tap[s];
-  // twiddles in wfft.cuh's per-stage layout, k grid, the shot's taper
+  // twiddles in wfft.cuh's per-stage layout
   for (int i = threadIdx.x; i < tw_entries<E>(); i += blockDim.x) {
     int S = 1, L = WPlan<E>::r(0), off = 0;
     while (S < WPlan<E>::n - 1 && i >= off + (WPlan<E>::r(S) - 1) * L) {
@@ -71,21 +66,33 @@ __global__ void __launch_bounds__(kOffRows * 32, 1) kw_off(OffCtx c, const OffGr
     const int R = WPlan<E>::r(S), r = (i - off) / L + 1, l = (i - off) % L;
     sm.tw[i] = c.tw[r * l * (N / (L * R))];
   }
-  for (int i = threadIdx.x; i < N; i += blockDim.x) sm.kx[i] = c.kx[i];
-  for (int i = threadIdx.x; i < nxg; i += blockDim.x) sm.taper[i] = c.taperN[c.tpo[s] + i];
-
+  __syncthreads();
   const bool act = warp < gp.n;
-  const int f = gp.f0 + (act ? warp : 0);
-  float2* Fr = store + c.roff[gp.row0 + (act ? warp : 0)];  // this row's [nz][nxg]
+  if (!act) return;  // no barrier below this point: the warps run on their own
+  const int f = gp.f0 + warp;
+  const size_t row = (size_t)gp.row0 + warp;
+  float2* Fr = store + c.roff[row];          // this row's field [nz][nxg]
+  const float2* PH = c.tph + c.poff[row];    // [nz][N]
+  const float2* FA = c.tfac + c.roff[row];   // [nz][nxg]
   float2* sb = sm.sb0 + warp * wbuf_len<E>();
-  const float om = c.omega[f], w2 = om * om;
-  const float2* qs = c.q + c.toff[s];
-  const float2* srs = c.sref + (size_t)s * nz;
+  float2* sph = sm.slots + (size_t)warp * (N + nxg_max);
+  float2* sfa = sph + N;
   const float2 zero = make_float2(0.f, 0.f);
   const int nsteps = nz - 1;
   auto dep = [&](int i) { return MODE == 0 ? i : (MODE == 1 ? nz - 1 - i : i + 1); };
-  auto issue = [&](int i) {
-    if (i < nsteps) cta_copy(sm.ring + (size_t)(i % 3) * nxg_max, qs + (size_t)dep(i) * nxg, nxg * 8);
+  // the tables of step i into the slots; every lane commits a group per call
+  auto issue_ph = [&](int i) {
+    if (i < nsteps) warp_copy(sph, PH + (size_t)dep(i) * N, N * 8, lane);
+    cp_commit();
+  };
+  auto issue_fa = [&](int i) {
+    if (i < nsteps) warp_copy(sfa, FA + (size_t)dep(i) * nxg, nxg * 8, lane);
+    cp_commit();
+  };
+  // all but the latest group landed, for every lane of the warp
+  auto ready = [&]() {
+    cp_wait1();
+    __syncwarp();
   };
   // grid index of register j (clamped) and whether it is on the aperture
   auto xat = [&](int j, bool& in) {
@@ -167,34 +174,45 @@ __global__ void __launch_bounds__(kOffRows * 32, 1) kw_off(OffCtx c, const OffGr
     }
   };
   // W = P_d W (SSF.cpp:8-31 with one reference): FFT, phase, IFFT, split step
-  auto step_fwd = [&](int d, const float2* qrow) {
+  auto step_fwd = [&](int i) {
 #pragma unroll
     for (int j = 0; j < E; ++j) X[j] = W[j];
     wfft<E, false>(X, sb, sm.tw, lane);
-    const float2 sr = srs[d];
+    ready();
 #pragma unroll
-    for (int j = 0; j < E; ++j) X[j] = c_mul(X[j], phase_factor(w2, sr, sm.kx[lane + 32 * j], c.eps, c.dz, c.phase_law));
+    for (int j = 0; j < E; ++j) X[j] = c_mul(X[j], sph[lane + 32 * j]);
+    __syncwarp();
+    issue_ph(i + 1);
     wfft<E, true>(X, sb, sm.tw, lane);
+    ready();
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       bool in;
       const int x = xat(j, in);
-      W[j] = in ? c_mul(X[j], ssf_factor(qrow[x], om, c.dz, sm.taper[x])) : zero;
+      const float2 fx = sfa[x];
+      W[j] = in ? c_mul(X[j], fx) : zero;
     }
+    __syncwarp();
+    issue_fa(i + 1);
   };
   // W = P^H_d W (SSF.cpp:33-60): conj(split step), FFT, conj(phase), IFFT
-  auto step_adj = [&](int d, const float2* qrow) {
+  auto step_adj = [&](int i) {
+    ready();
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       bool in;
       const int x = xat(j, in);
-      X[j] = in ? c_mulc(W[j], ssf_factor(qrow[x], om, c.dz, sm.taper[x])) : zero;
+      const float2 fx = sfa[x];
+      X[j] = in ? c_mulc(W[j], fx) : zero;
     }
+    __syncwarp();
+    issue_fa(i + 1);
     wfft<E, false>(X, sb, sm.tw, lane);
-    const float2 sr = srs[d];
+    ready();
 #pragma unroll
-    for (int j = 0; j < E; ++j)
-      X[j] = c_mulc(X[j], phase_factor(w2, sr, sm.kx[lane + 32 * j], c.eps, c.dz, c.phase_law));
+    for (int j = 0; j < E; ++j) X[j] = c_mulc(X[j], sph[lane + 32 * j]);
+    __syncwarp();
+    issue_ph(i + 1);
     wfft<E, true>(X, sb, sm.tw, lane);
 #pragma unroll
     for (int j = 0; j < E; ++j) {
@@ -205,41 +223,34 @@ __global__ void __launch_bounds__(kOffRows * 32, 1) kw_off(OffCtx c, const OffGr
   };
 
   w_zero<E>(W);
-  issue(0);
-  cp_commit();
-  issue(1);
-  cp_commit();
-  __syncthreads();  // the taper and the static tables
-  if (act) {
-    if (MODE == 0) {
-      inject_src(0);
-      store_row(0);
-    } else if (MODE == 1) {
+  if (MODE == 2) {
+    issue_fa(0);
+    issue_ph(0);
+  } else {
+    issue_ph(0);
+    issue_fa(0);
+  }
+  if (MODE == 0) {
+    inject_src(0);
+    store_row(0);
+  } else if (MODE == 1) {
 #pragma unroll
-      for (int j = 0; j < E; ++j) {
-        bool in;
-        const int x = xat(j, in);
-        const float2 v = Fr[(size_t)(nz - 1) * nxg + x];
-        W[j] = in ? v : zero;
-      }
-      record(nz - 1);
-    } else {
-      inject_rec(0);
-      store_row(0);
+    for (int j = 0; j < E; ++j) {
+      bool in;
+      const int x = xat(j, in);
+      const float2 v = Fr[(size_t)(nz - 1) * nxg + x];
+      W[j] = in ? v : zero;
     }
+    record(nz - 1);
+  } else {
+    inject_rec(0);
+    store_row(0);
   }
   for (int i = 0; i < nsteps; ++i) {
-    __syncthreads();  // slot (i + 2) % 3 is no longer read
-    issue(i + 2);
-    cp_commit();
-    cp_wait1();
-    __syncthreads();
-    if (!act) continue;
     const int d = dep(i);
-    const float2* qrow = sm.ring + (size_t)(i % 3) * nxg_max;
     if (MODE == 1) {
       if (lane == 0 && d >= 2) l2_prefetch(Fr + (size_t)(d - 2) * nxg, nxg * 8);
-      step_fwd(d, qrow);
+      step_fwd(i);
 #pragma unroll
       for (int j = 0; j < E; ++j) {
         bool in;
@@ -249,11 +260,11 @@ __global__ void __launch_bounds__(kOffRows * 32, 1) kw_off(OffCtx c, const OffGr
       }
       record(d - 1);
     } else if (MODE == 0) {
-      step_fwd(d, qrow);
+      step_fwd(i);
       inject_src(d + 1);
       store_row(d + 1);
     } else {
-      step_adj(d, qrow);
+      step_adj(i);
       inject_rec(d);
       store_row(d);
     }

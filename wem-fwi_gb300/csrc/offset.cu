@@ -15,6 +15,7 @@
 
 #include "fft.cuh"
 #include "kernels.h"
+#include "phase.cuh"
 
 namespace wg {
 
@@ -26,17 +27,19 @@ size_t off_smem_w(int);
 namespace {
 
 constexpr int kSrcChunk = 256;  // aperture points per CTA of the source kernel
+constexpr int kSrcBatch = 8;    // frequencies staged per barrier in the source kernel
 constexpr int kImgChunk = 128;  // model columns per CTA of the image kernel
-constexpr int kImgBatch = 4;    // frequencies staged per barrier in the image kernel
+constexpr int kImgBatch = 16;   // frequencies staged per barrier in the image kernel
 
 // grid (nz, ns, chunks); thread t: padded aperture point x = chunk * 256 + t.
 // The lag values r_l(x - l) stay in registers for all frequencies of the
-// shot; each frequency's bg segment [x_lo - 2 hm, x_hi + 2 hm] goes through
-// shared memory.
+// shot; the bg segments [x_lo - 2 hm, x_hi + 2 hm] of kSrcBatch frequencies
+// go through shared memory per barrier, so each thread has that many loads
+// in flight.
 template <int NL>
 __global__ void __launch_bounds__(kSrcChunk) k_off_source(OffCtx c, const float2* model, const float2* bg,
                                                           float2* sc) {
-  extern __shared__ float2 seg[];
+  extern __shared__ float2 seg[];  // [kSrcBatch][len]
   const int z = blockIdx.x, s = blockIdx.y;
   const int x0 = c.x0[s], w = c.w[s], pad = c.pad, nxg = w + 2 * pad, hm = (c.nh - 1) / 2;
   const int xlo = blockIdx.z * kSrcChunk;
@@ -51,21 +54,25 @@ __global__ void __launch_bounds__(kSrcChunk) k_off_source(OffCtx c, const float2
     if (k < c.nh && on && y >= pad && y < pad + w) rv[k] = model[((size_t)k * c.nz + z) * c.nx + x0 + y - pad];
   }
   const int lo = xlo - 2 * hm, len = kSrcChunk + 4 * hm;
-  for (int f = 0; f < c.nfreq; ++f) {
-    const size_t row = (size_t)c.rowbase[s] + f;
-    const float2* b = bg + c.roff[row] + (size_t)z * nxg;
+  const size_t r0 = (size_t)c.rowbase[s];
+  for (int f0 = 0; f0 < c.nfreq; f0 += kSrcBatch) {
+    const int nb = min(kSrcBatch, c.nfreq - f0);
     __syncthreads();
-    for (int i = threadIdx.x; i < len; i += blockDim.x) {
-      const int xb = lo + i;
-      seg[i] = (xb >= 0 && xb < nxg) ? b[xb] : make_float2(0.f, 0.f);
+    for (int i = threadIdx.x; i < nb * len; i += blockDim.x) {
+      const int b = i / len, xb = lo + i % len;
+      const float2* src = bg + c.roff[r0 + f0 + b] + (size_t)z * nxg;
+      seg[i] = (xb >= 0 && xb < nxg) ? src[xb] : make_float2(0.f, 0.f);
     }
     __syncthreads();
     if (!on) continue;
-    float2 acc = make_float2(0.f, 0.f);
+    for (int b = 0; b < nb; ++b) {
+      const float2* g = seg + (size_t)b * len + (x - lo);
+      float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int k = 0; k < NL; ++k)
-      if (k < c.nh) acc = c_fma(acc, rv[k], seg[x - 2 * (k - hm) - lo]);
-    sc[c.roff[row] + (size_t)z * nxg + x] = acc;
+      for (int k = 0; k < NL; ++k)
+        if (k < c.nh) acc = c_fma(acc, rv[k], g[-2 * (k - hm)]);
+      sc[c.roff[r0 + f0 + b] + (size_t)z * nxg + x] = acc;
+    }
   }
 }
 
@@ -122,12 +129,37 @@ __global__ void __launch_bounds__(kImgChunk) k_off_image(OffCtx c, const float2*
   }
 }
 
+// grid (nz, rows): the phase-shift factors of row `row0 + blockIdx.y` at
+// depth z over the k grid of its length, and its split-step factors (taper
+// over N included) over the aperture; the formulas of the table builders
+// (phase.cuh), from the aperture's reference slowness and split-step
+// exponents
+__global__ void k_off_tables(OffCtx c, int row0, int N) {
+  const int z = blockIdx.x;
+  const int row = row0 + blockIdx.y, s = c.rowshot[row], f = row - c.rowbase[s];
+  const int nxg = c.w[s] + 2 * c.pad;
+  const float w = c.omega[f];
+  const float2 sr = c.sref[(size_t)s * c.nz + z];
+  float2* ph = const_cast<float2*>(c.tph) + c.poff[row] + (size_t)z * N;
+  for (int k = threadIdx.x; k < N; k += blockDim.x) ph[k] = phase_factor(w * w, sr, c.kx[k], c.eps, c.dz, c.phase_law);
+  const float2* q = c.q + c.toff[s] + (size_t)z * nxg;
+  const float* tp = c.taperN + c.tpo[s];
+  float2* fa = const_cast<float2*>(c.tfac) + c.roff[row] + (size_t)z * nxg;
+  for (int x = threadIdx.x; x < nxg; x += blockDim.x) fa[x] = ssf_factor(q[x], w, c.dz, tp[x]);
+}
+
 template <class K>
 void set_smem(K kern, size_t bytes) {
   if (bytes > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 }  // namespace
+
+void launch_off_tables(const OffCtx& c, int row0, int nrows, int N, cudaStream_t st) {
+  if (nrows <= 0) return;
+  k_off_tables<<<dim3(c.nz, nrows), 256, 0, st>>>(c, row0, N);
+  note_launch();
+}
 
 int off_row_length(int min_n) {
   for (int e : {8, 12, 16, 24, 32})
@@ -164,7 +196,7 @@ void launch_off_source(const OffCtx& c, const float2* model, const float2* bg, f
                        cudaStream_t st) {
   const int hm = (c.nh - 1) / 2;
   const dim3 grid(c.nz, c.ns, (nxg_max + kSrcChunk - 1) / kSrcChunk);
-  const size_t sm = (size_t)(kSrcChunk + 4 * hm) * 8;
+  const size_t sm = (size_t)kSrcBatch * (kSrcChunk + 4 * hm) * 8;
   auto go = [&](auto kern) {
     set_smem(kern, sm);
     kern<<<grid, kSrcChunk, sm, st>>>(c, model, bg, sc);
