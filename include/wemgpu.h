@@ -244,6 +244,41 @@ int bornoff_forward(bornoff_handle* h, const void* model, void* data, int data_k
 int bornoff_adjoint(bornoff_handle* h, void* model, const void* data, int data_kind, int add);
 int bornoff_rows(bornoff_handle* h, int* row_len, int* tap);
 
+/* 3D one-way operators on planes (no reference counterpart: the reference
+ * propagates 2D slices; at ny = 1 these are WEM, propagator/src/
+ * wem_prop.cpp:9-78, and BornRefl, ext_born_refl.cpp:8-105).  The depth step
+ * is the reference's SSF / PSPI step (SSF.cpp:8-60, PSPI.cpp:8-53) with a 2D
+ * FFT of each depth slice and k^2 = kx^2 + ky^2 in the phase shift
+ * (phase_shift.ispc:2-16); the taper is the product of the x and y tapers;
+ * RefSampler (RefSampler.cpp:10-91) runs on each slice flattened row by row
+ * (y-major); sources and receivers spread along x only (ngs, ngr).
+ * Models are [nz][ny][nx] complex64; data [ns][nr][nt] (time) or
+ * [ns][nr][nbin] (bins) as in 2D.  Row lengths: nx + 2 pad + 2 tap and
+ * ny + 2 pad_y + 2 tap_y each in {256, 384, 512, 768, 1024}, or ny = 1 with
+ * no y padding.  checkpoint k > 1 keeps the down field every k depths and
+ * recomputes the segments between in the up sweep (the same numbers). */
+typedef struct wem3d_params {
+  wem_params p;          /* x, z and time axes, propagation; device coordinates
+                            p.src_x/src_z (ns) and p.rec_x/rec_z (nr) required */
+  int ny;
+  float oy, dy;
+  int pad_y, tap_y;      /* edge pad + taper width, FFT zero pad along y */
+  const float* src_y;    /* ns */
+  const float* rec_y;    /* nr */
+} wem3d_params;
+typedef struct wem3d_handle wem3d_handle;
+int wem3d_create(const wem3d_params* p, const float* wavelet, wem3d_handle** out);
+void wem3d_destroy(wem3d_handle* h);
+int wem3d_get_nfreq(wem3d_handle* h, int* nfreq);
+int wem3d_forward(wem3d_handle* h, const void* slow2, const void* rho, void* data, int data_kind, int add,
+                  int checkpoint);
+typedef struct refl3d_handle refl3d_handle;
+int refl3d_create(const wem3d_params* p, const float* wavelet, const void* bg_slow2, refl3d_handle** out);
+void refl3d_destroy(refl3d_handle* h);
+int refl3d_set_background(refl3d_handle* h, const void* bg_slow2);
+int refl3d_forward(refl3d_handle* h, const void* model, void* data, int data_kind, int add, int checkpoint);
+int refl3d_adjoint(refl3d_handle* h, void* model, const void* data, int data_kind, int add);
+
 typedef struct borntomo_handle borntomo_handle;
 int borntomo_create(const wem_params* p, const float* wavelet, const void* bg_slow2, borntomo_handle** out);
 void borntomo_destroy(borntomo_handle* h);

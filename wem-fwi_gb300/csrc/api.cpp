@@ -190,6 +190,60 @@ std::vector<float> host_floats(const void* p, size_t nfloat) {
   return h;
 }
 
+// The traces' time <-> frequency transform over n samples for nf
+// propagated bins from b0: the FFT plan with its per-stage twiddle tables
+// ([r - 1][l] per stage, in double rounded once) and the natural table of the
+// restricted DFT; the launch shape for ntr traces
+TimeFreq make_timefreq(int n, int nt, int nf, int b0, int ntr, Buf& tftw, Buf& tfwn, TfShape& shape) {
+  TimeFreq t{};
+  t.n = n;
+  t.nt = nt;
+  t.nf = nf;
+  t.b0 = b0;
+  t.sc = (float)(1.0 / std::sqrt((double)n));
+  t.wn = upload(tfwn, to_f2(twiddles(n)));
+  // radices, largest first: 16, 12, 8, 6 (in-register DFTs), then 4, 3, 2, 5, 7
+  std::vector<int> rad;
+  int m = n;
+  for (int r : {16, 12, 8, 6, 4, 3, 2, 5, 7})
+    while (m % r == 0) {
+      rad.push_back(r);
+      m /= r;
+    }
+  t.fft = m == 1 && (int)rad.size() <= kMaxStages && n <= 16384;
+  if (t.fft) {
+    const long double pi = 3.14159265358979323846264338327950288L;
+    std::vector<float2> tws;
+    t.plan.n = n;
+    t.plan.nstage = (int)rad.size();
+    int L = 1;
+    for (size_t s = 0; s < rad.size(); ++s) {
+      TfStage& S = t.st[s];
+      S.R = rad[s];
+      t.plan.radix[s] = S.R;
+      S.L = L;
+      S.nb = n / S.R;
+      S.ld = n + (n >> 4) + 1;
+      S.twoff = (int)tws.size();
+      S.mag_nb = (unsigned)((((unsigned long long)1 << 32) + S.nb - 1) / S.nb);
+      S.mag_L = (unsigned)((((unsigned long long)1 << 32) + L - 1) / L);
+      for (int k = 0; k < 7; ++k)
+        S.w7[k] = make_float2((float)std::cos(-2 * pi * k / 7), (float)std::sin(-2 * pi * k / 7));
+      for (int r = 1; r < S.R; ++r)
+        for (int l = 0; l < L; ++l) {
+          const long double a = -2 * pi * (long double)(r * l) / ((long double)L * S.R);
+          tws.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
+        }
+      L *= S.R;
+    }
+    t.tw_len = (int)tws.size();
+    t.tws = upload(tftw, tws);
+  }
+  shape = timefreq_shape(t, ntr);
+  require(shape.ok, "time axis too long for the time-frequency kernels' shared memory");
+  return t;
+}
+
 class Engine {
  public:
   // kind: 0 BornFull / WEM, 1 BornRefl, 2 BornTomo (propagator/src/ext_born_refl.cpp,
@@ -1405,57 +1459,7 @@ class Engine {
   }
 
  private:
-  // the FFT plan with its per-stage twiddle tables ([r - 1][l] per stage, in
-  // double rounded once) and the natural table of the restricted DFT
-  void build_timefreq(int n) {
-    TimeFreq& t = tf_;
-    t = TimeFreq{};
-    t.n = n;
-    t.nt = p_.nt;
-    t.nf = F_;
-    t.b0 = geo_.bin[0];
-    t.sc = (float)(1.0 / std::sqrt((double)n));
-    t.wn = upload(tfwn_, to_f2(twiddles(n)));
-    // radices, largest first: 16, 12, 8, 6 (in-register DFTs), then 4, 3, 2, 5, 7
-    std::vector<int> rad;
-    int m = n;
-    for (int r : {16, 12, 8, 6, 4, 3, 2, 5, 7})
-      while (m % r == 0) {
-        rad.push_back(r);
-        m /= r;
-      }
-    t.fft = m == 1 && (int)rad.size() <= kMaxStages && n <= 16384;
-    if (t.fft) {
-      const long double pi = 3.14159265358979323846264338327950288L;
-      std::vector<float2> tws;
-      t.plan.n = n;
-      t.plan.nstage = (int)rad.size();
-      int L = 1;
-      for (size_t s = 0; s < rad.size(); ++s) {
-        TfStage& S = t.st[s];
-        S.R = rad[s];
-        t.plan.radix[s] = S.R;
-        S.L = L;
-        S.nb = n / S.R;
-        S.ld = n + (n >> 4) + 1;
-        S.twoff = (int)tws.size();
-        S.mag_nb = (unsigned)((((unsigned long long)1 << 32) + S.nb - 1) / S.nb);
-        S.mag_L = (unsigned)((((unsigned long long)1 << 32) + L - 1) / L);
-        for (int k = 0; k < 7; ++k)
-          S.w7[k] = make_float2((float)std::cos(-2 * pi * k / 7), (float)std::sin(-2 * pi * k / 7));
-        for (int r = 1; r < S.R; ++r)
-          for (int l = 0; l < L; ++l) {
-            const long double a = -2 * pi * (long double)(r * l) / ((long double)L * S.R);
-            tws.push_back(make_float2((float)std::cos(a), (float)std::sin(a)));
-          }
-        L *= S.R;
-      }
-      t.tw_len = (int)tws.size();
-      t.tws = upload(tftw_, tws);
-    }
-    tfs_ = timefreq_shape(t, geo_.ns * geo_.nr);
-    require(tfs_.ok, "time axis too long for the time-frequency kernels' shared memory");
-  }
+  void build_timefreq(int n) { tf_ = make_timefreq(n, p_.nt, F_, geo_.bin[0], geo_.ns * geo_.nr, tftw_, tfwn_, tfs_); }
 
   // bins <- bins of (the bins' time traces - obs); the loss 1/2 |residual|^2
   // lands in page-locked host memory once the stream has reached it (the
@@ -1497,6 +1501,359 @@ class Engine {
     if (kind == WEM_DATA_TIME) {
       s.in(data, (size_t)ntr * p_.nt * 4);
       time_to_bins((const float*)s.dev);
+    } else {
+      require(kind == WEM_DATA_FREQ, "unknown data kind");
+      s.in(data, (size_t)ntr * geo_.nbin * 8);
+      launch_bin_window((const float2*)s.dev, bins_, ntr, geo_.nbin, F_, geo_.bin[0], 0, 0, 0);
+    }
+    cuda_check(cudaGetLastError(), "absorb launch");
+    cuda_check(cudaStreamSynchronize(0), "absorb");
+  }
+};
+
+// ------------------------------------------------------------ 3D
+// 3D one-way modelling and reflectivity Born on planes of ny x nx points per
+// depth (no reference counterpart; at ny = 1 the 2D WEM and BornRefl).  The
+// depth recursions run as per-depth batched passes over every (shot,
+// frequency) row (kernels3d.cuh); forward-type fields keep their spectrum
+// along x (S) and the per-reference planes after the column pass (T).
+class Engine3D {
+ public:
+  Engine3D(const wem3d_params& q, const float* wavelet) : p_(q.p) {
+    require(wavelet != nullptr, "wavelet is NULL");
+    require(q.ny >= 1 && q.dy > 0, "ny must be >= 1 and dy > 0");
+    require(q.pad_y >= 0 && q.tap_y >= 0 && q.pad_y != 1, "pad_y/tap_y must be >= 0 (pad_y != 1)");
+    require(q.ny > 1 || (q.pad_y == 0 && q.tap_y == 0), "a single line (ny = 1) takes no y padding");
+    require(p_.src_x && p_.src_z && p_.rec_x && p_.rec_z && q.src_y && q.rec_y,
+            "3D devices need x, y and z coordinate arrays");
+    require(p_.cmap == WEM_CMAP_NONE, "3D operators have no conformal maps");
+    geo_ = make_geometry(p_, wavelet);
+    ny_ = q.ny;
+    pady_ = q.pad_y;
+    const int nx = p_.nx, nz = p_.nz;
+    nxg_ = nx + 2 * p_.pad;
+    nyg_ = ny_ + 2 * pady_;
+    Nx_ = nxg_ + 2 * p_.tap;
+    Ny_ = nyg_ + 2 * q.tap_y;
+    require(k3_supported(Nx_, Ny_), "3D planes need Nx = nx + 2 pad + 2 tap and Ny = ny + 2 pad_y + 2 tap_y "
+                                    "in {256, 384, 512, 768, 1024} (or Ny = 1 for ny = 1)");
+    require(p_.nref <= nxg_ * nyg_, "nref larger than the padded slice");
+    F_ = geo_.nfreq();
+    const int ns = geo_.ns, nr = geo_.nr;
+    rows_ = F_ * ns;
+    auto yidx = [&](float y) {
+      const int j = (int)((y - q.oy) / q.dy + .5f);
+      require(j >= 0 && j < ny_, "Device is out of bounds!");
+      return j;
+    };
+    std::vector<int> sy(ns), ry(nr);
+    for (int s = 0; s < ns; ++s) sy[s] = yidx(q.src_y[s]);
+    for (int i = 0; i < nr; ++i) ry[i] = yidx(q.rec_y[i]);
+    // receivers by (depth, padded line, column)
+    std::vector<int> ord(nr);
+    std::iota(ord.begin(), ord.end(), 0);
+    auto key = [&](int i) { return ((long long)geo_.rz[i] * nyg_ + ry[i] + pady_) * (nxg_ + 1) + geo_.rx[i]; };
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return key(a) < key(b); });
+    std::vector<int> rptr((size_t)nz * nyg_ + 1, 0), rxs(nr);
+    for (int i = 0; i < nr; ++i) rptr[(size_t)geo_.rz[ord[i]] * nyg_ + ry[ord[i]] + pady_ + 1]++;
+    for (size_t k = 0; k + 1 < rptr.size(); ++k) rptr[k + 1] += rptr[k];
+    for (int i = 0; i < nr; ++i) rxs[i] = geo_.rx[ord[i]];
+    for (int s = 0; s < ns; ++s) require(geo_.rx.size() > 0 && geo_.sx[s] < nx, "source outside the model");
+    // static tables
+    std::vector<double> kx = k_grid(Nx_, p_.dx), ky = k_grid(Ny_, q.dy);
+    c_.Qx = Nx_ / 2;
+    c_.Qy = std::max(Ny_ / 2, 1);
+    std::vector<float> kxq(kx.begin(), kx.begin() + c_.Qx), kyq(ky.begin(), ky.begin() + c_.Qy);
+    std::vector<double> tx = taper(nxg_, p_.pad), ty = taper(nyg_, pady_);
+    std::vector<float> tp((size_t)nyg_ * nxg_);
+    for (int y = 0; y < nyg_; ++y)
+      for (int x = 0; x < nxg_; ++x) tp[(size_t)y * nxg_ + x] = (float)(tx[x] * ty[y] / ((double)Nx_ * Ny_));
+    std::vector<float> om(F_);
+    for (int f = 0; f < F_; ++f) om[f] = (float)(2 * 3.14159265358979323846 * (double)geo_.freq[f]);
+    Ctx3& c = c_;
+    c.Nx = Nx_;
+    c.Ny = Ny_;
+    c.nxg = nxg_;
+    c.nyg = nyg_;
+    c.tapx = p_.tap;
+    c.tapy = q.tap_y;
+    c.pad = p_.pad;
+    c.pady = pady_;
+    c.nx = nx;
+    c.ny = ny_;
+    c.nz = nz;
+    c.nref = p_.nref;
+    c.prop = p_.prop;
+    c.ns = ns;
+    c.nr = nr;
+    c.nfreq = F_;
+    c.ngs = p_.ngs;
+    c.ngr = p_.ngr;
+    c.rows = rows_;
+    c.dz = p_.dz;
+    c.twx = upload(twx_, to_f2(twiddles(Nx_)));
+    c.twy = upload(twy_, to_f2(twiddles(Ny_)));
+    c.taper = upload(taper_, tp);
+    c.omega = upload(om_, om);
+    c.wave = upload(wave_, to_f2(geo_.wave_at));
+    c.sx = upload(sx_, geo_.sx);
+    c.sy = upload(sy_, sy);
+    c.sz = upload(sz_, geo_.sz);
+    std::vector<float> gsf(geo_.gs.begin(), geo_.gs.end()), grf(geo_.gr.begin(), geo_.gr.end());
+    c.gs = upload(gs_, gsf);
+    c.gr = upload(gr_, grf);
+    c.rptr = upload(rptr_, rptr);
+    c.rid = upload(rid_, ord);
+    c.rxs = upload(rxs_, rxs);
+    kxq_ = upload(kxb_, kxq);
+    kyq_ = upload(kyb_, kyq);
+    tf_ = make_timefreq(geo_.nt_pad, p_.nt, F_, geo_.bin[0], ns * nr, tftw_, tfwn_, tfs_);
+    bins_ = binsbuf_.as<float2>((size_t)ns * nr * F_);
+  }
+
+  int nfreq() const { return F_; }
+
+  // background [nz][ny][nx] slowness^2 and density: padded slices, the
+  // RefSampler of each flattened slice, split-step exponents, Reflect and the
+  // quadrant phase tables
+  void set_background(const void* s2, const void* rho) {
+    require(s2 && rho, "background model is NULL");
+    const int nz = p_.nz, nref = p_.nref;
+    const size_t n = (size_t)nz * ny_ * p_.nx, plane = (size_t)nyg_ * nxg_;
+    Staged ss, sr;
+    ss.in(s2, n * 8);
+    sr.in(rho, n * 8);
+    float2* sp = sp_.as<float2>((size_t)nz * plane);
+    float2* dp = dp_.as<float2>((size_t)nz * plane);
+    launch_pad3((const float2*)ss.dev, sp, nz, ny_, p_.nx, pady_, p_.pad, 0);
+    launch_pad3((const float2*)sr.dev, dp, nz, ny_, p_.nx, pady_, p_.pad, 0);
+    const int K = std::max(nref, 2);
+    require((long long)plane - (long long)nz * nref >= K || plane * 4 <= (size_t)max_smem_per_block(),
+            "slice too large for the RefSampler history of this depth count");
+    float2* sref = sref_.as<float2>((size_t)nz * nref);
+    signed char* ref = ref_.as<signed char>((size_t)nz * plane);
+    int* bad = bad_.as<int>(1);
+    cuda_check(cudaMemsetAsync(bad, 0x7f, sizeof(int), 0), "memset");
+    launch_sref(sp, sref, 1, nz, (int)plane, nref, bad, 0);
+    launch_refsampler(p_.refs_mode == WEM_REFS_NEAREST ? 1 : 0, sp, sref, 1, nz, (int)plane, nref,
+                      scr_.as<float>(refs_scratch_floats(1, nz, nref)), ref, 0);
+    const bool ssf = p_.prop == WEM_PROP_SSF;
+    float2* q = ssf ? q_.as<float2>((size_t)nz * plane) : nullptr;
+    float2* rc = rc_.as<float2>((size_t)nz * plane);
+    launch_point_tables(1, nz, (int)plane, nref, 0, p_.eps, sp, nullptr, dp, sref, ref, q, rc, nullptr, nullptr, nullptr,
+                        nullptr, nullptr, 0);
+    c_.ref = ref;
+    c_.q = q;
+    c_.rc = rc;
+    float2* ph = ph_.as<float2>((size_t)F_ * nz * nref * c_.Qy * c_.Qx);
+    launch_k3_phase(c_, sref, kxq_, kyq_, p_.eps, p_.phase_law, ph, 0);
+    c_.ph = ph;
+    cuda_check(cudaGetLastError(), "3D table kernels");
+    int hbad = 0;
+    cuda_check(cudaMemcpy(&hbad, bad, sizeof hbad, cudaMemcpyDeviceToHost), "D2H status");
+    if (hbad != kNoBad) {
+      float2 v{};
+      cuda_check(cudaMemcpy(&v, sref + hbad, sizeof v, cudaMemcpyDeviceToHost), "D2H sref");
+      throw Fail(WEM_EINVAL, "Ref velocity " + std::to_string(v.x) + " at the layer " + std::to_string(hbad / nref));
+    }
+    have_bg_ = true;
+  }
+
+  // background slowness^2 with unit density (the reflectivity Born takes no
+  // density, as BornRefl)
+  void set_background_unit(const void* s2) {
+    std::vector<float> ones((size_t)2 * p_.nz * ny_ * p_.nx, 0.f);
+    for (size_t i = 0; i < ones.size(); i += 2) ones[i] = 1.f;
+    set_background(s2, ones.data());
+  }
+
+  // nonlinear modelling (wem_prop.cpp:52-74 on planes): down sweep recording
+  // the direct field and keeping R D; up sweep of the reflections recorded.
+  // checkpoint k > 1: D kept every k depths, R D recomputed per segment
+  void wem_forward(const void* s2, const void* rho, void* data, int kind, int add, int ck) {
+    set_background(s2, rho);
+    zero_bins();
+    forward_two_sweeps(ck, true, nullptr);
+    emit(data, kind, add);
+  }
+
+  // reflectivity Born (ext_born_refl.cpp:8-57 with one reflectivity for all
+  // frequencies): bg = Down(src); record Up(r bg)
+  void refl_forward(const void* model, void* data, int kind, int add, int ck) {
+    require(have_bg_, "background not set");
+    require(model && data, "NULL argument");
+    Staged m;
+    m.in(model, (size_t)p_.nz * ny_ * p_.nx * 8);
+    zero_bins();
+    forward_two_sweeps(ck, false, (const float2*)m.dev);
+    emit(data, kind, add);
+  }
+
+  // its adjoint (ext_born_refl.cpp:60-105): image = sum conj(bg) Up^H(rec^H d),
+  // both fields marching down together
+  void refl_adjoint(void* model, const void* data, int kind, int add) {
+    require(have_bg_, "background not set");
+    require(model && data, "NULL argument");
+    absorb(data, kind);
+    const int nz = p_.nz;
+    const size_t fp = (size_t)rows_ * nyg_ * nxg_;
+    Planes A = planes(0), B = planes(1);
+    float2* wb = wsp_[0].as<float2>(fp);
+    float2* wa = wsp_[1].as<float2>(fp);
+    Staged o;
+    o.out(model, (size_t)nz * ny_ * p_.nx * 8, add != 0);
+    for (int z = 0; z < nz; ++z) {
+      Pass3 a{};
+      a.z = z;
+      a.zt = z - 1;
+      a.init = z == 0 ? 1 : 0;
+      a.src = 1;
+      a.spatial = wb;
+      a.tin = A.T;
+      a.tout = A.S;
+      a.last = z == nz - 1;
+      launch_k3_rows(c_, a, 0, 0);
+      Pass3 b{};
+      b.z = z;
+      b.zt = z + 1 < nz ? z + 1 : -1;
+      b.init = z == 0 ? 1 : 0;
+      b.rec_in = 1;
+      b.spatial = wa;
+      b.tin = B.S;
+      b.tout = B.T;
+      b.bins = bins_;
+      b.last = z == nz - 1;
+      launch_k3_rows(c_, b, 1, 0);
+      launch_k3_image(c_, z, wb, wa, (float2*)o.dev, add, 0);
+      if (z + 1 < nz) {
+        launch_k3_cols(c_, z, 0, A.S, A.T, 0);
+        launch_k3_cols(c_, z + 1, 1, B.T, B.S, 0);
+      }
+    }
+    cuda_check(cudaGetLastError(), "3D launches");
+    cuda_check(cudaStreamSynchronize(0), "3D adjoint");
+    o.finish(model);
+  }
+
+ private:
+  struct Planes {
+    float2 *S, *T;
+  };
+  wem_params p_;
+  Geometry geo_;
+  int ny_ = 1, pady_ = 0, nxg_ = 0, nyg_ = 0, Nx_ = 0, Ny_ = 0, F_ = 0, rows_ = 0;
+  bool have_bg_ = false;
+  Ctx3 c_{};
+  const float* kxq_ = nullptr;
+  const float* kyq_ = nullptr;
+  Buf twx_, twy_, taper_, om_, wave_, sx_, sy_, sz_, gs_, gr_, rptr_, rid_, rxs_, kxb_, kyb_, tftw_, tfwn_, binsbuf_;
+  Buf sp_, dp_, sref_, ref_, bad_, scr_, q_, rc_, ph_;
+  Buf pl_[2][2], wsp_[2], store_, seg_, lossbuf_;
+  TimeFreq tf_{};
+  TfShape tfs_{};
+  float2* bins_ = nullptr;
+
+  // plane set k: S [rows][Ny][Nx] and nref T planes
+  Planes planes(int k) {
+    const size_t plane = (size_t)rows_ * Ny_ * Nx_;
+    return Planes{pl_[k][0].as<float2>(plane), pl_[k][1].as<float2>(plane * p_.nref)};
+  }
+
+  // down sweep of the source field over depths z0..z1 on plane set P (from
+  // zero, or from the stored field `load` at z0); `at` sets each depth's
+  // stores and records
+  template <class F>
+  void down(int z0, int z1, const float2* load, Planes P, F at) {
+    for (int z = z0; z <= z1; ++z) {
+      Pass3 a{};
+      a.z = z;
+      a.zt = z == z0 ? -1 : z - 1;
+      a.init = z == z0 ? (load ? 2 : 1) : 0;
+      a.load = load;
+      a.src = (z == z0 && load) ? 0 : 1;
+      a.tin = P.T;
+      a.tout = P.S;
+      a.last = z == z1;
+      a.bins = bins_;
+      at(z, a);
+      launch_k3_rows(c_, a, 0, 0);
+      if (z < z1) launch_k3_cols(c_, z, 0, P.S, P.T, 0);
+    }
+  }
+
+  // WEM (wem = true: record the down field, up sweep of R D) or the
+  // reflectivity Born (refl: up sweep of refl bg), with stored or
+  // checkpointed down fields
+  void forward_two_sweeps(int ck, bool wem, const float2* refl) {
+    const int nz = p_.nz;
+    const size_t fp = (size_t)rows_ * nyg_ * nxg_;
+    const bool cp = ck > 1;
+    const int ncp = cp ? (nz - 1) / ck + 1 : nz;
+    float2* st = store_.as<float2>((size_t)ncp * fp);
+    Planes A = planes(0);
+    down(0, nz - 1, nullptr, A, [&](int z, Pass3& a) {
+      a.record = wem ? 1 : 0;
+      if (!cp || z % ck == 0) {
+        a.store = st + (size_t)(cp ? z / ck : z) * fp;
+        a.store_rw = (wem && !cp) ? 1 : 0;
+      }
+    });
+    // up sweep: U[nz-1] = src(nz-1), U[z-1] = P_z U[z] + src(z-1), recorded,
+    // src(z) = R[z] D[z] (WEM) or refl[z] bg[z]
+    float2* seg = cp ? seg_.as<float2>((size_t)(ck + 1) * fp) : nullptr;
+    int zs = nz;  // first depth of the recomputed segment
+    Planes B = cp ? planes(1) : Planes{};
+    for (int z = nz - 1; z >= 0; --z) {
+      if (cp && z < zs) {
+        const int z0 = (z / ck) * ck;
+        down(z0, z, st + (size_t)(z0 / ck) * fp, B, [&](int d, Pass3& a) { a.store = seg + (size_t)(d - z0) * fp; });
+        zs = z0;
+      }
+      Pass3 a{};
+      a.z = z;
+      a.zt = z == nz - 1 ? -1 : z + 1;
+      a.init = z == nz - 1 ? 1 : 0;
+      a.add = cp ? seg + (size_t)(z - zs) * fp : st + (size_t)z * fp;
+      a.add_rw = (wem && cp) ? 1 : 0;
+      a.refl = wem ? nullptr : refl;
+      a.record = 1;
+      a.tin = A.T;
+      a.tout = A.S;
+      a.bins = bins_;
+      a.last = z == 0;
+      launch_k3_rows(c_, a, 0, 0);
+      if (z > 0) launch_k3_cols(c_, z, 0, A.S, A.T, 0);
+    }
+    cuda_check(cudaGetLastError(), "3D launches");
+  }
+
+  void zero_bins() {
+    cuda_check(cudaMemsetAsync(bins_, 0, (size_t)geo_.ns * geo_.nr * F_ * 8, 0), "memset");
+  }
+
+  void emit(void* data, int kind, int add) {
+    require(data != nullptr, "data is NULL");
+    const int ntr = geo_.ns * geo_.nr;
+    Staged o;
+    if (kind == WEM_DATA_TIME) {
+      o.out(data, (size_t)ntr * p_.nt * 4, add != 0);
+      launch_timefreq(0, tf_, tfs_, bins_, (float*)o.dev, nullptr, ntr, add, nullptr, 0);
+    } else {
+      require(kind == WEM_DATA_FREQ, "unknown data kind");
+      o.out(data, (size_t)ntr * geo_.nbin * 8, add != 0);
+      launch_bin_window(bins_, (float2*)o.dev, ntr, geo_.nbin, F_, geo_.bin[0], 1, add, 0);
+    }
+    cuda_check(cudaGetLastError(), "emit launch");
+    cuda_check(cudaStreamSynchronize(0), "operator");
+    o.finish(data);
+  }
+
+  void absorb(const void* data, int kind) {
+    const int ntr = geo_.ns * geo_.nr;
+    Staged s;
+    if (kind == WEM_DATA_TIME) {
+      s.in(data, (size_t)ntr * p_.nt * 4);
+      launch_timefreq(1, tf_, tfs_, bins_, const_cast<float*>((const float*)s.dev), nullptr, ntr, 0, nullptr, 0);
     } else {
       require(kind == WEM_DATA_FREQ, "unknown data kind");
       s.in(data, (size_t)ntr * geo_.nbin * 8);
@@ -1714,6 +2071,8 @@ struct fwi_handle { std::unique_ptr<Engine> e; };
 struct bornrefl_handle { std::unique_ptr<Engine> e; };
 struct borntomo_handle { std::unique_ptr<Engine> e; };
 struct bornoff_handle { std::unique_ptr<Engine> e; };
+struct wem3d_handle { std::unique_ptr<Engine3D> e; };
+struct refl3d_handle { std::unique_ptr<Engine3D> e; };
 struct wemop_handle { std::unique_ptr<RowOps> r; };
 
 extern "C" {
@@ -1888,6 +2247,47 @@ int bornoff_adjoint(bornoff_handle* h, void* model, const void* data, int kind, 
 }
 int bornoff_rows(bornoff_handle* h, int* row_len, int* tap) {
   return guard([&] { require(h != nullptr, "NULL handle"); h->e->off_rows(row_len, tap); });
+}
+
+int wem3d_create(const wem3d_params* p, const float* wavelet, wem3d_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<wem3d_handle>();
+    h->e = std::make_unique<Engine3D>(*p, wavelet);
+    *out = h.release();
+  });
+}
+void wem3d_destroy(wem3d_handle* h) { delete h; }
+int wem3d_forward(wem3d_handle* h, const void* s2, const void* rho, void* data, int kind, int add, int checkpoint) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->wem_forward(s2, rho, data, kind, add, checkpoint); });
+}
+int refl3d_create(const wem3d_params* p, const float* wavelet, const void* s2, refl3d_handle** out) {
+  return guard([&] {
+    require(p && out, "NULL argument");
+    auto h = std::make_unique<refl3d_handle>();
+    h->e = std::make_unique<Engine3D>(*p, wavelet);
+    h->e->set_background_unit(s2);
+    *out = h.release();
+  });
+}
+void refl3d_destroy(refl3d_handle* h) { delete h; }
+int refl3d_set_background(refl3d_handle* h, const void* s2) {
+  return guard([&] {
+    require(h != nullptr, "NULL handle");
+    h->e->set_background_unit(s2);
+  });
+}
+int refl3d_forward(refl3d_handle* h, const void* model, void* data, int kind, int add, int checkpoint) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->refl_forward(model, data, kind, add, checkpoint); });
+}
+int refl3d_adjoint(refl3d_handle* h, void* model, const void* data, int kind, int add) {
+  return guard([&] { require(h != nullptr, "NULL handle"); h->e->refl_adjoint(model, data, kind, add); });
+}
+int wem3d_get_nfreq(wem3d_handle* h, int* n) {
+  return guard([&] {
+    require(h && n, "NULL argument");
+    *n = h->e->nfreq();
+  });
 }
 
 int borntomo_create(const wem_params* p, const float* wavelet, const void* s2, borntomo_handle** out) {

@@ -216,6 +216,71 @@ void launch_off_crop(const OffCtx& c, const float2* s2, int nxg_max, float2* sp,
 void launch_off_q(const OffCtx& c, const float2* sp, const signed char* ref, int ssf, int nxg_max, float2* q,
                   cudaStream_t st);
 
+// ---- 3D one-way operators (k3d.cu).  A (shot, frequency) row is a plane of
+// Ny x Nx FFT points (Nx = 32 Ex; Ny = 32 Ey or 1) holding the padded model
+// slice nyg x nxg at offset (tapy, tapx).  A depth step is two batched
+// passes over all rows: the column pass (transforms along y, the phase shift
+// per reference) and the row pass (transforms along x and every point
+// operation).  Rows r = f ns + s.
+struct Ctx3 {
+  int Nx, Ny, nxg, nyg, tapx, tapy, pad, pady, nx, ny, nz, nref, prop, ns, nr, nfreq, ngs, ngr, rows;
+  int Qx, Qy;              // quadrant of the phase tables: Nx / 2 x max(Ny / 2, 1)
+  float dz;
+  const float2* twx;       // [Nx] exp(-2 pi i t / Nx)
+  const float2* twy;       // [Ny]
+  const float* taper;      // [nyg][nxg] taper_x taper_y / (Nx Ny)
+  const float2* ph;        // [F][nz][nref][Qy][Qx] phase-shift factors by |kx|, |ky|
+  const float2* q;         // [nz][nyg][nxg] split-step exponent (SSF), null for PSPI
+  const signed char* ref;  // [nz][nyg][nxg] reference of each point, -1 none
+  const float2* rc;        // [nz][nyg][nxg] Reflect coefficients
+  const float* omega;      // [F]
+  const float2* wave;      // [F]
+  const int* sx;           // [ns] source column, row, depth (model grid)
+  const int* sy;
+  const int* sz;
+  const float* gs;         // [2 ngs + 1] spreading along x
+  const float* gr;         // [2 ngr + 1]
+  const int* rptr;         // [nz * nyg + 1] receivers by (depth, padded line) in rid / rxs
+  const int* rid;
+  const int* rxs;          // receiver model column, ascending within a line
+};
+// per-launch arguments of the row pass; planes of stored fields are
+// [rows][nyg][nxg]
+struct Pass3 {
+  int z;                   // depth of the field this pass produces (forward) or reads (adjoint)
+  int zt;                  // depth of the split-step tables applied in this pass (-1 none)
+  int init;                // 0: from the transform input, 1: zero, 2: load `load`
+  int src;                 // inject the source at depth z
+  int rec_in;              // add the receivers' data of depth z (adjoint of the record)
+  int record;              // record the field at the receivers of depth z
+  int last;                // no transform output
+  const float2* load;      // init 2: the field
+  float2* store;           // the field (or R[z] x field with store_rw) out
+  int store_rw;
+  const float2* add;       // field += add (add_rw: R[z] x add; add_refl: refl[z] x add)
+  int add_rw;
+  const float2* refl;      // [nz][ny][nx] reflectivity of add_refl (model grid)
+  float2* spatial;         // the field out (imaging)
+  const float2* tin;       // transform input planes: forward nref x [rows][Ny][Nx], adjoint [rows][Ny][Nx]
+  float2* tout;            // transform output planes: forward [rows][Ny][Nx], adjoint nref x [rows][Ny][Nx]
+  float2* bins;            // [ns][nr][F]
+};
+bool k3_supported(int Nx, int Ny);
+// row pass (adj: the adjoint step's order: inverse transform, point
+// operations, per-reference split step and forward transform)
+void launch_k3_rows(const Ctx3& c, const Pass3& a, int adj, cudaStream_t st);
+// column pass of the step at depth z: forward S -> T_j (nref planes),
+// adjoint T_j -> S
+void launch_k3_cols(const Ctx3& c, int z, int adj, const float2* in, float2* out, cudaStream_t st);
+// image[z][y][x] (+)= sum over rows (in order) conj(bg) a at depth z
+void launch_k3_image(const Ctx3& c, int z, const float2* bg, const float2* a, float2* img, int add, cudaStream_t st);
+// quadrant phase tables from the reference slownesses [nz][nref] and the
+// k grids
+void launch_k3_phase(const Ctx3& c, const float2* sref, const float* kx, const float* ky, float eps, int law,
+                     float2* ph, cudaStream_t st);
+// edge-extended padding of [M][nz][ny][nx] to [M][nz][nyg][nxg]
+void launch_pad3(const float2* in, float2* out, int nz, int ny, int nx, int pady, int pad, cudaStream_t st);
+
 // ---- background tables on the device (tables.cu)
 void launch_pad_edge(const float2* in, float2* out, int M, int nz, int nx, int pad, cudaStream_t st);
 // reference slownesses [M][nz][nref]; bad (may be null): atomicMin of the

@@ -17,8 +17,9 @@ namespace wg {
 // EXACT_KZ law (extPropagator/src/Phshift.cpp:59,81): kz = sqrt(a + i (w^2
 // s_im + 1e-5)), factor exp(-i dz conj(kz)) = exp(-dz Im kz - i dz Re kz);
 // Im kz >= 0 for b >= 0, the principal root's sign otherwise.
-__device__ __forceinline__ float2 phase_factor(float w2, float2 s, float k, float eps, float dz, int law) {
-  const float a = fmaf(w2, s.x, -k * k);
+// k2: the squared wavenumber (kx^2 + ky^2 in 3D)
+__device__ __forceinline__ float2 phase_factor_k2(float w2, float2 s, float k2, float eps, float dz, int law) {
+  const float a = fmaf(w2, s.x, -k2);
   const bool exact = law == WEM_PHASE_EXACT_KZ;
   const float b = exact ? fmaf(w2, s.y, 1e-5f) : w2 * fmaf(-eps, s.x, s.y);
   const float cc = sqrtf(fmaf(a, a, b * b));
@@ -36,6 +37,9 @@ __device__ __forceinline__ float2 phase_factor(float w2, float2 s, float k, floa
   float sn, cs;
   sincosf(re * dz, &sn, &cs);
   return make_float2(e * cs, -e * sn);
+}
+__device__ __forceinline__ float2 phase_factor(float w2, float2 s, float k, float eps, float dz, int law) {
+  return phase_factor_k2(w2, s, __fmul_rn(k, k), eps, dz, law);
 }
 
 // SSF per-point factor: tp * exp(-i w dz q) (SplitStep.cpp:13-14), tp the

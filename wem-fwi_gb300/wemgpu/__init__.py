@@ -20,7 +20,7 @@ def __getattr__(name):
         from . import ops
         return getattr(ops, name)
     if name in ("WemOp", "BornOp", "ExtWemOp", "ExtBornOp", "BornReflOp", "BornTomoOp", "BornOffsetOp", "RowOps",
-                "FwiOp",
+                "FwiOp", "Wem3DOp", "Refl3DOp",
                 "Interp2DOp"):
         from . import core
         return getattr(core, name)

@@ -61,6 +61,15 @@ _SIGS = {
     "bornoff_forward": (_i, [_h, _v, _v, _i, _i]),
     "bornoff_adjoint": (_i, [_h, _v, _v, _i, _i]),
     "bornoff_rows": (_i, [_h, _v, _v]),
+    "wem3d_create": (_i, [_v, _v, ctypes.POINTER(_h)]),
+    "wem3d_destroy": (None, [_h]),
+    "wem3d_get_nfreq": (_i, [_h, ctypes.POINTER(_i)]),
+    "wem3d_forward": (_i, [_h, _v, _v, _v, _i, _i, _i]),
+    "refl3d_create": (_i, [_v, _v, _v, ctypes.POINTER(_h)]),
+    "refl3d_destroy": (None, [_h]),
+    "refl3d_set_background": (_i, [_h, _v]),
+    "refl3d_forward": (_i, [_h, _v, _v, _i, _i, _i]),
+    "refl3d_adjoint": (_i, [_h, _v, _v, _i, _i]),
     "borntomo_create": (_i, [_pp, _v, _v, ctypes.POINTER(_h)]),
     "borntomo_destroy": (None, [_h]),
     "borntomo_set_background": (_i, [_h, _v]),

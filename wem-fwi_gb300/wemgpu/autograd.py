@@ -97,6 +97,35 @@ def modelled_data(s2, rho, wem: WemOp, born: BornOp = None, exact: bool = False,
     return FWIGradient.apply(s2, rho, wem, born)
 
 
+class Reflectivity3D(torch.autograd.Function):
+    """d = L r with L the 3D reflectivity Born (``Refl3DOp``; BornRefl's
+    operator on planes); backward: the migration L^H(dL/dd).  The forward's
+    stored background field is kept every ``checkpoint`` depths (k > 1) and
+    recomputed between, with the same numbers."""
+
+    @staticmethod
+    def forward(ctx, model, op, checkpoint: int = 0):
+        if not model.is_cuda:
+            raise ValueError("Reflectivity3D works on CUDA tensors")
+        d = torch.empty(op.data_shape(0), dtype=torch.float32, device=model.device)
+        op.forward(model.detach().contiguous(), d, checkpoint=int(checkpoint))
+        ctx.op = op
+        return d
+
+    @staticmethod
+    def backward(ctx, grad_d):
+        op = ctx.op
+        img = torch.zeros(op.model_shape, dtype=torch.complex64, device=grad_d.device)
+        op.adjoint(img, grad_d.contiguous())
+        return img, None, None
+
+
+def reflectivity_data_3d(model, op, checkpoint: int = 0):
+    """Synthetic data of a 3D reflectivity that backpropagates through the
+    migration (least-squares migration gradients)."""
+    return Reflectivity3D.apply(model, op, checkpoint)
+
+
 class FwiObjective:
     """The L2 FWI objective and its gradient, one call per iteration.
 

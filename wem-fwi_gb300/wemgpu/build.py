@@ -21,9 +21,10 @@ LIB = os.path.join(OUT_DIR, "libwemgpu.so")
 OBJ_DIR = os.path.join(OUT_DIR, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["kernels.cu", "kernels_w.cu", "tables.cu", "timefreq.cu", "grad.cu", "offset.cu", "noalloc.cu", "interp.cu",
-           "rowops.cu", "api.cpp", "planner.cpp", "cmap.cpp"] + [
-    f"kw_e{e}_{p}.cu" for e in (32, 24, 16, 12, 8) for p in ("adj", "adj1", "wem", "fwd", "grad", "off")]
+SOURCES = ["kernels.cu", "kernels_w.cu", "tables.cu", "timefreq.cu", "grad.cu", "offset.cu", "k3d.cu", "noalloc.cu",
+           "interp.cu", "rowops.cu", "api.cpp", "planner.cpp", "cmap.cpp"] + [
+    f"kw_e{e}_{p}.cu" for e in (32, 24, 16, 12, 8) for p in ("adj", "adj1", "wem", "fwd", "grad", "off")] + [
+    f"k3_e{e}.cu" for e in (32, 24, 16, 12, 8)]
 
 # host code whose float results must not depend on the machine: the
 # conformal maps turn float coordinates into grid indices, so no multiply-add

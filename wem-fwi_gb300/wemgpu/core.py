@@ -264,6 +264,96 @@ class BornOffsetOp(_Base):
         return model
 
 
+class _Base3D:
+    """3D operators: models ``[nz][ny][nx]``, data as in 2D."""
+
+    _destroy = None
+
+    def __init__(self, q, wavelet):
+        self.q = q
+        self.p = q.p
+        self.wavelet = np.ascontiguousarray(np.asarray(wavelet, dtype=np.float32)).reshape(-1)
+        if self.wavelet.size != self.p.nt:
+            raise ValueError(f"wavelet has {self.wavelet.size} samples, params say nt={self.p.nt}")
+        self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h and h.value and self._destroy:
+            try:
+                getattr(_lib.load(), self._destroy)(h)
+            except Exception:
+                pass
+            self.h = ctypes.c_void_p()
+
+    @property
+    def model_shape(self):
+        return (self.p.nz, self.q.ny, self.p.nx)
+
+    @property
+    def nbin(self):
+        return self.p.nbin if self.p.nbin else self.p.nt + self.p.tpad
+
+    def data_shape(self, kind):
+        return (self.p.ns, self.p.nr, self.p.nt if kind == WEM_DATA_TIME else self.nbin)
+
+    def _data_ptr(self, data, writable):
+        kind = _data_kind(data)
+        dt = np.float32 if kind == WEM_DATA_TIME else np.complex64
+        return ptr(data, dt, self.data_shape(kind), "data", writable), kind
+
+    def nfreq(self) -> int:
+        n = ctypes.c_int()
+        _lib.call("wem_count_freqs", ctypes.byref(self.p), None, ctypes.byref(n))
+        return n.value
+
+
+class Wem3DOp(_Base3D):
+    """3D nonlinear modelling on planes (WEM's call sequence,
+    propagator/src/wem_prop.cpp:9-78, with a 2D FFT per depth slice);
+    ``checkpoint`` k > 1 keeps every k-th depth of the down field."""
+
+    _destroy = "wem3d_destroy"
+
+    def __init__(self, q, wavelet):
+        super().__init__(q, wavelet)
+        _lib.call("wem3d_create", ctypes.byref(q), self.wavelet.ctypes.data_as(ctypes.c_void_p), ctypes.byref(self.h))
+
+    def forward(self, s2, rho, data, add=False, checkpoint=0):
+        d, kind = self._data_ptr(data, True)
+        _lib.call("wem3d_forward", self.h, ptr(s2, np.complex64, self.model_shape, "slowness"),
+                  ptr(rho, np.complex64, self.model_shape, "density"), d, kind, int(bool(add)), int(checkpoint))
+        return data
+
+
+class Refl3DOp(_Base3D):
+    """3D reflectivity Born (BornRefl's operator, ext_born_refl.cpp:8-105,
+    one reflectivity for every frequency): forward records Up(r bg),
+    adjoint is the migration image sum conj(bg) Up^H(data)."""
+
+    _destroy = "refl3d_destroy"
+
+    def __init__(self, q, wavelet, bg_s2):
+        super().__init__(q, wavelet)
+        _lib.call("refl3d_create", ctypes.byref(q), self.wavelet.ctypes.data_as(ctypes.c_void_p),
+                  ptr(bg_s2, np.complex64, self.model_shape, "slowness"), ctypes.byref(self.h))
+
+    def set_background(self, s2):
+        _lib.call("refl3d_set_background", self.h, ptr(s2, np.complex64, self.model_shape, "slowness"))
+
+    def forward(self, model, data, add=False, checkpoint=0):
+        d, kind = self._data_ptr(data, True)
+        _lib.call("refl3d_forward", self.h, ptr(model, np.complex64, self.model_shape, "model"), d, kind,
+                  int(bool(add)), int(checkpoint))
+        return data
+
+    def adjoint(self, model, data, add=False):
+        d, kind = self._data_ptr(data, False)
+        _lib.call("refl3d_adjoint", self.h, ptr(model, np.complex64, self.model_shape, "model", True), d, kind,
+                  int(bool(add)))
+        return model
+
+
 class BornTomoOp(_Base):
     """Frequency-extended tomographic Born (BornTomo,
     propagator/src/ext_born_tomo.cpp:9-119): model [nz][nx] is a slowness^2

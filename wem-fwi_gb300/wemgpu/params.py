@@ -138,3 +138,45 @@ def make_params(par: Any, *, nx: int, nz: int, dx: float, dz: float,
         p._keep.append(arr)
         p.cmap_angles = arr.ctypes.data_as(_fp)
     return p
+
+
+class WemParams3D(ctypes.Structure):
+    """ctypes mirror of ``struct wem3d_params`` (3D operators)."""
+
+    _fields_ = [("p", WemParams), ("ny", ctypes.c_int), ("oy", ctypes.c_float), ("dy", ctypes.c_float),
+                ("pad_y", ctypes.c_int), ("tap_y", ctypes.c_int), ("src_y", _fp), ("rec_y", _fp)]
+
+    def __init__(self, *a, **kw):
+        super().__init__(*a, **kw)
+        self._keep: list = []
+
+    @property
+    def ns(self):
+        return self.p.ns
+
+    @property
+    def nr(self):
+        return self.p.nr
+
+
+def make_params3d(par: Any, *, nx: int, ny: int, nz: int, dx: float, dy: float, dz: float, nt: int, dt: float,
+                  sx, sy, sz, rx, ry, rz, ox: float = 0.0, oy: float = 0.0, oz: float = 0.0,
+                  pad_y: int = 0, tap_y: int = 0) -> WemParams3D:
+    """3D parameter block: the 2D keys of :func:`make_params` for the x, z and
+    time axes and the propagation, the y axis, and explicit device
+    coordinates (x, y, z per source and per receiver)."""
+    m = dict(_as_mapping(par))
+    m.update(sx=list(sx), sz=list(sz), rx=list(rx), rz=list(rz))
+    q = WemParams3D()
+    base = make_params(m, nx=nx, nz=nz, dx=dx, dz=dz, nt=nt, dt=dt, ox=ox, oz=oz)
+    q.p = base  # a field copy: the coordinate arrays stay alive in q._keep
+    q._keep.extend(base._keep)
+    q.ny, q.oy, q.dy, q.pad_y, q.tap_y = int(ny), float(oy), float(dy), int(pad_y), int(tap_y)
+    ys = np.ascontiguousarray(np.asarray(sy, dtype=np.float32))
+    yr = np.ascontiguousarray(np.asarray(ry, dtype=np.float32))
+    if ys.size != q.p.ns or yr.size != q.p.nr:
+        raise ValueError("sy / ry must give one y per source / receiver")
+    q._keep.extend([ys, yr])
+    q.src_y = ys.ctypes.data_as(_fp)
+    q.rec_y = yr.ctypes.data_as(_fp)
+    return q

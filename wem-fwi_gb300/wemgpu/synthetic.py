@@ -17,6 +17,8 @@ shapes and value distributions, deterministically from a seed:
 * ``c4``: extended Born with nh = 21 subsurface-offset lags, 1024x400,
   dx=dz=10 m, 64 shots, 80 frequencies in 3-20 Hz, uneven per-shot
   apertures of 256-1024 cells.
+* ``c5``: 3D PSPI (nref 3) with a 2D FFT per depth slice, 256x256x300,
+  dx=dy=dz=15 m, 16 shots on a 4x4 grid, 64 frequencies in 3-15 Hz.
 
 Slowness is the complex squared slowness 1/v^2 - i q of the reference
 (propagator/test/test_wem_ops.py:51-52); density is 1.
@@ -140,6 +142,35 @@ def c4(seed=0, nh=21):
     apertures = np.stack([x0, widths], 1).astype(np.int32)
     return dict(name="c4", par=par, nx=nx, nz=nz, dx=dx, dz=dx, nt=nt, dt=dt, nh=nh,
                 wavelet=ricker(nt, dt, 10.0), slow=s, rho=np.ones_like(s), refl=refl, apertures=apertures)
+
+
+def c5(seed=0, rstep=2):
+    """3D PSPI with a 2D FFT per slice: 256 x 256 x 300, dx = dy = dz = 15 m,
+    16 shots on a 4 x 4 grid, 64 frequencies in 3-15 Hz, nref = 3; velocity a
+    linear gradient 1500 -> 3500 m/s in depth plus Gaussian-smoothed (sigma
+    6 cells) +-8 % noise; receivers every ``rstep`` cells on the surface;
+    the reflectivity of the migration pair is 1 % random spikes N(0, 0.1)."""
+    from .params import make_params3d
+    nx = ny = 256
+    nz, d = 300, 15.0
+    rng = np.random.default_rng(seed)
+    v = 1500.0 + 2000.0 * np.linspace(0, 1, nz)[:, None, None] * np.ones((1, ny, nx))
+    n = _smooth(rng.uniform(-1, 1, (nz, ny, nx)), 6)
+    n /= max(np.abs(n).max(), 1e-12)
+    v = v * (1 + 0.08 * n)
+    s = _slow(v)
+    nt, dt = 648, 0.008  # 64 bins from 3 to 15 Hz, a smooth FFT length
+    g = (np.arange(4) + 0.5) * (nx / 4) * d
+    sx, sy = np.meshgrid(g, g)
+    sx, sy = sx.ravel(), sy.ravel()
+    rx, ry = np.meshgrid(np.arange(0, nx, rstep) * d, np.arange(0, ny, rstep) * d)
+    rx, ry = rx.ravel(), ry.ravel()
+    par = dict(prop="pspi", nref=3, tap=0, pad=0, fmin=3.0, fmax=15.0, eps=0.04, ngs=0, ngr=0, ntaylor=1)
+    q = make_params3d(par, nx=nx, ny=ny, nz=nz, dx=d, dy=d, dz=d, nt=nt, dt=dt, sx=sx, sy=sy,
+                      sz=np.zeros_like(sx), rx=rx, ry=ry, rz=np.zeros_like(rx))
+    refl = ((rng.random((nz, ny, nx)) < 0.01) * rng.normal(0, 0.1, (nz, ny, nx))).astype(np.complex64)
+    return dict(name="c5", q=q, nx=nx, ny=ny, nz=nz, nt=nt, dt=dt, wavelet=ricker(nt, dt, 10.0), slow=s,
+                rho=np.ones_like(s), refl=refl)
 
 
 CONFIGS = {"c1": c1, "c2": c2, "c3": c3, "c4": c4}
