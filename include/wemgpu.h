@@ -207,7 +207,13 @@ int born_adjoint(born_handle* h, void* dslow2, void* drho,
  * ext_born_tomo.cpp:9-119).  model: complex [nz][nx] slowness^2
  * perturbation; the down- and up-scattering terms of BornFull with the
  * reflectivity set by borntomo_set_refl ([nfreq][nz][nx]) in place of R.
- * Backgrounds are slowness^2 only (the reference takes no density). */
+ * Backgrounds are slowness^2 only (the reference takes no density).
+ * Both keep the reference's conventions for these classes, which differ
+ * from BornFull's (ext_born_refl.cpp:18-25, ext_born_tomo.cpp:20-25): they
+ * propagate on the model grid itself (no edge padding; p->pad is only the
+ * taper width of OneStep.h:27-35), the source spreads over p->ngs cells
+ * (the reference's parameter "ng") and the receivers are points (p->ngr is
+ * not read). */
 typedef struct bornrefl_handle bornrefl_handle;
 int bornrefl_create(const wem_params* p, const float* wavelet, const void* bg_slow2, bornrefl_handle** out);
 void bornrefl_destroy(bornrefl_handle* h);
@@ -224,10 +230,11 @@ int bornrefl_adjoint(bornrefl_handle* h, void* model, const void* data, int data
  *   forward  bg = Down(src); sc(x) = sum_l r_l(x - l) bg(x - 2l); record Up(sc)
  *   adjoint  bg = Down(src); a = Up^H(data); image_l(x) += conj(bg(x - l)) a(x + l)
  * Shot s propagates on its aperture, model columns [ap_x0[s], ap_x0[s] +
- * ap_w[s]) (even widths; NULL: the whole model for every shot), edge-padded
- * by pad and zero-padded to the row length N_s, the smallest of 256, 384,
- * 512, 768, 1024 with N_s >= ap_w[s] + 2 pad + 2 tap, equally on both sides
- * (bornoff_rows reports N_s and the leading zero pad).  The aperture is a
+ * ap_w[s]) (even widths; NULL: the whole model for every shot), with
+ * BornRefl's conventions (no edge padding, pad the taper width, source
+ * spread ngs, point receivers), zero-padded to the row length N_s, the
+ * smallest of 256, 384, 512, 768, 1024 with N_s >= ap_w[s] + 2 tap, equally
+ * on both sides (bornoff_rows reports N_s and the leading zero pad).  The aperture is a
  * cropped model as WEM.from_subspace builds it (propagator/src/python/
  * WEM.py:24-30): the reference slowness comes from the aperture, receivers
  * outside it record zero and are ignored by the adjoint.  One reference
@@ -255,8 +262,11 @@ int bornoff_rows(bornoff_handle* h, int* row_len, int* tap);
  * Models are [nz][ny][nx] complex64; data [ns][nr][nt] (time) or
  * [ns][nr][nbin] (bins) as in 2D.  Row lengths: nx + 2 pad + 2 tap and
  * ny + 2 pad_y + 2 tap_y each in {256, 384, 512, 768, 1024}, or ny = 1 with
- * no y padding.  checkpoint k > 1 keeps the down field every k depths and
- * recomputes the segments between in the up sweep (the same numbers). */
+ * no y padding.  The reflectivity Born pair (refl3d_*) keeps BornRefl's
+ * conventions: no edge padding (pad and pad_y are taper widths only, so
+ * nx + 2 tap and ny + 2 tap_y are the row lengths) and point receivers.
+ * checkpoint k > 1 keeps the down field every k depths and recomputes the
+ * segments between in the up sweep (the same numbers). */
 typedef struct wem3d_params {
   wem_params p;          /* x, z and time axes, propagation; device coordinates
                             p.src_x/src_z (ns) and p.rec_x/rec_z (nr) required */

@@ -2,11 +2,11 @@
 restatement in ``wem_oracle.cpp``; only tests/, ``__graft_entry__.smoke()``
 and bench.py's CPU-baseline leg import it, as the checker.
 
-PARITY UNPINNED: the reference cannot be built here (FFTW, TBB, Boost, SEP
-I/O and ISPC are absent) and its tests hold no numeric golden vectors; the
-restatement is pinned by the reference's structural known-answer test
-(extWEM == WEM on a frequency-constant model), dot tests, its fp64 twin and
-numpy.fft.
+PARITY PINNED: the restatement is held to the outputs of the reference's
+own sources (compiled by oracle/ref/Makefile against stand-ins for its
+external libraries; golden fixtures tests/golden/ref_*.npz, checked by
+tests/test_ref_pin.py), besides the reference's known-answer test (extWEM ==
+WEM on a frequency-constant model), dot tests, its fp64 twin and numpy.fft.
 """
 from __future__ import annotations
 

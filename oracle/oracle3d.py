@@ -98,13 +98,16 @@ def ps_factor(w, k2, dz, s, eps, law, R, C):
 class Problem3D:
     """Everything a (shot, frequency) plane needs: grids, devices, tables."""
 
-    def __init__(self, q, wavelet, s2, rho, prec=32):
+    def __init__(self, q, wavelet, s2, rho, prec=32, refl=False):
+        # refl: the 2D BornRefl conventions (ext_born_refl.cpp:18-25): no
+        # model padding, pad and pad_y the taper widths only, point receivers
         p = q.p
         R, C = _types(prec)
         self.R, self.C, self.p, self.prec = R, C, p, prec
-        self.ny, self.pady, self.tapy = q.ny, q.pad_y, q.tap_y
-        self.nx, self.nz, self.pad, self.tapx = p.nx, p.nz, p.pad, p.tap
-        self.nxg, self.nyg = p.nx + 2 * p.pad, q.ny + 2 * q.pad_y
+        self.ny, self.pady, self.tapy = q.ny, (0 if refl else q.pad_y), q.tap_y
+        self.nx, self.nz, self.pad, self.tapx = p.nx, p.nz, (0 if refl else p.pad), p.tap
+        self.ngs, self.ngr = p.ngs, (0 if refl else p.ngr)
+        self.nxg, self.nyg = p.nx + 2 * self.pad, q.ny + 2 * self.pady
         self.Nx, self.Ny = self.nxg + 2 * p.tap, self.nyg + 2 * q.tap_y
         self.freq, self.bin, self.nt_pad = freqs(p)
         # unitary FFT of the time-padded wavelet (FFT1_r.cpp:74-83)
@@ -121,7 +124,7 @@ class Problem3D:
                     for i in range(ns)]
         self.rec = [(idx(p.rec_x[i], p.ox, p.dx), idx(q.rec_y[i], q.oy, q.dy), idx(p.rec_z[i], p.oz, p.dz))
                     for i in range(nr)]
-        self.gs, self.gr = window(p.ngs, R), window(p.ngr, R)
+        self.gs, self.gr = window(self.ngs, R), window(self.ngr, R)
         # padded slices (edge-extended) and their tables
         sp = self.pad3(np.asarray(s2, np.complex64))
         dp = self.pad3(np.asarray(rho, np.complex64))
@@ -138,7 +141,7 @@ class Problem3D:
             self.rc[z] = num / den
         kx, ky = k_grid(self.Nx, p.dx, R), k_grid(self.Ny, q.dy, R)
         self.k2 = (kx[None, :] * kx[None, :] + ky[:, None] * ky[:, None]).astype(R)
-        self.taper = (taper(self.nyg, self.pady, R)[:, None] * taper(self.nxg, self.pad, R)[None, :]).astype(R)
+        self.taper = (taper(self.nyg, q.pad_y, R)[:, None] * taper(self.nxg, p.pad, R)[None, :]).astype(R)
 
     def pad3(self, m):
         m = np.asarray(m).reshape(self.nz, self.ny, self.nx)
@@ -194,24 +197,24 @@ class Problem3D:
     def spread_src(self, W, s, f):
         x, y, z = self.src[s]
         v = self.wave_f[self.bin[f]]
-        for g in range(-self.p.ngs, self.p.ngs + 1):
+        for g in range(-self.ngs, self.ngs + 1):
             xx = x + g + self.pad
             if 0 <= xx < self.nxg:
-                W[z, y + self.pady, xx] += self.gs[g + self.p.ngs] * v
+                W[z, y + self.pady, xx] += self.gs[g + self.ngs] * v
 
     def gather(self, W, vals):
         for i, (x, y, z) in enumerate(self.rec):
-            for g in range(-self.p.ngr, self.p.ngr + 1):
+            for g in range(-self.ngr, self.ngr + 1):
                 xx = x + g + self.pad
                 if 0 <= xx < self.nxg:
-                    vals[i] += self.gr[g + self.p.ngr] * W[z, y + self.pady, xx]
+                    vals[i] += self.gr[g + self.ngr] * W[z, y + self.pady, xx]
 
     def spread_rec(self, W, vals):
         for i, (x, y, z) in enumerate(self.rec):
-            for g in range(-self.p.ngr, self.p.ngr + 1):
+            for g in range(-self.ngr, self.ngr + 1):
                 xx = x + g + self.pad
                 if 0 <= xx < self.nxg:
-                    W[z, y + self.pady, xx] += self.gr[g + self.p.ngr] * vals[i]
+                    W[z, y + self.pady, xx] += self.gr[g + self.ngr] * vals[i]
 
     def down(self, M, om):
         W = M.copy()
@@ -280,7 +283,7 @@ def wem_forward(q, wavelet, s2, rho, kind=WEM_DATA_TIME, prec=32):
 def refl_forward(q, wavelet, s2, model, kind=WEM_DATA_TIME, prec=32):
     """BornRefl with one reflectivity [nz][ny][nx] for every frequency."""
     ones = np.ones_like(np.asarray(s2))
-    P = Problem3D(q, wavelet, s2, ones, prec)
+    P = Problem3D(q, wavelet, s2, ones, prec, refl=True)
     p = P.p
     m = np.zeros((P.nz, P.nyg, P.nxg), P.C)
     m[:, P.pady:P.pady + P.ny, P.pad:P.pad + P.nx] = np.asarray(model).reshape(P.nz, P.ny, P.nx)
@@ -301,7 +304,7 @@ def refl_forward(q, wavelet, s2, model, kind=WEM_DATA_TIME, prec=32):
 def refl_adjoint(q, wavelet, s2, data, kind=WEM_DATA_TIME, prec=32):
     """image = sum over (shot, frequency) of conj(bg) Up^H(rec^H data)."""
     ones = np.ones_like(np.asarray(s2))
-    P = Problem3D(q, wavelet, s2, ones, prec)
+    P = Problem3D(q, wavelet, s2, ones, prec, refl=True)
     p = P.p
     D = _absorb(P, data, kind)
     img = np.zeros((P.nz, P.nyg, P.nxg), P.C)

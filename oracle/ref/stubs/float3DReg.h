@@ -1,0 +1,54 @@
+// Stand-in for sepVector's float3DReg (test infrastructure only).
+#pragma once
+#include <vector>
+#include "floatHyper.h"
+#include "boost/multi_array.hpp"
+typedef boost::multi_array<float, 3> float3D;
+namespace SEP {
+class float3DReg : public floatHyper {
+ public:
+  float3DReg() {}
+  float3DReg(std::shared_ptr<hypercube> h) { init(h); }
+  float3DReg(const int n1, const int n2, const int n3) {
+    std::vector<axis> a;
+    a.push_back(axis(n1));
+    a.push_back(axis(n2));
+    a.push_back(axis(n3));
+    init(std::make_shared<hypercube>(a));
+  }
+  float3DReg(const axis& a1, const axis& a2, const axis& a3) {
+    std::vector<axis> a;
+    a.push_back(a1);
+    a.push_back(a2);
+    a.push_back(a3);
+    init(std::make_shared<hypercube>(a));
+  }
+  float3DReg(std::shared_ptr<hypercube> h, const float3D& vals) {
+    init(h);
+    std::copy(vals.data(), vals.data() + vals.num_elements(), _mat->data());
+  }
+  std::shared_ptr<float3DReg> clone() const {
+    auto x = std::make_shared<float3DReg>(getHyper());
+    if (!getSpaceOnly()) std::copy(_mat->data(), _mat->data() + _mat->num_elements(), x->_mat->data());
+    return x;
+  }
+  std::shared_ptr<float3DReg> cloneSpace() const {
+    auto x = std::make_shared<float3DReg>(getHyper());
+    x->setSpace();
+    return x;
+  }
+  void allocate() { init(getHyper()); }
+  virtual void cleanMemory() { setSpace(); }
+  std::shared_ptr<float3D> _mat;
+
+ private:
+  void init(std::shared_ptr<hypercube> h) {
+    setHyper(h);
+    std::vector<axis> ax = h->getAxes();
+    ax.resize(3, axis(1));
+    _mat.reset(new float3D(boost::extents[ax[2].n][ax[1].n][ax[0].n]));
+    setData(_mat->data());
+  }
+};
+}  // namespace SEP
+#include "sep_all.h"

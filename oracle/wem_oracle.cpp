@@ -1,6 +1,6 @@
 // ORACLE — test infrastructure only (see wem_oracle.hpp).  Drivers of the
 // CPU restatement and the extern "C" surface that tests/ and bench.py reach
-// through ctypes.  PARITY UNPINNED (no reference build, no golden vectors).
+// through ctypes.  PARITY PINNED to the reference run (tests/test_ref_pin.py).
 //
 // Drivers follow the reference's per-(shot, frequency) call sequence
 // literally, without the algebraic fusions the GPU library makes, so that
@@ -649,16 +649,37 @@ std::vector<C<R>> pad_field(const wem_params& p, const float* a, int slices, boo
   return out;
 }
 
+// BornRefl and BornTomo propagate on the model grid itself
+// (ext_born_refl.cpp:18-25, ext_born_tomo.cpp:20-25: Down/Up on the unpadded
+// slowness): `pad` is only OneStep's taper width (OneStep.h:27-35), the
+// source spreads over "ng" cells (here ngs) and the receivers are points
+// (Injection's default ng = 0), with no pad offset.  The returned block drives
+// the geometry; the caller's block, with its pad, drives Core's taper.
+inline wem_params refl_grid(const wem_params& p) {
+  check(p.pad != 1, "pad == 1 makes the taper divide by zero (Taper.h:19)");
+  wem_params q = p;
+  q.pad = 0;
+  q.ngr = 0;
+  return q;
+}
+
+// a block whose `pad` is the taper width `w` (Core reads the taper from it)
+inline wem_params with_taper(wem_params p, int w) {
+  p.pad = w;
+  return p;
+}
+
 // BornRefl::fwd_propagate (ext_born_refl.cpp:8-57): per (frequency, shot)
 // bg = Down(src); sc = bg m_f (IC::forward); Up in place; record.
 template <class R>
-void bornrefl_forward(const wem_params& p, const float* wavelet, const float* bs2, const float* model, void* data,
+void bornrefl_forward(const wem_params& p_in, const float* wavelet, const float* bs2, const float* model, void* data,
                       int kind, bool add, int nthreads) {
+  const wem_params p = refl_grid(p_in);
   Problem<R> P(p, wavelet);
   const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
   std::vector<C<R>> sp = pad_field<R>(p, bs2, 1, true);
   std::vector<C<R>> m = pad_field<R>(p, model, nf, false);
-  Core<R> core(p, sp.data(), nx, nz);
+  Core<R> core(p_in, sp.data(), nx, nz);
   DataF<R> D = new_dataf(P);
   const size_t ng = (size_t)nx * nz;
   parallel_for(nf, nthreads, [&](int f, int) {
@@ -684,12 +705,13 @@ void bornrefl_forward(const wem_params& p, const float* wavelet, const float* bs
 
 // BornRefl::adj_propagate (ext_born_refl.cpp:60-105): image_f += conj(bg) Up^H(rec)
 template <class R>
-void bornrefl_adjoint(const wem_params& p, const float* wavelet, const float* bs2, float* model, const void* data,
+void bornrefl_adjoint(const wem_params& p_in, const float* wavelet, const float* bs2, float* model, const void* data,
                       int kind, bool add, int nthreads) {
+  const wem_params p = refl_grid(p_in);
   Problem<R> P(p, wavelet);
   const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
   std::vector<C<R>> sp = pad_field<R>(p, bs2, 1, true);
-  Core<R> core(p, sp.data(), nx, nz);
+  Core<R> core(p_in, sp.data(), nx, nz);
   DataF<R> D = absorb_data(P, data, kind, nthreads);
   const size_t ng = (size_t)nx * nz, nm = (size_t)p.nx * nz;
   std::vector<C<R>> out(nm * nf);
@@ -720,12 +742,12 @@ void bornrefl_adjoint(const wem_params& p, const float* wavelet, const float* bs
 // No reference counterpart.  Per shot, BornRefl (ext_born_refl.cpp:8-105) on
 // the cropped model of the shot's aperture, as WEM.from_subspace builds a
 // sub-propagator (propagator/src/python/WEM.py:24-30): the aperture's model
-// columns [x0, x0 + w), padded by pad (edge-extended), a row of nxg + 2 tap_s
-// points, its own RefSampler; the shot's devices inside the aperture.  The
-// imaging condition IC (ic.cpp:5-29) is extended over horizontal lags
-// l = -hm .. hm:  forward sc(x) = sum_l r_l(x - l) bg(x - 2l),
-// adjoint image_l(y) += conj(bg(y - l)) a(y + l), r and the image zero off
-// the aperture's model cells, bg and a zero off the padded row.
+// columns [x0, x0 + w) with BornRefl's conventions (refl_grid: no model pad,
+// `pad` the taper width, point receivers), a row of w + 2 tap_s points, its
+// own RefSampler; the shot's devices inside the aperture.  The imaging
+// condition IC (ic.cpp:5-29) is extended over horizontal lags l = -hm .. hm:
+// forward sc(x) = sum_l r_l(x - l) bg(x - 2l), adjoint
+// image_l(y) += conj(bg(y - l)) a(y + l), r, bg and a zero off the aperture.
 template <class R>
 struct Aperture {
   wem_params ps;             // the cropped problem: nx = w, tap = tap_s
@@ -768,9 +790,10 @@ Aperture<R> make_aperture(const Problem<R>& P, const float* bs2, int is, int x0,
 }
 
 template <class R>
-void offborn_forward(const wem_params& p, const float* wavelet, const float* bs2, int nh, const int* ax0,
+void offborn_forward(const wem_params& p_in, const float* wavelet, const float* bs2, int nh, const int* ax0,
                      const int* aw, const int* atap, const float* model, void* data, int kind, bool add,
                      int nthreads) {
+  const wem_params p = refl_grid(p_in);
   check(nh >= 1 && nh % 2 == 1, "nh must be odd");
   check(p.nref == 1, "one reference slowness");
   Problem<R> P(p, wavelet);
@@ -781,7 +804,7 @@ void offborn_forward(const wem_params& p, const float* wavelet, const float* bs2
   for (int is = 0; is < p.ns; ++is) {
     Aperture<R> A = make_aperture(P, bs2, is, ax0[is], aw[is], atap[is]);
     const int nxg = A.nxg;
-    Core<R> core(A.ps, A.sp.data(), nxg, nz);
+    Core<R> core(with_taper(A.ps, p_in.pad), A.sp.data(), nxg, nz);
     const size_t ng = (size_t)nxg * nz;
     parallel_for(nf, nthreads, [&](int f, int) {
       const int bin = P.F.bin[f];
@@ -810,9 +833,10 @@ void offborn_forward(const wem_params& p, const float* wavelet, const float* bs2
 }
 
 template <class R>
-void offborn_adjoint(const wem_params& p, const float* wavelet, const float* bs2, int nh, const int* ax0,
+void offborn_adjoint(const wem_params& p_in, const float* wavelet, const float* bs2, int nh, const int* ax0,
                      const int* aw, const int* atap, float* model, const void* data, int kind, bool add,
                      int nthreads) {
+  const wem_params p = refl_grid(p_in);
   check(nh >= 1 && nh % 2 == 1, "nh must be odd");
   check(p.nref == 1, "one reference slowness");
   Problem<R> P(p, wavelet);
@@ -824,7 +848,7 @@ void offborn_adjoint(const wem_params& p, const float* wavelet, const float* bs2
   for (int is = 0; is < p.ns; ++is) {
     Aperture<R> A = make_aperture(P, bs2, is, ax0[is], aw[is], atap[is]);
     const int nxg = A.nxg;
-    Core<R> core(A.ps, A.sp.data(), nxg, nz);
+    Core<R> core(with_taper(A.ps, p_in.pad), A.sp.data(), nxg, nz);
     const size_t ng = (size_t)nxg * nz;
     parallel_for(nf, nthreads, [&](int f, int) {
       const int bin = P.F.bin[f];
@@ -858,14 +882,15 @@ void offborn_adjoint(const wem_params& p, const float* wavelet, const float* bs2
 // Down, reflectivity, Up, record; Born_down.cpp:14-27) and Born_up on the
 // up background Up(refl_f bg) (Born_up.cpp:14-22)
 template <class R>
-void borntomo_forward(const wem_params& p, const float* wavelet, const float* bs2, const float* refl,
+void borntomo_forward(const wem_params& p_in, const float* wavelet, const float* bs2, const float* refl,
                       const float* dm, void* data, int kind, bool add, int nthreads) {
+  const wem_params p = refl_grid(p_in);
   Problem<R> P(p, wavelet);
   const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
   std::vector<C<R>> sp = pad_field<R>(p, bs2, 1, true);
   std::vector<C<R>> rf = pad_field<R>(p, refl, nf, true);
   std::vector<C<R>> g = pad_field<R>(p, dm, 1, false);
-  Core<R> core(p, sp.data(), nx, nz);
+  Core<R> core(p_in, sp.data(), nx, nz);
   DataF<R> D = new_dataf(P);
   const size_t ng = (size_t)nx * nz;
   parallel_for(nf, nthreads, [&](int f, int) {
@@ -906,14 +931,15 @@ void borntomo_forward(const wem_params& p, const float* wavelet, const float* bs
 // then shots) the row ends with the LinUp^H term of the last (f, s) alone, so
 // the as-coded mode runs the terms in that order in one task.
 template <class R>
-void borntomo_adjoint(const wem_params& p, const float* wavelet, const float* bs2, const float* refl, float* dm,
+void borntomo_adjoint(const wem_params& p_in, const float* wavelet, const float* bs2, const float* refl, float* dm,
                       const void* data, int kind, bool add, int nthreads) {
+  const wem_params p = refl_grid(p_in);
   Problem<R> P(p, wavelet);
   const int nx = P.nxg, nz = p.nz, nf = P.nfreq();
   const bool exact = p.adjoint_mode == WEM_ADJ_EXACT;
   std::vector<C<R>> sp = pad_field<R>(p, bs2, 1, true);
   std::vector<C<R>> rf = pad_field<R>(p, refl, nf, true);
-  Core<R> core(p, sp.data(), nx, nz);
+  Core<R> core(p_in, sp.data(), nx, nz);
   DataF<R> D = absorb_data(P, data, kind, nthreads);
   const size_t ng = (size_t)nx * nz, nm = (size_t)p.nx * nz;
   const int ntask = exact ? nf : 1;

@@ -7,13 +7,14 @@
 // gives the fp32 restatement (the parity target) and its fp64 twin (the
 // accuracy oracle).  Each function cites the reference file:line it follows.
 //
-// PARITY UNPINNED: the reference needs FFTW, TBB, Boost, the SEP I/O
-// libraries and the ISPC compiler, none of which exist here, and its tests
-// hold no numeric golden vectors.  What pins this restatement is structural:
-// the reference's one known-answer test (extWEM on a frequency-constant model
-// equals WEM bit for bit, propagator/test/test_wem_ops.py:268-282), dot-product
-// tests on the reference's test setups, the fp64 twin, and numpy.fft for the
-// transform.
+// PARITY PINNED to the reference run: the reference's own propagator
+// sources, compiled unchanged by oracle/ref/Makefile against stand-ins for
+// FFTW, TBB, Boost and the SEP libraries, give the golden outputs of
+// tests/golden/ref_*.npz (tests/test_ref_pin.py: this restatement within 5e-5
+// of them for WEM, BornFull, BornRefl, BornTomo, extWEM and extBornFull).
+// Also: the reference's known-answer test (extWEM on a frequency-constant
+// model equals WEM bit for bit, propagator/test/test_wem_ops.py:268-282),
+// dot-product tests on the reference's set-ups, the fp64 twin, numpy.fft.
 #pragma once
 
 #include <algorithm>

@@ -1,0 +1,98 @@
+"""Generate the reference-run golden fixtures of tests/golden (ref_*.npz).
+
+The outputs come from the reference's own operator classes (WEM, BornFull,
+BornRefl, BornTomo, extWEM, extBornFull of propagator/src), compiled from
+the reference checkout by oracle/ref/Makefile and called through
+oracle/ref_oracle.py; this script needs that checkout (WEM_REFERENCE, or the
+default path in ref_oracle).  Each fixture holds its inputs (wavelet, models,
+perturbations, data) and the reference's outputs, so the tests compare
+against them on machines without the reference.
+
+    python tests/golden/make_ref_golden.py
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path[:0] = [ROOT, os.path.join(ROOT, "wem-fwi_gb300"), os.path.join(ROOT, "tests")]
+
+from cases import rand_c, small_case  # noqa: E402
+from oracle import ref_oracle as R  # noqa: E402
+
+# (name, small_case keywords, operators)
+CASES = [
+    ("ssf", dict(prop="ssf", nref=1, ns=2), ("wem", "born")),
+    ("pspi3", dict(prop="pspi", nref=3, ns=2, tap=4, pad=2), ("wem", "born")),
+    ("ssf_t2_tap0", dict(prop="ssf", nref=1, ns=1, nx=50, tap=0, pad=0, ntaylor=2), ("wem", "born")),
+    ("pspi2_odd_t0", dict(prop="pspi", nref=2, ns=2, nx=51, ntaylor=0), ("wem", "born")),
+    ("ssf_tpad", dict(prop="ssf", nref=1, ns=1, nz=20), ("wem", "born")),
+    ("refl_tomo", dict(prop="pspi", nref=2, ns=2, nz=12, tap=4, pad=3), ("refl", "tomo")),
+    ("ext", dict(prop="ssf", nref=1, ns=2, nz=16), ("extwem", "extborn")),
+]
+# BornRefl and BornTomo spread the source over "ng" cells (ext_born_refl.cpp:18)
+EXTRA_PAR = {"ssf_tpad": dict(tpad=32), "refl_tomo": dict(ng=2)}
+
+
+def run_case(name, kw, ops, seed):
+    p, par, wav, s, rho = small_case(**kw)
+    par = dict(par, **EXTRA_PAR.get(name, {}))
+    g = R.Grid(p.nx, p.nz, p.dx, p.dz, p.nt, p.dt)
+    nf = R.nfreq(par, g, wav)
+    rng = np.random.default_rng(seed)
+    out = dict(wav=wav, s=s, rho=rho, nf=np.int32(nf))
+    data_in = (rng.random((int(par["ns"]), int(par["nr"]), p.nt)) - .5).astype(np.float32)
+    out["data_in"] = data_in
+    if "wem" in ops:
+        out["wem"] = R.wem_forward(par, g, wav, s, rho)
+    if "born" in ops:
+        ds = (rand_c(rng, s.shape) * 1e-8).astype(np.complex64)
+        dr = (rand_c(rng, s.shape) * 0.1).astype(np.complex64)
+        out.update(ds=ds, dr=dr)
+        out["born_fwd"] = R.born_forward(par, g, wav, s, rho, ds, dr)
+        out["born_adj_s"], out["born_adj_r"] = R.born_adjoint(par, g, wav, s, rho, data_in)
+    if "refl" in ops:
+        m = (rand_c(rng, (nf, p.nz, p.nx)) * 0.1).astype(np.complex64)
+        out["refl_m"] = m
+        out["refl_fwd"] = R.bornrefl_forward(par, g, wav, s, m)
+        out["refl_adj"] = R.bornrefl_adjoint(par, g, wav, s, data_in, nf)
+    if "tomo" in ops:
+        refl = (rand_c(rng, (nf, p.nz, p.nx)) * 0.2).astype(np.complex64)
+        dm = (rand_c(rng, s.shape) * 1e-8).astype(np.complex64)
+        out.update(tomo_refl=refl, tomo_dm=dm)
+        out["tomo_fwd"] = R.borntomo_forward(par, g, wav, s, refl, dm)
+        out["tomo_adj"] = R.borntomo_adjoint(par, g, wav, s, refl, data_in)
+    if "extwem" in ops or "extborn" in ops:
+        s3 = (np.repeat(s[None], nf, 0) * (1 + 0.02 * rng.standard_normal((nf, 1, 1)))).astype(np.complex64)
+        r3 = np.repeat(rho[None], nf, 0).astype(np.complex64)
+        out.update(s3=s3, r3=r3)
+        if "extwem" in ops:
+            out["extwem"] = R.extwem_forward(par, g, wav, s3, r3)
+        if "extborn" in ops:
+            ds3 = (rand_c(rng, s3.shape) * 1e-8).astype(np.complex64)
+            dr3 = (rand_c(rng, s3.shape) * 0.1).astype(np.complex64)
+            out.update(ds3=ds3, dr3=dr3)
+            out["extborn_fwd"] = R.extborn_forward(par, g, wav, s3, r3, ds3, dr3)
+            out["extborn_adj_s"], out["extborn_adj_r"] = R.extborn_adjoint(par, g, wav, s3, r3, data_in)
+    meta = dict(name=name, small_case=kw, par=par, ops=list(ops), seed=seed,
+                source="reference propagator/src compiled by oracle/ref/Makefile")
+    out["meta"] = np.frombuffer(json.dumps(meta).encode(), np.uint8)
+    return out
+
+
+def main():
+    if not R.available():
+        raise SystemExit(f"reference checkout not found at {R.ref_root()} (set WEM_REFERENCE)")
+    R.build()
+    for i, (name, kw, ops) in enumerate(CASES):
+        out = run_case(name, kw, ops, seed=100 + i)
+        path = os.path.join(HERE, f"ref_{name}.npz")
+        np.savez_compressed(path, **out)
+        print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
+
+
+if __name__ == "__main__":
+    main()

@@ -14,7 +14,9 @@ from wemgpu.params import WEM_DATA_FREQ, WEM_DATA_TIME, make_params, make_params
 
 
 def case3d(nx=24, ny=24, nz=8, pad=2, pady=2, prop="ssf", nref=1, ns=2, nt=64, dt=0.008, fmin=6.0, fmax=12.0,
-           phase_law="ispc", seed=7, ngs=1, ngr=0, rstep=2, N=256):
+           phase_law="ispc", seed=7, ngs=1, ngr=0, rstep=2, N=256, refl=False):
+    """refl: the plane lengths of the reflectivity pair, which does not pad
+    the model (pad, pad_y are taper widths there): N = nx + 2 tap."""
     rng = np.random.default_rng(seed)
     s2d, rho2d = layered_model(nz, nx, seed)
     # a slowness that varies along y too
@@ -28,8 +30,9 @@ def case3d(nx=24, ny=24, nz=8, pad=2, pady=2, prop="ssf", nref=1, ns=2, nt=64, d
     rx, ry = np.meshgrid(np.arange(0, nx, rstep) * d, np.arange(0, ny, rstep) * d)
     rx, ry = rx.ravel(), ry.ravel()
     rz = np.zeros_like(rx)
-    tap = (N - nx - 2 * pad) // 2
-    tapy = (N - ny - 2 * pady) // 2 if ny > 1 else 0
+    grid_pad, grid_pady = (0, 0) if refl else (pad, pady)
+    tap = (N - nx - 2 * grid_pad) // 2
+    tapy = (N - ny - 2 * grid_pady) // 2 if ny > 1 else 0
     par = dict(prop=prop, nref=nref, tap=tap, pad=pad, fmin=fmin, fmax=fmax, ngs=ngs, ngr=ngr, phase_law=phase_law)
     q = make_params3d(par, nx=nx, ny=ny, nz=nz, dx=d, dy=d, dz=d, nt=nt, dt=dt, sx=sx, sy=sy, sz=sz, rx=rx, ry=ry,
                       rz=rz, pad_y=pady if ny > 1 else 0, tap_y=tapy)
@@ -97,8 +100,9 @@ def test_3d_single_line_is_2d_gpu(gpu_lib, oracle, prop, nref):
     assert rel_l2(d3, d2) < 1e-5
     o = oracle.wem_forward(p2, wav, s2, r2, kind=WEM_DATA_TIME, prec=64)
     assert rel_l2(d3, o) < 1e-4
-    op = Refl3DOp(q, wav, s)
-    ref = BornReflOp(p2, wav, s2)
+    qr, par_r, _, _, _ = case3d(ny=1, prop=prop, nref=nref, nx=40, rstep=1, refl=True)
+    op = Refl3DOp(qr, wav, s)
+    ref = BornReflOp(params2d(qr, par_r), wav, s2)
     nf = ref.nfreq()
     rng = np.random.default_rng(3)
     m = rand_c(rng, s.shape)
@@ -127,6 +131,7 @@ def test_3d_matches_oracle(gpu_lib, kw):
     for prec in (32, 64):
         o = O3.wem_forward(q, wav, s, rho, kind=WEM_DATA_TIME, prec=prec)
         assert rel_l2(d, o) < 1e-4, (prec, rel_l2(d, o))
+    q, par, wav, s, rho = case3d(refl=True, **kw)
     op = Refl3DOp(q, wav, s)
     rng = np.random.default_rng(4)
     m = rand_c(rng, s.shape)
@@ -154,9 +159,10 @@ def test_3d_matches_oracle(gpu_lib, kw):
 def test_3d_checkpointing_is_bit_exact(gpu_lib):
     from wemgpu.core import Refl3DOp, Wem3DOp
     q, par, wav, s, rho = case3d(nz=11, prop="pspi", nref=2)
+    qr = case3d(nz=11, prop="pspi", nref=2, refl=True)[0]
     rng = np.random.default_rng(5)
     m = rand_c(rng, s.shape)
-    op = Refl3DOp(q, wav, s)
+    op = Refl3DOp(qr, wav, s)
     wem = Wem3DOp(q, wav)
     d0 = np.zeros((q.p.ns, q.p.nr, q.p.nt), np.float32)
     op.forward(m, d0)
@@ -176,7 +182,7 @@ def test_3d_autograd_is_the_adjoint(gpu_lib):
     import torch
     from wemgpu.autograd import reflectivity_data_3d
     from wemgpu.core import Refl3DOp
-    q, par, wav, s, rho = case3d(nz=6)
+    q, par, wav, s, rho = case3d(nz=6, refl=True)
     op = Refl3DOp(q, wav, s)
     rng = np.random.default_rng(6)
     m = torch.from_numpy(rand_c(rng, s.shape)).cuda().requires_grad_(True)

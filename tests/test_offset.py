@@ -23,9 +23,10 @@ ROWS = (256, 384, 512, 768, 1024)
 
 def row_of(w, pad, tap):
     """Row length and leading zero pad of an aperture row: the smallest of
-    the warp kernels' lengths that holds w + 2 pad + 2 tap, padded equally."""
-    n = next(r for r in ROWS if r >= w + 2 * pad + 2 * tap)
-    return n, (n - w - 2 * pad) // 2
+    the warp kernels' lengths that holds w + 2 tap, padded equally (the
+    aperture is not padded by `pad`, BornRefl's taper width)."""
+    n = next(r for r in ROWS if r >= w + 2 * tap)
+    return n, (n - w) // 2
 
 
 def offset_case(nx=120, nz=20, ns=4, pad=4, tap=0, prop="ssf", phase_law="ispc", widths=(40, 64, 120, 80),
@@ -123,10 +124,10 @@ def test_oracle_dot(oracle, nh):
 
 
 def test_row_rule():
-    assert row_of(40, 4, 0) == (256, 104)
+    assert row_of(40, 4, 0) == (256, 108)
     assert row_of(256, 0, 0) == (256, 0)
     assert row_of(258, 0, 0) == (384, 63)
-    assert row_of(1000, 4, 6) == (1024, 8)
+    assert row_of(1000, 4, 6) == (1024, 12)
 
 
 # ------------------------------------------------------------------- GPU
@@ -185,10 +186,10 @@ def test_offset_one_lag_is_bornrefl_gpu(gpu_lib):
     """One lag, full apertures: the GPU offset operator against the GPU
     BornRefl (its own oracle-pinned path) with the same row."""
     from wemgpu.core import BornReflOp
-    p, par, wav, s, _, _ = offset_case(widths=(120,), tap=64)  # 120 + 8 + 128 = 256 points
+    p, par, wav, s, _, _ = offset_case(widths=(120,), tap=68)  # 120 + 136 = 256 points (pad is the taper)
     ap = np.array([(0, p.nx)] * p.ns, np.int32)
     op = _op(p, wav, s, 1, ap)
-    assert list(op.rows()[1]) == [64] * p.ns
+    assert list(op.rows()[1]) == [68] * p.ns
     ref = BornReflOp(p, wav, s)
     nf = ref.nfreq()
     rng = np.random.default_rng(5)

@@ -1,9 +1,9 @@
 """CPU checks of the oracle (the restatement the GPU is held to).
 
-PARITY UNPINNED: no reference build and no numeric golden vectors exist, so
-the oracle is pinned by the reference's structural known-answer test, exact
-dot tests, numpy.fft and its fp64 twin, and by the documented quirks of the
-reference code it reproduces.
+The oracle is pinned to the reference run by tests/test_ref_pin.py (golden
+outputs of the reference's own sources); these checks add the reference's
+structural known-answer test, exact dot tests, numpy.fft, its fp64 twin and
+the documented quirks of the reference code it reproduces.
 """
 import numpy as np
 import pytest

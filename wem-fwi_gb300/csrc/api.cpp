@@ -249,9 +249,12 @@ class Engine {
   // kind: 0 BornFull / WEM, 1 BornRefl, 2 BornTomo (propagator/src/ext_born_refl.cpp,
   // ext_born_tomo.cpp); the variants run on the Born passes with the
   // switches of DevCtx
-  Engine(const wem_params& p, const float* wavelet, bool ext, bool born, int kind = 0)
-      : p_(p), ext_(ext), born_(born), kind_(kind) {
+  Engine(const wem_params& p_in, const float* wavelet, bool ext, bool born, int kind = 0)
+      : p_(refl_conventions(p_in, kind)), ext_(ext), born_(born), kind_(kind),
+        taper_w_(p_in.pad) {
+    const wem_params& p = p_;
     require(wavelet != nullptr, "wavelet is NULL");
+    require(taper_w_ != 1, "pad == 1 makes the taper divide by zero (Taper.h:19)");
     geo_ = make_geometry(p, wavelet);
     F_ = geo_.nfreq();
     M_ = ext ? F_ : 1;
@@ -305,6 +308,21 @@ class Engine {
 
   int nfreq() const { return F_; }
   const wem_params& params() const { return p_; }
+
+  // BornRefl and BornTomo (ext_born_refl.cpp:18-25, ext_born_tomo.cpp:20-25)
+  // propagate on the model grid itself: Down/Up are built on the unpadded
+  // slowness, so `pad` is only the width of OneStep's taper (OneStep.h:27-35),
+  // the source spreads over the reference's "ng" cells (here `ngs`) and the
+  // receivers are points (Injection's default ng = 0), none offset by a pad.
+  // The offset Born (kind 3) is BornRefl on each shot's cropped model and
+  // keeps these conventions.
+  static wem_params refl_conventions(wem_params p, int kind) {
+    if (kind == 1 || kind == 2 || kind == 3) {
+      p.pad = 0;
+      p.ngr = 0;
+    }
+    return p;
+  }
 
   void set_background(const void* s2, const void* rho) {
     require(s2 && rho, "background model is NULL");
@@ -516,7 +534,7 @@ class Engine {
                 "source of shot " + std::to_string(s) + " outside its aperture");
       const int nxg = o.w + 2 * pad;
       o.N = off_row_length(nxg + 2 * p_.tap);
-      require(o.N > 0, "aperture of shot " + std::to_string(s) + " too wide: w + 2 pad + 2 tap must be <= 1024");
+      require(o.N > 0, "aperture of shot " + std::to_string(s) + " too wide: w + 2 tap must be <= 1024");
       o.tap = (o.N - nxg) / 2;
     }
     // rows: shots by row length, then shot, then frequency
@@ -538,7 +556,7 @@ class Engine {
       toff[s] = t;
       t += (long long)nz * nxg;
       tpo[s] = (int)tpr.size();
-      const std::vector<double> tp = taper(nxg, pad);
+      const std::vector<double> tp = taper(nxg, taper_w_);
       for (int i = 0; i < nxg; ++i) tpr.push_back((float)(tp[i] / o.N));
       onxg_max_ = std::max(onxg_max_, nxg);
     }
@@ -951,7 +969,7 @@ class Engine {
   // one shot of a conformal-map operator: its mapped grid (p.dx, p.dz) and
   // devices (g) and the gather tables of its map
   Engine(const wem_params& p, const Geometry& g, const ShotMap& m, bool born, std::shared_ptr<Scratch> ws)
-      : p_(p), ext_(false), born_(born), kind_(0) {
+      : p_(p), ext_(false), born_(born), kind_(0), taper_w_(p.pad) {
     ws_ = std::move(ws);
     geo_ = g;
     F_ = geo_.nfreq();
@@ -1049,6 +1067,7 @@ class Engine {
   wem_params p_;
   bool ext_, born_;
   int kind_ = 0;
+  int taper_w_ = 0;  // OneStep's taper width: the reference's `pad`
   int M_img_ = 1;  // image slices: per frequency for the extended operators and BornRefl
   bool have_bg_ = false;
   Geometry geo_;
@@ -1185,7 +1204,7 @@ class Engine {
   void build_static() {
     const Geometry& g = geo_;
     std::vector<cd> tw = twiddles(g.N);
-    std::vector<double> k = k_grid(g.N, p_.dx), tp = taper(g.nxg, p_.pad);
+    std::vector<double> k = k_grid(g.N, p_.dx), tp = taper(g.nxg, taper_w_);
     std::vector<float> kf(k.begin(), k.end()), tpf(g.nxg), om(F_);
     for (int i = 0; i < g.nxg; ++i) tpf[i] = (float)(tp[i] / g.N);
     for (int f = 0; f < F_; ++f) om[f] = (float)(2 * 3.14159265358979323846 * (double)g.freq[f]);
@@ -1519,8 +1538,16 @@ class Engine {
 // along x (S) and the per-reference planes after the column pass (T).
 class Engine3D {
  public:
-  Engine3D(const wem3d_params& q, const float* wavelet) : p_(q.p) {
+  // refl: the reflectivity Born / migration pair, which keeps the 2D
+  // BornRefl conventions (ext_born_refl.cpp:18-25): propagation on the model
+  // plane itself, pad and pad_y the taper widths only, point receivers
+  Engine3D(const wem3d_params& q, const float* wavelet, bool refl = false) : p_(q.p) {
     require(wavelet != nullptr, "wavelet is NULL");
+    const int twx = p_.pad, twy = q.pad_y;
+    if (refl) {
+      p_.pad = 0;
+      p_.ngr = 0;
+    }
     require(q.ny >= 1 && q.dy > 0, "ny must be >= 1 and dy > 0");
     require(q.pad_y >= 0 && q.tap_y >= 0 && q.pad_y != 1, "pad_y/tap_y must be >= 0 (pad_y != 1)");
     require(q.ny > 1 || (q.pad_y == 0 && q.tap_y == 0), "a single line (ny = 1) takes no y padding");
@@ -1529,14 +1556,16 @@ class Engine3D {
     require(p_.cmap == WEM_CMAP_NONE, "3D operators have no conformal maps");
     geo_ = make_geometry(p_, wavelet);
     ny_ = q.ny;
-    pady_ = q.pad_y;
+    pady_ = refl ? 0 : q.pad_y;
     const int nx = p_.nx, nz = p_.nz;
     nxg_ = nx + 2 * p_.pad;
     nyg_ = ny_ + 2 * pady_;
     Nx_ = nxg_ + 2 * p_.tap;
     Ny_ = nyg_ + 2 * q.tap_y;
-    require(k3_supported(Nx_, Ny_), "3D planes need Nx = nx + 2 pad + 2 tap and Ny = ny + 2 pad_y + 2 tap_y "
-                                    "in {256, 384, 512, 768, 1024} (or Ny = 1 for ny = 1)");
+    require(k3_supported(Nx_, Ny_), refl ? "3D reflectivity planes need Nx = nx + 2 tap and Ny = ny + 2 tap_y "
+                                           "in {256, 384, 512, 768, 1024} (or Ny = 1 for ny = 1)"
+                                         : "3D planes need Nx = nx + 2 pad + 2 tap and Ny = ny + 2 pad_y + 2 tap_y "
+                                           "in {256, 384, 512, 768, 1024} (or Ny = 1 for ny = 1)");
     require(p_.nref <= nxg_ * nyg_, "nref larger than the padded slice");
     F_ = geo_.nfreq();
     const int ns = geo_.ns, nr = geo_.nr;
@@ -1564,7 +1593,7 @@ class Engine3D {
     c_.Qx = Nx_ / 2;
     c_.Qy = std::max(Ny_ / 2, 1);
     std::vector<float> kxq(kx.begin(), kx.begin() + c_.Qx), kyq(ky.begin(), ky.begin() + c_.Qy);
-    std::vector<double> tx = taper(nxg_, p_.pad), ty = taper(nyg_, pady_);
+    std::vector<double> tx = taper(nxg_, twx), ty = taper(nyg_, twy);
     std::vector<float> tp((size_t)nyg_ * nxg_);
     for (int y = 0; y < nyg_; ++y)
       for (int x = 0; x < nxg_; ++x) tp[(size_t)y * nxg_ + x] = (float)(tx[x] * ty[y] / ((double)Nx_ * Ny_));
@@ -2265,7 +2294,7 @@ int refl3d_create(const wem3d_params* p, const float* wavelet, const void* s2, r
   return guard([&] {
     require(p && out, "NULL argument");
     auto h = std::make_unique<refl3d_handle>();
-    h->e = std::make_unique<Engine3D>(*p, wavelet);
+    h->e = std::make_unique<Engine3D>(*p, wavelet, true);
     h->e->set_background_unit(s2);
     *out = h.release();
   });

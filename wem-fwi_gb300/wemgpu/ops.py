@@ -29,6 +29,17 @@ def _grid_params(par, model_hyper: Hypercube, wave: Vector, data: Vector = None)
     return p
 
 
+def _refl_params(par, model_hyper: Hypercube, wave: Vector, data: Vector = None):
+    """BornRefl / BornTomo read the source spreading from "ng"
+    (ext_born_refl.cpp:18, ext_born_tomo.cpp:20) and record with point
+    receivers; the library takes "ng" in ngs."""
+    p = _grid_params(par, model_hyper, wave, data)
+    m = par.pars if hasattr(par, "pars") else (par or {})
+    p.ngs = int(m.get("ng", 0))
+    p.ngr = 0
+    return p
+
+
 def _vecs(model):
     if isinstance(model, SuperVector):
         return model.vecs
@@ -207,7 +218,7 @@ class BornRefl(Propagator):
 
     def __init__(self, model, slowness, data, wave, par):
         self.wave, self.par, self.domain, self.range = wave, par, model, data
-        self.params = _grid_params(par, slowness.getHyper(), wave, data)
+        self.params = _refl_params(par, slowness.getHyper(), wave, data)
         self.cppMode = core.BornReflOp(self.params, wave.getNdArray(), slowness.getNdArray())
 
     def set_background(self, slow):
@@ -229,7 +240,7 @@ class BornTomo(Propagator):
 
     def __init__(self, model, data, wave, par):
         self.wave, self.par, self.domain, self.range = wave, par, model, data
-        self.params = _grid_params(par, model.getHyper(), wave, data)
+        self.params = _refl_params(par, model.getHyper(), wave, data)
         self.cppMode = core.BornTomoOp(self.params, wave.getNdArray(), model.getNdArray())
 
     def setBgRefl(self, refl):
