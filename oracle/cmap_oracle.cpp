@@ -2,7 +2,8 @@
 // restated in cmap_oracle.hpp (conformal/src: ShiftAndScale.h, ComplexLog.h,
 // Rotation.h; propagator/src/PropParam.h:88-137).  Compiled with
 // -ffp-contract=off: float coordinates are truncated to grid cells, so the
-// rounding must not change with the machine.  PARITY UNPINNED.
+// rounding must not change with the machine.  PARITY PINNED to the reference
+// run (tests/test_ref_pin.py).
 #include "cmap_oracle.hpp"
 
 namespace wo {

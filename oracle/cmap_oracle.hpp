@@ -4,7 +4,10 @@
 // (propagator/src/PropParam.h:88-137, wem_prop.cpp:19-45,
 // born_prop.cpp:28-70, 138-232).  Only the oracle drivers include it.
 //
-// PARITY UNPINNED (no reference build, no golden vectors).  The maps follow
+// PARITY PINNED: WEM and Born through both maps (and with explicit device
+// coordinates) are held to the reference's own sources, compiled unchanged
+// by oracle/ref/Makefile (fixtures tests/golden/ref_cmap_*.npz,
+// tests/test_ref_pin.py).  The maps follow
 // the reference class by class: each holds its coordinate tables zmap (the
 // preimage of every output sample), umap (the image of every input sample)
 // and its Jacobian, in float complex arithmetic, and a chain applies its two

@@ -3,12 +3,11 @@ interpolation operators of the FWI preconditioner; only tests/ import it,
 as the checker of the library's ``lanczos2d_*`` / ``spline2d_*`` entry
 points.
 
-PARITY UNPINNED: the reference's operator library cannot be built here
-(ISPC, TBB, Boost and SEP I/O are absent) and its tests hold no numeric
-golden vectors for these operators (operator/test/test_operator.py runs dot
-tests only); the restatement is pinned by its dot test (Lanczos, and the
-spline before its edge copies), by partition of unity on the interior and
-by exact reproduction of samples that fall on coarse nodes.
+PARITY PINNED: the reference's own LanczosInterpolation2D.h / Spline2D.h
+and lanczos_kernel.ispc, compiled by oracle/ref/Makefile, give the golden
+outputs of tests/golden/refinterp.npz (tests/test_ref_pin.py, 1e-5); also
+its dot test (Lanczos, and the spline before its edge copies), partition of
+unity on the interior and exact reproduction of samples on coarse nodes.
 
 Filters follow the reference's loops and arithmetic (float32 with the
 Lanczos weights in float64, as the reference mixes them); the products are

@@ -15,6 +15,8 @@
 #include <vector>
 
 #include "BornFull.h"
+#include "LanczosInterpolation2D.h"
+#include "Spline2D.h"
 #include "BornRefl.h"
 #include "BornTomo.h"
 #include "WEM.h"
@@ -227,6 +229,32 @@ int ref_extborn(const char* kv, int adj, int nt, float ot, float dt, const float
     } else {
       op.forward(m, d, false);
       std::memcpy(data, d->getVals(), sizeof(float) * (size_t)nt * nr * ns);
+    }
+  });
+}
+
+// LanczosInterpolation2D (kind 0; p0, p1 the half widths in coarse cells)
+// or Spline2D (kind 1; p0, p1 = a, b) from the coarse model grid
+// (mn1 x mn2, spacings md1, md2) to the fine one (dn1 x dn2): forward reads
+// model and writes data, adjoint the reverse (operator/src/
+// LanczosInterpolation2D.h:14-90, Spline2D.h:14-90)
+int ref_interp2d(int kind, int adj, int mn1, float md1, int mn2, float md2, int dn1, float dd1, int dn2, float dd2,
+                 float p0, float p1, float* model, float* data) {
+  return guarded([&] {
+    auto m = std::make_shared<complex2DReg>(std::make_shared<hypercube>(axis(mn1, 0.f, md1), axis(mn2, 0.f, md2)));
+    auto d = std::make_shared<complex2DReg>(std::make_shared<hypercube>(axis(dn1, 0.f, dd1), axis(dn2, 0.f, dd2)));
+    const size_t nm = sizeof(std::complex<float>) * (size_t)mn1 * mn2, nd = sizeof(std::complex<float>) * (size_t)dn1 * dn2;
+    std::unique_ptr<Operator<complex2DReg, complex2DReg>> op;
+    if (kind == 0) op.reset(new LanczosInterpolation2D(m, d, std::vector<float>{p0, p1}));
+    else op.reset(new Spline2D(m, d, p0, p1));
+    if (adj) {
+      std::memcpy(d->getVals(), data, nd);
+      op->adjoint(m, d, false);
+      std::memcpy(model, m->getVals(), nm);
+    } else {
+      std::memcpy(m->getVals(), model, nm);
+      op->forward(m, d, false);
+      std::memcpy(data, d->getVals(), nd);
     }
   });
 }

@@ -18,9 +18,13 @@ does, and returns numpy arrays in the library's layouts: models [nz][nx]
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
+import json
 import os
+import shutil
 import subprocess
+import tempfile
 
 import numpy as np
 
@@ -57,16 +61,42 @@ def lib():
     return _lib
 
 
+_TMP = None
+
+
+def _json_file(obj) -> str:
+    """A JSON file the reference reads by path (its "coord" geometry file,
+    Device.h:65-85, and the "cmap_angles" file, PropParam.h:119-129)."""
+    global _TMP
+    if _TMP is None:
+        _TMP = tempfile.mkdtemp(prefix="wemref_")
+        atexit.register(shutil.rmtree, _TMP, True)
+    fd, path = tempfile.mkstemp(suffix=".json", dir=_TMP)
+    with os.fdopen(fd, "w") as f:
+        json.dump(obj, f)
+    return path
+
+
 def _kv(par: dict) -> bytes:
+    """The reference's parameters as "key=value;..."; coordinate lists (sx,
+    sz, rx, rz) and rotation angles go into the JSON files it reads."""
     items = []
+    coords = {}
     for k, v in par.items():
         if k in _OWN_KEYS:
             if str(v).lower() != str(_OWN_KEYS[k]):
                 raise ValueError(f"the reference has no {k}={v!r} (it behaves as {k}={_OWN_KEYS[k]!r})")
             continue
+        if k in ("sx", "sz", "rx", "rz"):
+            coords[k] = [float(x) for x in np.asarray(v, np.float64).ravel()]
+            continue
+        if k == "cmap_angles" and not isinstance(v, str):
+            v = _json_file({"a": [float(x) for x in np.asarray(v, np.float64).ravel()]})
         if isinstance(v, (list, tuple, np.ndarray)):
-            raise ValueError(f"{k}: coordinate lists go through the reference's JSON file path, not offered here")
+            raise ValueError(f"{k}: lists are not reference parameters")
         items.append(f"{k}={int(v) if isinstance(v, bool) else v}")
+    if coords:
+        items.append(f"coord={_json_file(coords)}")
     return ";".join(items).encode()
 
 
@@ -101,7 +131,9 @@ class Grid:
 
 
 def _counts(par):
-    return int(par["ns"]), int(par["nr"])
+    ns = len(par["sx"]) if "sx" in par else int(par["ns"])
+    nr = len(par["rx"]) if "rx" in par else int(par["nr"])
+    return ns, nr
 
 
 def nfreq(par, g: Grid, wavelet) -> int:
@@ -207,3 +239,22 @@ def extborn_adjoint(par, g: Grid, wavelet, bs2, brho, data):
     d = np.ascontiguousarray(data, np.float32)
     _call("ref_extborn", h[0], 1, *h[1:], nf, _p(bs2), _p(brho), _p(ds2), _p(drho), ns, nr, _p(d))
     return ds2, drho
+
+
+def interp2d(kind, model_axes, data_axes, p0, p1, x, adj=False):
+    """LanczosInterpolation2D ("lanczos": p0, p1 the half widths in coarse
+    cells) or Spline2D ("spline": p0, p1 = a, b) from the coarse grid
+    model_axes = ((n1, d1), (n2, d2)) to the fine grid data_axes; forward
+    maps a model [n2][n1] to data, adjoint the reverse."""
+    (mn1, md1), (mn2, md2) = model_axes
+    (dn1, dd1), (dn2, dd2) = data_axes
+    m = np.zeros((mn2, mn1), np.complex64)
+    d = np.zeros((dn2, dn1), np.complex64)
+    if adj:
+        d[:] = x
+    else:
+        m[:] = x
+    _call("ref_interp2d", 0 if kind == "lanczos" else 1, int(adj), mn1, ctypes.c_float(md1), mn2,
+          ctypes.c_float(md2), dn1, ctypes.c_float(dd1), dn2, ctypes.c_float(dd2), ctypes.c_float(p0),
+          ctypes.c_float(p1), _p(m), _p(d))
+    return m if adj else d

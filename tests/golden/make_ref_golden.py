@@ -1,7 +1,9 @@
-"""Generate the reference-run golden fixtures of tests/golden (ref_*.npz).
+"""Generate the reference-run golden fixtures of tests/golden (ref_*.npz and
+refinterp.npz).
 
 The outputs come from the reference's own operator classes (WEM, BornFull,
-BornRefl, BornTomo, extWEM, extBornFull of propagator/src), compiled from
+BornRefl, BornTomo, extWEM, extBornFull of propagator/src; the interpolators
+LanczosInterpolation2D and Spline2D of operator/src), compiled from
 the reference checkout by oracle/ref/Makefile and called through
 oracle/ref_oracle.py; this script needs that checkout (WEM_REFERENCE, or the
 default path in ref_oracle).  Each fixture holds its inputs (wavelet, models,
@@ -20,10 +22,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path[:0] = [ROOT, os.path.join(ROOT, "wem-fwi_gb300"), os.path.join(ROOT, "tests")]
 
-from cases import rand_c, small_case  # noqa: E402
+from cases import cmap_case, rand_c, small_case  # noqa: E402
 from oracle import ref_oracle as R  # noqa: E402
 
-# (name, small_case keywords, operators)
+# (name, case keywords, operators); keywords with "cmap" build a
+# cmap_case (explicit device coordinates, a conformal map), the others a
+# small_case
 CASES = [
     ("ssf", dict(prop="ssf", nref=1, ns=2), ("wem", "born")),
     ("pspi3", dict(prop="pspi", nref=3, ns=2, tap=4, pad=2), ("wem", "born")),
@@ -32,19 +36,26 @@ CASES = [
     ("ssf_tpad", dict(prop="ssf", nref=1, ns=1, nz=20), ("wem", "born")),
     ("refl_tomo", dict(prop="pspi", nref=2, ns=2, nz=12, tap=4, pad=3), ("refl", "tomo")),
     ("ext", dict(prop="ssf", nref=1, ns=2, nz=16), ("extwem", "extborn")),
+    ("coords", dict(cmap=0, prop="pspi", nref=2), ("wem", "born")),
+    ("cmap_log", dict(cmap=1, prop="ssf", nref=1), ("wem", "born")),
+    ("cmap_rot", dict(cmap=2, prop="pspi", nref=3), ("wem", "born")),
 ]
+
+
+def make_case(kw):
+    return cmap_case(**kw) if "cmap" in kw else small_case(**kw)
 # BornRefl and BornTomo spread the source over "ng" cells (ext_born_refl.cpp:18)
 EXTRA_PAR = {"ssf_tpad": dict(tpad=32), "refl_tomo": dict(ng=2)}
 
 
 def run_case(name, kw, ops, seed):
-    p, par, wav, s, rho = small_case(**kw)
+    p, par, wav, s, rho = make_case(kw)
     par = dict(par, **EXTRA_PAR.get(name, {}))
     g = R.Grid(p.nx, p.nz, p.dx, p.dz, p.nt, p.dt)
     nf = R.nfreq(par, g, wav)
     rng = np.random.default_rng(seed)
     out = dict(wav=wav, s=s, rho=rho, nf=np.int32(nf))
-    data_in = (rng.random((int(par["ns"]), int(par["nr"]), p.nt)) - .5).astype(np.float32)
+    data_in = (rng.random((p.ns, p.nr, p.nt)) - .5).astype(np.float32)
     out["data_in"] = data_in
     if "wem" in ops:
         out["wem"] = R.wem_forward(par, g, wav, s, rho)
@@ -77,9 +88,38 @@ def run_case(name, kw, ops, seed):
             out.update(ds3=ds3, dr3=dr3)
             out["extborn_fwd"] = R.extborn_forward(par, g, wav, s3, r3, ds3, dr3)
             out["extborn_adj_s"], out["extborn_adj_r"] = R.extborn_adjoint(par, g, wav, s3, r3, data_in)
-    meta = dict(name=name, small_case=kw, par=par, ops=list(ops), seed=seed,
+    par = {k: (list(map(float, v)) if isinstance(v, (list, tuple, np.ndarray)) else v) for k, v in par.items()}
+    meta = dict(name=name, case=kw, par=par, ops=list(ops), seed=seed,
                 source="reference propagator/src compiled by oracle/ref/Makefile")
     out["meta"] = np.frombuffer(json.dumps(meta).encode(), np.uint8)
+    return out
+
+
+# model-space interpolators of the FWI preconditioner (operator/src
+# LanczosInterpolation2D.h, Spline2D.h): (name, coarse axes, fine axes,
+# kind, parameters); axes ((n1, d1), (n2, d2)) as scripts/fwi.py builds them
+INTERP = [
+    ("fwi_like_lanczos", ((17, 47.5), (9, 37.375)), ((77, 10.0), (24, 13.0)), "lanczos", (2.0, 3.0)),
+    ("fwi_like_spline", ((17, 47.5), (9, 37.375)), ((77, 10.0), (24, 13.0)), "spline", (1 / 3, 1 / 3)),
+    ("square_bspline", ((12, 3.0), (12, 3.0)), ((34, 1.0), (34, 1.0)), "spline", (0.0, 1.0)),
+    ("bench_lanczos", ((13, 200.0), (9, 150.0)), ((193, 12.5), (93, 13.0)), "lanczos", (1.0, 1.0)),
+]
+
+
+def interp_fixture(seed):
+    rng = np.random.default_rng(seed)
+    out, meta = {}, []
+    for name, ma, da, kind, (p0, p1) in INTERP:
+        (m1, m2), (d1, d2) = ma, da
+        m = (rng.standard_normal((m2[0], m1[0])) + 1j * rng.standard_normal((m2[0], m1[0]))).astype(np.complex64)
+        d = (rng.standard_normal((d2[0], d1[0])) + 1j * rng.standard_normal((d2[0], d1[0]))).astype(np.complex64)
+        out[name + "_m"], out[name + "_d"] = m, d
+        out[name + "_fwd"] = R.interp2d(kind, ma, da, p0, p1, m)
+        out[name + "_adj"] = R.interp2d(kind, ma, da, p0, p1, d, adj=True)
+        meta.append(dict(name=name, model_axes=ma, data_axes=da, kind=kind, params=[p0, p1]))
+    out["meta"] = np.frombuffer(json.dumps(dict(cases=meta, seed=seed,
+                                                source="reference operator/src compiled by oracle/ref/Makefile")
+                                           ).encode(), np.uint8)
     return out
 
 
@@ -87,6 +127,9 @@ def main():
     if not R.available():
         raise SystemExit(f"reference checkout not found at {R.ref_root()} (set WEM_REFERENCE)")
     R.build()
+    path = os.path.join(HERE, "refinterp.npz")
+    np.savez_compressed(path, **interp_fixture(200))
+    print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
     for i, (name, kw, ops) in enumerate(CASES):
         out = run_case(name, kw, ops, seed=100 + i)
         path = os.path.join(HERE, f"ref_{name}.npz")

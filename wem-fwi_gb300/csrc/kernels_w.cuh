@@ -316,6 +316,24 @@ __device__ __forceinline__ void adj_post(const WRow& w, const float2 (&X)[E], fl
   }
 }
 
+// Forward step with several references (SSF.cpp:14-31, PSPI.cpp:11-28):
+// the padded row is transformed once and every reference's field is the
+// inverse transform of that spectrum times its phase row, selected into Y.
+// X holds the row on entry; the caller's state row is dead meanwhile.
+template <int E, class O>
+__device__ __forceinline__ void fwd_step_mr(const WRow& w, const Tabs& T, int nref, float2 (&X)[E], O&& Y) {
+  wfft<E, false>(X, w.sb, w.tw, w.lane);
+#pragma unroll 1
+  for (int jr = 0; jr < nref; ++jr) {
+    float2 Z[E];
+#pragma unroll
+    for (int j = 0; j < E; ++j) Z[j] = X[j];
+    fwd_mid<E>(w, T, jr, Z);
+    wfft<E, true>(Z, w.sb, w.tw, w.lane);
+    fwd_post<E, true>(w, T, jr, Z, Y);
+  }
+}
+
 // Taylor Born scatter (Scatter.cpp:35-111) for ntaylor <= 1; mode 0 forward,
 // 1 adjoint as coded (filter before scaling), 2 exact adjoint.
 // pre: the filter's input, u or conj(c_1) u (exact adjoint)
@@ -541,19 +559,19 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
     }
     if (z == nz - 1) break;
     // W = P_z W
-#pragma unroll 1
-    for (int jr = 0; jr < nj; ++jr) {
+    if constexpr (MR) {
+#pragma unroll
+      for (int j = 0; j < E; ++j) X[j] = W[j];
+      fwd_step_mr<E>(w, T, nj, X, Y);
+#pragma unroll
+      for (int j = 0; j < E; ++j) W[j] = Y[j];
+    } else {
 #pragma unroll
       for (int j = 0; j < E; ++j) X[j] = W[j];
       wfft<E, false>(X, w.sb, w.tw, lane);
-      fwd_mid<E>(w, T, jr, X);
+      fwd_mid<E>(w, T, 0, X);
       wfft<E, true>(X, w.sb, w.tw, lane);
-      if constexpr (MR) fwd_post<E, true>(w, T, jr, X, Y);
-      else fwd_post<E, false>(w, T, jr, X, W);
-    }
-    if constexpr (MR) {
-#pragma unroll
-      for (int j = 0; j < E; ++j) W[j] = Y[j];
+      fwd_post<E, false>(w, T, 0, X, W);
     }
     w_inject_src<E>(w, W, s, f, z + 1);
   }
@@ -583,19 +601,19 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
     if (!L.row_bytes && lane == 0 && z >= 2) l2_prefetch(A + (size_t)(z - 2) * nxg, nxg * 8);
     const Tabs T = ring.tabs(z);
     // W = P_z W + R[z-1] down[z-1]
-#pragma unroll 1
-    for (int jr = 0; jr < nj; ++jr) {
+    if constexpr (MR) {
+#pragma unroll
+      for (int j = 0; j < E; ++j) X[j] = W[j];
+      fwd_step_mr<E>(w, T, nj, X, Y);
+#pragma unroll
+      for (int j = 0; j < E; ++j) W[j] = Y[j];
+    } else {
 #pragma unroll
       for (int j = 0; j < E; ++j) X[j] = W[j];
       wfft<E, false>(X, w.sb, w.tw, lane);
-      fwd_mid<E>(w, T, jr, X);
+      fwd_mid<E>(w, T, 0, X);
       wfft<E, true>(X, w.sb, w.tw, lane);
-      if constexpr (MR) fwd_post<E, true>(w, T, jr, X, Y);
-      else fwd_post<E, false>(w, T, jr, X, W);
-    }
-    if constexpr (MR) {
-#pragma unroll
-      for (int j = 0; j < E; ++j) W[j] = Y[j];
+      fwd_post<E, false>(w, T, 0, X, W);
     }
     const float2* a = L.row_bytes ? wrow + (size_t)((z - 1) & 1) * nxg : A + (size_t)(z - 1) * nxg;
 #pragma unroll
@@ -638,9 +656,11 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, SlotLayout L
   // the three ops of one depth with tables T; up adds the stored rows
   // (a: A[z-1], b: B[z-1]) after the steps, down injects the source
   auto depth_ops = [&](const Tabs& T, int znext, const float2* a, const float2* b) {
+    // several references: ops 1 and 2 follow the loop, written out so that
+    // the stepped row is dead while its spectrum and transform are live
 #pragma unroll 1
-    for (int k = 0; k < 3; ++k) {
-      const int nj = (MR && k > 0) ? c.nref : 1;
+    for (int k = 0; k < (MR ? 1 : 3); ++k) {
+      const int nj = 1;
 #pragma unroll 1
       for (int jr = 0; jr < nj; ++jr) {
         if (k == 0) {
@@ -673,22 +693,24 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_fwd(DevCtx c, SlotLayout L
             const float2 v = sc_val(iw, 0, t1, k0, k1, c_mul(bg[j], q), X[j]);
             if (in) sd[j] = c_add(sd[j], v);
           }
-        } else if constexpr (MR) {
-          fwd_post<E, true>(w, T, jr, X, Y);
-        } else {
+        } else if constexpr (!MR) {
           if (k == 1) fwd_post<E, false>(w, T, jr, X, sd);
           else fwd_post<E, false>(w, T, jr, X, bg);
         }
       }
-      if constexpr (MR) {
-        if (k == 1) {
+    }
+    if constexpr (MR) {
+      // sd = P sd, then bg = P bg
 #pragma unroll
-          for (int j = 0; j < E; ++j) sd[j] = Y[j];
-        } else if (k == 2) {
+      for (int j = 0; j < E; ++j) X[j] = sd[j];
+      fwd_step_mr<E>(w, T, c.nref, X, Y);
 #pragma unroll
-          for (int j = 0; j < E; ++j) bg[j] = Y[j];
-        }
-      }
+      for (int j = 0; j < E; ++j) sd[j] = Y[j];
+#pragma unroll
+      for (int j = 0; j < E; ++j) X[j] = bg[j];
+      fwd_step_mr<E>(w, T, c.nref, X, Y);
+#pragma unroll
+      for (int j = 0; j < E; ++j) bg[j] = Y[j];
     }
     if (a) {
 #pragma unroll
@@ -837,11 +859,22 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
     if (!act) continue;
     w_store<E>(w, SBG + (size_t)z * nxg, bg);
     if (z == nz - 1) continue;
+    if constexpr (MR) {
+      // bg = P bg: one forward transform for all references; the bg row
+      // is dead until the references' sum replaces it
+#pragma unroll
+      for (int j = 0; j < E; ++j) X[j] = bg[j];
+      fwd_step_mr<E>(w, ring.tabs(z), nj_step, X, Y);
+#pragma unroll
+      for (int j = 0; j < E; ++j) bg[j] = Y[j];
+      w_inject_src<E>(w, bg, s, f, z + 1);
+    }
 #pragma unroll 1
-    for (int k = 0; k < 2; ++k) {
+    for (int k = MR ? 1 : 0; k < 2; ++k) {
       const Tabs T = ring.tabs(z + k);
+      const int nj = nj_step;
 #pragma unroll 1
-      for (int jr = 0; jr < nj_step; ++jr) {
+      for (int jr = 0; jr < nj; ++jr) {
         if (k == 0) {
 #pragma unroll
           for (int j = 0; j < E; ++j) X[j] = bg[j];
@@ -912,9 +945,26 @@ __global__ void __launch_bounds__(kW * 32, 1) kw_born_adj(DevCtx c, SlotLayout L
         }
         if (!c.no_fwd_record) w_inject_rec<E>(w, wd, s, bin, nz - 1, bins);
       }
+      if constexpr (MR) {
+        // D first (it is independent of B and C): bu[z-1] = P_z bu +
+        // R[z-1] bg[z-1], one forward transform for all references
+        if (z < nz && z >= 2) {
+#pragma unroll
+          for (int j = 0; j < E; ++j) X[j] = bu[j];
+          fwd_step_mr<E>(w, ring.tabs(z), nj_step, X, Y);
+#pragma unroll
+          for (int j = 0; j < E; ++j) {
+            bool in;
+            const int x = xclamp(w, j, in);
+            const float2 r = Tp.rc[x], b = bgp[x];
+            bu[j] = in ? c_fma(Y[j], r, b) : Y[j];
+          }
+        }
+      }
 #pragma unroll 1
       for (int k = 0; k < 4; ++k) {
         // k: 0 B, 1 C, 2 D, 3 A
+        if (MR && k == 2) continue;
         const bool on = k < 2 ? (z < nz) : (k == 2 ? (z < nz && z >= 2) : (z >= 2 && (z < nz || keep_last)));
         if (!on) continue;
         const bool step = (k == 0 || k == 2);
