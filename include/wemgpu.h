@@ -166,6 +166,13 @@ int wem_set_kernel_path(int path);
  * Results do not depend on it beyond float rounding of the image sums. */
 int wem_set_row_ctas(int mode);
 
+/* Source field of fwi_gradient (no counterpart in the reference: pass
+ * structure).  1 (default): where both passes run in one launch of the
+ * grouped warp kernels, the modelling pass stores the down-going source
+ * field and the Born adjoint reuses it instead of recomputing it; 0: the
+ * Born adjoint recomputes it.  Results differ by float rounding only. */
+int wem_set_gradient_split(int on);
+
 /* ------------------------------------------------ nonlinear modelling (WEM) */
 typedef struct wem_handle wem_handle;
 

@@ -36,6 +36,7 @@ bool g_stats_on = false;
 bool g_plain = false;
 int g_path = 0;  // 0 automatic, 1 shared-memory kernels, 2 warp-per-row kernels
 int g_rows = 0;  // 0 automatic, 1 grouped rows per CTA, 2 one-row CTAs
+bool g_split_off = false;  // fwi_gradient: the Born adjoint recomputes the source field
 std::vector<std::pair<std::string, KStat>> g_stats;
 
 std::mutex g_stats_mu;  // engines may run on several host threads
@@ -387,7 +388,10 @@ class Engine {
     const bool wp = warp_path();
     if (wp) pick_row_ctas();
     int G = wp ? warp_G(0) : pick_G([&](int g) { return smem_wem(ctx_, g); });
+    int chunks = 0;
+    wem_rows_all_ = false;
     for_chunks(G, plane * 8, [&](const Group* gd, int ng, int rows) {
+      wem_rows_all_ = ++chunks == 1 && (size_t)rows == (size_t)F_ * geo_.ns;
       float2* A = ws_->store1.as<float2>((size_t)rows * plane);
       if (wp) timed("k_wem", [&] { launch_pass_warp(0, ctx_, gd, ng, nullptr, nullptr, A, nullptr, nullptr, bins_, nullptr, nullptr, 0, 0); });
       else timed("k_wem", [&] { launch_wem(ctx_, gd, ng, G, A, bins_, 0); });
@@ -428,15 +432,39 @@ class Engine {
     }
     set_background(s2, rho);
     zero_bins();
+    // The modelling's down sweep computes the Born adjoint's source field bg
+    // (the same background, tables and kernels): with both passes in one
+    // launch of the warp kernels, rows numbered alike, the modelling stores
+    // bg itself and the adjoint runs only the receiver side's down sweep
+    const bool split = split_gradient();
+    ctx_.wem_store_bg = split ? 1 : 0;
     wem_pass();
+    ctx_.wem_store_bg = 0;
     // residual r = WEM(m) - d_obs in time, loss = 1/2 |r|^2, r back to bins
     const size_t nd = (size_t)geo_.ns * geo_.nr * p_.nt;
     Staged obs;
     obs.in(dobs, nd * 4);
     double* loss_h = residual_bins((const float*)obs.dev);
+    // the adjoint takes the stored bg only when the modelling ran every row
+    // in one launch and its own launch holds every row too (adj_pass)
+    adj_split_req_ = split && wem_rows_all_;
     adj_pass();
+    adj_split_req_ = false;
     grad_out(g_s2, g_rho, 0);  // ends with the stream synchronised
     return *loss_h;
+  }
+
+  // fwi_gradient may hand the source field from the modelling to the Born
+  // adjoint: warp kernels with grouped CTAs and one reference, the as-coded
+  // adjoint; the passes check that each ran every row in one launch (rows
+  // numbered frequency-major in both; the modelling's stored rows are the
+  // adjoint's first stored field, ws_->store1)
+  bool split_gradient() {
+    if (g_plain || g_split_off || !warp_path() || p_.nref != 1 || ext_ || kind_ != 0) return false;
+    if (p_.adjoint_mode != WEM_ADJ_COMPAT) return false;
+    pick_row_ctas();
+    if (!warp_adj_split(ctx_)) return false;
+    return true;
   }
 
   void born_forward(const void* ds2, const void* drho, void* data, int kind, int add) {
@@ -798,8 +826,11 @@ class Engine {
       float2* SG = reuse ? ws_->store3.as<float2>((size_t)rows * plane) : nullptr;
       float2* pr = ws_->part1.as<float2>((size_t)ng * plane);
       float2* ps = ws_->part2.as<float2>((size_t)ng * plane);
+      // rows numbered as the modelling's: the stored bg lines up
+      ctx_.adj_split = adj_split_req_ && wp && (size_t)rows == (size_t)F_ * geo_.ns ? 1 : 0;
       if (wp) timed("k_born_adj", [&] { launch_pass_warp(2, ctx_, gd, ng, nullptr, nullptr, BG, T, SG, bins_, pr, ps, compat, 0); });
       else timed("k_born_adj", [&] { launch_born_adj(ctx_, gd, ng, G, BG, T, bins_, pr, ps, compat, 0); });
+      ctx_.adj_split = 0;
       cuda_check(cudaGetLastError(), "k_born_adj launch");
       // chunk-local group ranges of each image slice
       std::vector<int> beg(M_img_ + 1, 0);
@@ -1068,6 +1099,8 @@ class Engine {
   bool ext_, born_;
   int kind_ = 0;
   int taper_w_ = 0;  // OneStep's taper width: the reference's `pad`
+  bool wem_rows_all_ = false;   // the last modelling pass ran every row in one launch
+  bool adj_split_req_ = false;  // fwi_gradient: the stored rows hold bg for the adjoint
   int M_img_ = 1;  // image slices: per frequency for the extended operators and BornRefl
   bool have_bg_ = false;
   Geometry geo_;
@@ -2147,6 +2180,10 @@ int wem_set_row_ctas(int mode) {
     require(mode >= 0 && mode <= 2, "mode must be 0, 1 or 2");
     g_rows = mode;
   });
+}
+int wem_set_gradient_split(int on) {
+  g_split_off = on == 0;
+  return WEM_OK;
 }
 int wem_set_plain(int plain) {
   g_plain = plain != 0;

@@ -14,6 +14,8 @@ void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* 
 template <int E>
 bool adj_reuse_w(const DevCtx& c, int compat);
 template <int E>
+bool adj_split_w(const DevCtx& c);
+template <int E>
 size_t smem_w_e(const DevCtx& c, bool slots);
 template <int E>
 int adj_rows_w(const DevCtx& c);
@@ -105,6 +107,17 @@ void launch_grad_warp(const DevCtx& c, const Group* g, int ng, const GradArgs& a
     case 24: launch_grad_w<24>(c, g, ng, a, st); break;
     case 32: launch_grad_w<32>(c, g, ng, a, st); break;
     default: break;
+  }
+}
+
+bool warp_adj_split(const DevCtx& c) {
+  switch (c.N / 32) {
+    case 8: return adj_split_w<8>(c);
+    case 12: return adj_split_w<12>(c);
+    case 16: return adj_split_w<16>(c);
+    case 24: return adj_split_w<24>(c);
+    case 32: return adj_split_w<32>(c);
+    default: return false;
   }
 }
 

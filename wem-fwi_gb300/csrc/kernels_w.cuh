@@ -550,12 +550,13 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
     if (!act) continue;
     const Tabs T = ring.tabs(z);
     w_record<E>(w, W, s, bin, z, bins);
+    const bool sbg = c.wem_store_bg != 0;
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       bool in;
       const int x = xclamp(w, j, in);
       const float2 r = T.rc[x];
-      if (in) A[(size_t)z * nxg + x] = c_mul(r, W[j]);
+      if (in) A[(size_t)z * nxg + x] = sbg ? W[j] : c_mul(r, W[j]);
     }
     if (z == nz - 1) break;
     // W = P_z W
@@ -581,7 +582,19 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
   auto issue_row = [&](int d) {
     if (L.row_bytes && act && d >= 0) warp_copy(wrow + (size_t)(d & 1) * nxg, A + (size_t)d * nxg, nxg * 8, lane);
   };
-  if (act) w_load<E>(w, A + (size_t)(nz - 1) * nxg, W);
+  if (act) {
+    w_load<E>(w, A + (size_t)(nz - 1) * nxg, W);
+    if (c.wem_store_bg) {
+      // the stored row is bg[nz-1]: the up field starts as R[nz-1] bg[nz-1]
+      const float2* r = rc_row(c, f, nz - 1);
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        bool in;
+        const float2 v = r[xclamp(w, j, in)];
+        W[j] = c_mul(v, W[j]);
+      }
+    }
+  }
   ring.issue(nz - 1);
   issue_row(nz - 2);
   cp_commit();
@@ -616,11 +629,23 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
       fwd_post<E, false>(w, T, 0, X, W);
     }
     const float2* a = L.row_bytes ? wrow + (size_t)((z - 1) & 1) * nxg : A + (size_t)(z - 1) * nxg;
+    if (c.wem_store_bg) {
+      // the stored row is bg[z-1]: W += R[z-1] bg[z-1]
+      const Tabs Tm = ring.tabs(z - 1);
 #pragma unroll
-    for (int j = 0; j < E; ++j) {
-      bool in;
-      const float2 v = a[xclamp(w, j, in)];
-      if (in) W[j] = c_add(W[j], v);
+      for (int j = 0; j < E; ++j) {
+        bool in;
+        const int x = xclamp(w, j, in);
+        const float2 v = a[x], r = Tm.rc[x];
+        if (in) W[j] = c_fma(W[j], r, v);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < E; ++j) {
+        bool in;
+        const float2 v = a[xclamp(w, j, in)];
+        if (in) W[j] = c_add(W[j], v);
+      }
     }
   }
   cp_wait0();
@@ -1128,7 +1153,10 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
     for (int x = lane; x < nxg; x += 32) xb[x] = zero;
   };
 
-  // ---------------- down sweep: bg (source side), wu (receiver side)
+  // ---------------- down sweep: bg (source side), wu (receiver side); with
+  // c.adj_split the modelling pass stored bg and kw_adj_down ran this sweep
+  // for the receiver side (T, its filtered spectra and the image IR)
+  if (!c.adj_split) {
   w_zero<E>(S);
   if (act) {
     if (!recv) {
@@ -1199,6 +1227,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
     __syncthreads();
     reduce_down(IR + (size_t)(z + 1) * nxg);
   }
+  }  // down sweep
 
   // ---------------- up sweep, iteration z = nz .. 1 builds image row z - 1
   // source side: bu[z-1] = P_z bu + R[z-1] bg[z-1] (op 0), LinUp^H
@@ -1362,6 +1391,105 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
   }
 }
 
+// Down sweep of the Born adjoint's receiver side alone, one warp per row,
+// for the FWI gradient, whose modelling pass has already stored the source
+// field bg of every depth (c.wem_store_bg): wu[0] = the injected data;
+// T[z+1] = P^H_{z+1} wu (stored, with its filtered spectrum for the
+// scatter's spectral reuse), wu[z+1] = T[z+1] + the data injected at z + 1;
+// IR[z] = sum over the CTA's rows, in row order, of wu[z] conj(bg[z]).  The
+// arithmetic of each row is that of kw_born_adj2's receiver warp; the
+// source warp's recomputation of bg is what this saves.  Two barriers per
+// depth, as there: the ring's copies are issued at the top of a depth and
+// waited for at its end; the products wait for the previous sum.
+template <int E, bool NT, int R>
+__global__ void __launch_bounds__(R * 32, 2) kw_adj_down(DevCtx c, SlotLayout L, const Group* groups,
+                                                         const float2* storeBG, float2* storeT, float2* storeG,
+                                                         const float2* bins, float2* imgR) {
+  const Carve<E> sm(c, L, false, R, true);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  stage_static<E>(c, sm);
+  const int nxg = c.nxg, nz = c.nz;
+  const Group gp = groups[blockIdx.x];
+  const int nrows = gp.n;
+  const bool act = warp < nrows;
+  float2* xb = sm.sb0 + warp * wbuf_len<E>();
+  const WRow w{c, sm.tw, xb, sm.taperN, sm.kx, lane, NT ? 0 : c.tap, NT ? 32 * E : c.nxg};
+  const int f = gp.f, s = gp.s0 + (act ? warp : 0), bin = c.bin[f];
+  const size_t plane = (size_t)nz * nxg, row = (size_t)gp.row0 + (act ? warp : 0);
+  const float2* SBG = storeBG + row * plane;
+  float2* ST = storeT + row * plane;
+  float2* SG = storeG ? storeG + row * plane : nullptr;
+  float2* IR = imgR + (size_t)blockIdx.x * plane;
+  const float om = c.omega[f];
+  const float2 zero = make_float2(0.f, 0.f);
+  const Ring ring{c, L, sm.ring, Src{nullptr, nullptr}, f};
+  const float2* xb0 = sm.sb0;
+  constexpr int WB = wbuf_len<E>();
+  float2 S[E], X[E], Yd[1];
+  // this row's products wu[z] conj(bg[z]) into its buffer
+  auto put_products = [&](int z) {
+    const float2* b = SBG + (size_t)z * nxg;
+#pragma unroll
+    for (int j = 0; j < E; ++j) {
+      bool in;
+      const int x = xclamp(w, j, in);
+      const float2 v = b[x];
+      if (in) xb[x] = c_mulc(S[j], v);
+    }
+  };
+  auto reduce_down = [&](float2* out) {
+    for (int x = threadIdx.x; x < nxg; x += blockDim.x) {
+      float2 a = zero;
+      for (int r = 0; r < nrows; ++r) a = c_add(a, xb0[r * WB + x]);
+      out[x] = a;
+    }
+  };
+  w_zero<E>(S);
+  if (act) {
+    w_inject_rec<E>(w, S, s, bin, 0, bins);
+    for (int x = lane; x < nxg; x += 32) ST[x] = zero;  // T[0] = 0
+    put_products(0);
+  }
+  ring.issue(0);
+  ring.issue(1);
+  cp_commit();
+  cp_wait0();
+  __syncthreads();
+  reduce_down(IR);
+  for (int z = 0; z + 1 < nz; ++z) {
+    __syncthreads();  // the buffers are summed; slot (z + 2) % 3 is free
+    ring.issue(z + 2);
+    cp_commit();
+    if (act) {
+      if (lane == 0 && z + 2 < nz) l2_prefetch(SBG + (size_t)(z + 2) * nxg, nxg * 8);
+      // T[z+1] = P^H_{z+1} wu
+      const Tabs T = ring.stabs(z + 1);
+      adj_pre<E, false>(w, T, 0, S, X);
+      wfft<E, false>(X, w.sb, w.tw, lane);
+      adj_mid<E, false>(w, T, 0, X, Yd);
+      if (SG) {
+        // filtered spectrum of T[z+1], every point (tap 0: N = nxg)
+        float2* g = SG + (size_t)(z + 1) * nxg;
+        const float s2 = 1.f / (om * om);
+#pragma unroll
+        for (int j = 0; j < E; ++j) {
+          const float k = w.kx[lane + 32 * j];
+          g[lane + 32 * j] = c_scale(X[j], k * k * s2);
+        }
+      }
+      wfft<E, true>(X, w.sb, w.tw, lane);
+      adj_post<E>(w, X, S);
+      w_store<E>(w, ST + (size_t)(z + 1) * nxg, S);
+      w_inject_rec<E>(w, S, s, bin, z + 1, bins);
+      put_products(z + 1);
+    }
+    cp_wait0();
+    __syncthreads();
+    reduce_down(IR + (size_t)(z + 1) * nxg);
+  }
+  cp_wait0();
+}
+
 // ------------------------------------------------------ host side
 // which: 0 WEM, 1 Born forward, 2 Born adjoint (one warp per row), 3 Born
 // adjoint with the two chains of a row on two warps (kw_born_adj2)
@@ -1377,6 +1505,7 @@ constexpr int kRowsWem = 16;
 // (kernels_wg.cuh); exchange buffers per CTA
 inline int nbuf_of(int which) {
   switch (which) {
+    case 8: return kRowsAdj2;
     case 3: return 2 * kRowsAdj2;
     case 7: return 2 * kRowsAdj2;
     case 4: return kRowsWem;
@@ -1387,6 +1516,7 @@ inline int nbuf_of(int which) {
 }
 // the tables a pass reads: as WEM (0), Born forward (1) or Born adjoint (2)
 inline int tables_of(int which) {
+  if (which == 8) return 3;  // the adjoint step alone: phase and split-step rows
   return (which == 4 || which == 5 || which == 7) ? 0 : ((which == 3 || which == 6) ? 2 : which);
 }
 // one-row CTAs leave the taper out of shared memory when the split-step table
@@ -1419,9 +1549,9 @@ SlotLayout slot_layout(const DevCtx& c, int pass, int limit) {
   L.fac = c.fac ? put(rowb) : -1;
   const bool need_ref = (!c.fac || c.nref > 1);
   L.ref = (need_ref && c.nxg % 16 == 0) ? put(c.nxg) : -1;
-  L.rc = put(rowb);
-  L.c0 = which != 0 ? put(rowb) : -1;
-  L.c1 = (which != 0 && c.ntaylor >= 1) ? put(rowb) : -1;
+  L.rc = which != 3 ? put(rowb) : -1;
+  L.c0 = (which != 0 && which != 3) ? put(rowb) : -1;
+  L.c1 = (which != 0 && which != 3 && c.ntaylor >= 1) ? put(rowb) : -1;
   L.dm = which == 1 ? put(rowb) : -1;
   L.dr = which == 1 ? put(rowb) : -1;
   L.bytes = off;
@@ -1558,6 +1688,18 @@ void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* 
       launch_adj2_one<E>(c, g, ng, sBG, sT, sG, bins, ir, is, compat, st);
       return;
     }
+    if (c.adj_split) {
+      // the receiver side's down sweep on its own (bg stored by the modelling)
+      const SlotLayout L8 = slot_layout<E>(c, 8, limit);
+      const size_t sm8 = smem_w<E>(c, 8, L8);
+      auto down = [&](auto kern) {
+        set_max_smem(kern);
+        kern<<<ng, kRowsAdj2 * 32, sm8, st>>>(c, L8, g, sBG, sT, sG, bins, ir);
+        note_launch();
+      };
+      if (c.tap == 0) down(kw_adj_down<E, true, kRowsAdj2>);
+      else down(kw_adj_down<E, false, kRowsAdj2>);
+    }
     const SlotLayout L3 = slot_layout<E>(c, 3, limit);
     const size_t sm3 = smem_w<E>(c, 3, L3);
     auto go = [&](auto kern) {
@@ -1578,6 +1720,16 @@ void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* 
   };
   if (c.nref > 1) go(kw_born_adj<E, true>);
   else go(kw_born_adj<E, false>);
+}
+
+// the FWI gradient may split the Born adjoint's down sweep off
+// (c.adj_split): one reference, the two-warp kernel with grouped CTAs, and
+// the receiver side's tables ring in shared memory
+template <int E>
+bool adj_split_w(const DevCtx& c) {
+  if (!adj2_fits<E>(c) || c.one_row) return false;
+  const SlotLayout L8 = slot_layout<E>(c, 8, max_smem_per_block());
+  return L8.nslots == 3 && (c.fac || L8.ref >= 0);
 }
 
 // rows per CTA the Born adjoint launcher expects

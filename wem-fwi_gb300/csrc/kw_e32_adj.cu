@@ -8,5 +8,6 @@ extern template void launch_adj2_one<32>(const DevCtx&, const Group*, int, float
 template void launch_adj_w<32>(const DevCtx&, const Group*, int, float2*, float2*, float2*, float2*, float2*,
                                 float2*, int, cudaStream_t);
 template bool adj_reuse_w<32>(const DevCtx&, int);
+template bool adj_split_w<32>(const DevCtx&);
 template int adj_rows_w<32>(const DevCtx&);
 }  // namespace wg

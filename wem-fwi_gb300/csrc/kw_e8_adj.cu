@@ -8,5 +8,6 @@ extern template void launch_adj2_one<8>(const DevCtx&, const Group*, int, float2
 template void launch_adj_w<8>(const DevCtx&, const Group*, int, float2*, float2*, float2*, float2*, float2*,
                                 float2*, int, cudaStream_t);
 template bool adj_reuse_w<8>(const DevCtx&, int);
+template bool adj_split_w<8>(const DevCtx&);
 template int adj_rows_w<8>(const DevCtx&);
 }  // namespace wg

@@ -33,6 +33,7 @@ _SIGS = {
     "wem_set_plain": (_i, [_i]),
     "wem_set_kernel_path": (_i, [_i]),
     "wem_set_row_ctas": (_i, [_i]),
+    "wem_set_gradient_split": (_i, [_i]),
     "wem_create": (_i, [_pp, _v, ctypes.POINTER(_h)]),
     "wem_destroy": (None, [_h]),
     "wem_get_nfreq": (_i, [_h, ctypes.POINTER(_i)]),
