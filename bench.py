@@ -19,9 +19,11 @@ that bounds it; ``cpu_baseline`` = the CPU restatement on the host cores on
 a bounded sample.  ``--workload c1|c2`` prints timings of the other
 configurations instead (not the benchmark line).
 
-``--impl reference`` times the CPU restatement of the reference (the
-reference itself cannot be built: FFTW, TBB, Boost, SEP I/O and ISPC are
-absent) on the same configuration and metric.
+``--impl reference`` times the CPU restatement of the reference on the same
+configuration and metric.  The reference's own sources compile only where
+its checkout is (oracle/ref, against stand-ins for FFTW, TBB, Boost and the
+SEP libraries: the pin of the restatement, not a build to time), so the arm
+runs the restatement, which is held to that build's outputs.
 """
 from __future__ import annotations
 
@@ -123,21 +125,23 @@ def workload(small=False, small_shots=8):
     return cfg
 
 
-# DRAM bytes (read + write) per (row, depth) of the pass kernels, from ncu
-# captures of the reduced case (16 shots x 21 frequencies, nz 300, N 768;
-# profiles/kw_born_adj2_e24_c3_small16.md): the traffic of a launch scales
-# with the rows it carries, so a full launch is this figure x rows x depths.
+# DRAM bytes (read + write) per (row, depth) of the gradient's passes, from
+# one ncu capture of the reduced case (16 shots x 21 frequencies, nz 300,
+# N 768; profiles/fwi_gradient_passes_e24_c3_small16.md; kernels of commit
+# 187d259): the traffic of a launch scales with the rows it carries, so a
+# full launch is this figure x rows x depths.  The Born adjoint pass of the
+# gradient is kw_adj_down + kw_born_adj2 (its up sweep), summed.
 TRAFFIC_PER_ROW_DEPTH = {
-    "k_born_adj": (1948216e3 + 2011339e3) / (336 * 300),
+    "k_born_adj": ((698917e3 + 1262201e3) + (1941243e3 + 78077e3)) / (336 * 300),
+    "k_wem": (692194e3 + 624966e3) / (336 * 300),
 }
-# warp instructions per (row, depth) of the pass kernels (smsp__inst_executed
-# of the same captures; profiles/kw_wem_e24_c3_small16.md for k_wem): the
-# pass kernels are bound by instruction issue, so the line also reports the
-# issue rate they reach against one warp instruction per SM sub-partition
-# per cycle
+# warp instructions per (row, depth) of the same passes (smsp__inst_executed
+# of the same capture): the pass kernels are bound by instruction issue, so
+# the line also reports the issue rate they reach against one warp
+# instruction per SM sub-partition per cycle
 INST_PER_ROW_DEPTH = {
-    "k_born_adj": 1387956947 / (336 * 300),
-    "k_wem": 418853610 / (336 * 300),
+    "k_born_adj": (254522058 + 907077570) / (336 * 300),
+    "k_wem": 444057558 / (336 * 300),
 }
 
 

@@ -170,7 +170,8 @@ int wem_set_row_ctas(int mode);
  * structure).  1 (default): where both passes run in one launch of the
  * grouped warp kernels, the modelling pass stores the down-going source
  * field and the Born adjoint reuses it instead of recomputing it; 0: the
- * Born adjoint recomputes it.  Results differ by float rounding only. */
+ * Born adjoint recomputes it.  Results differ by float rounding only;
+ * WEM_EINVAL for other values. */
 int wem_set_gradient_split(int on);
 
 /* ------------------------------------------------ nonlinear modelling (WEM) */

@@ -63,10 +63,11 @@ def test_invalid_parameters_are_rejected_on_host(lib, bad):
     assert e.value.code == 1  # WEM_EINVAL, before any device call
 
 
-@pytest.mark.parametrize("fn,bad", [("wem_set_kernel_path", 3), ("wem_set_row_ctas", 3), ("wem_set_row_ctas", -1)])
+@pytest.mark.parametrize("fn,bad", [("wem_set_kernel_path", 3), ("wem_set_row_ctas", 3), ("wem_set_row_ctas", -1),
+                                    ("wem_set_gradient_split", 2), ("wem_set_gradient_split", -1)])
 def test_launch_shape_knobs_validate_on_host(lib, fn, bad):
     from wemgpu._lib import WemError, call
     with pytest.raises(WemError) as e:
         call(fn, bad)
     assert e.value.code == 1  # WEM_EINVAL
-    call(fn, 0)  # the automatic choice is always accepted
+    call(fn, 1 if fn == "wem_set_gradient_split" else 0)  # the default is always accepted

@@ -591,9 +591,10 @@ def test_time_axis_lengths(gpu_lib, oracle, nt, tpad, dt):
 def test_fwi_gradient_split_matches_recompute(gpu_lib, oracle, case, row_ctas):
     """fwi_gradient with the source field stored by the modelling pass
     (kw_wem with wem_store_bg, the receiver side's down sweep in
-    kw_adj_down) equals the gradient whose Born adjoint recomputes it, and
-    the oracle's Born adjoint of the same residual; tap 0 with the spectral
-    reuse of the scatter and tap 4 without."""
+    kw_adj_down, kw_born_adj2's up sweep) equals the gradient whose Born
+    adjoint recomputes it, and the oracle's Born adjoint of the same
+    residual; tap 0 with the spectral reuse of the scatter and tap 4
+    without."""
     from wemgpu import _lib
     from wemgpu.core import FwiOp, WemOp
     p, par, wav, s, rho = small_case(nz=14, ns=4, **WARP_CASES[case])
@@ -603,16 +604,19 @@ def test_fwi_gradient_split_matches_recompute(gpu_lib, oracle, case, row_ctas):
     obs = (d * (1 + 0.1 * rng.standard_normal(d.shape))).astype(np.float32)
     out = {}
     try:
-        for on in (1, 0):
-            _lib.call("wem_set_gradient_split", on)
+        for mode in (1, 0):
+            _lib.call("wem_set_gradient_split", mode)
             g0, g1 = np.zeros_like(s), np.zeros_like(s)
             loss = FwiOp(p, wav).gradient(s, rho, obs, g0, g1)
-            out[on] = (loss, g0, g1)
+            out[mode] = (loss, g0, g1)
     finally:
         _lib.call("wem_set_gradient_split", 1)
-    (l1, a0, a1), (l0, b0, b1) = out[1], out[0]
-    assert l1 == pytest.approx(l0, rel=1e-6)
-    assert rel_l2(a0, b0) < 1e-5 and rel_l2(a1, b1) < 1e-5, (rel_l2(a0, b0), rel_l2(a1, b1))
+    l0, b0, b1 = out[0]
+    for mode in (1,):
+        l1, a0, a1 = out[mode]
+        assert l1 == pytest.approx(l0, rel=1e-6)
+        assert rel_l2(a0, b0) < 1e-5 and rel_l2(a1, b1) < 1e-5, (mode, rel_l2(a0, b0), rel_l2(a1, b1))
+    a0, a1 = out[1][1], out[1][2]
     res = (d - obs).astype(np.float32)
     q0, q1 = oracle.born_adjoint(p, wav, s, rho, res, kind=WEM_DATA_TIME, prec=64)
     assert rel_l2(a0, q0) < TOL_OP and rel_l2(a1, q1) < TOL_OP, (rel_l2(a0, q0), rel_l2(a1, q1))

@@ -2182,8 +2182,10 @@ int wem_set_row_ctas(int mode) {
   });
 }
 int wem_set_gradient_split(int on) {
-  g_split_off = on == 0;
-  return WEM_OK;
+  return guard([&] {
+    require(on == 0 || on == 1, "on must be 0 or 1");
+    g_split_off = on == 0;
+  });
 }
 int wem_set_plain(int plain) {
   g_plain = plain != 0;
