@@ -66,7 +66,10 @@ def test_fwi_gradient_matches_plain_launches(gpu_lib, case):
 
 def test_backward_is_the_transpose_of_born(gpu_lib):
     """Exact adjoint mode: for any data gradient r the leaves receive B^H r
-    with Re<B^H r, dm> = <B dm, r> (torch's convention for complex leaves)."""
+    with Re<B^H r, dm> = <B dm, r> (torch's convention for complex leaves),
+    to 1e-5.  r = B m' for an independent m' keeps both inner products far
+    from cancellation (white random data alone moves the ratio by up to
+    1e-4 through the float rounding of the outputs, test_born_dot_exact)."""
     from wemgpu.autograd import modelled_data
     from wemgpu.core import BornOp, WemOp
     p, wav, s, rho, d_obs, torch = _setup("exact")
@@ -76,17 +79,23 @@ def test_backward_is_the_transpose_of_born(gpu_lib):
     b = torch.from_numpy(rho).to(dev).requires_grad_(True)
     d = modelled_data(a, b, wem, born)
     rng = np.random.default_rng(21)
-    r = torch.from_numpy((rng.random(d.shape) - .5).astype(np.float32)).to(dev)
-    d.backward(r)
-    ds = (rng.standard_normal(s.shape) + 1j * rng.standard_normal(s.shape)).astype(np.complex64) * 1e-8
-    dr = (rng.standard_normal(s.shape) * 0.05).astype(np.complex64)
-    bd = np.zeros_like(d_obs)
+
+    def rc(shape):
+        return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+
+    ds, dr = rc(s.shape), rc(s.shape)
+    n0, n1 = rc(s.shape), rc(s.shape)
     born.set_background(s, rho)
+    rd = np.zeros_like(d_obs)
+    born.forward(n0 + 0.5 * ds, n1 + 0.5 * dr, rd)
+    r = torch.from_numpy(rd).to(dev)
+    d.backward(r)
+    bd = np.zeros_like(d_obs)
     born.forward(ds, dr, bd)
-    lhs = float(np.sum(bd.astype(np.float64) * r.cpu().numpy()))
+    lhs = float(np.sum(bd.astype(np.float64) * rd.astype(np.float64)))
     rhs = float(np.sum((np.conj(a.grad.cpu().numpy().astype(np.complex128)) * ds).real)
                 + np.sum((np.conj(b.grad.cpu().numpy().astype(np.complex128)) * dr).real))
-    assert abs(lhs / rhs - 1) < 1e-4, (lhs, rhs)
+    assert abs(lhs / rhs - 1) < 1e-5, (lhs, rhs)
 
 
 def test_objective_pspi_shared_memory_path(gpu_lib):
