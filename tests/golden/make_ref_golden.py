@@ -1,5 +1,5 @@
-"""Generate the reference-run golden fixtures of tests/golden (ref_*.npz and
-refinterp.npz).
+"""Generate the reference-run golden fixtures of tests/golden (ref_*.npz,
+refc1.npz and refinterp.npz).
 
 The outputs come from the reference's own operator classes (WEM, BornFull,
 BornRefl, BornTomo, extWEM, extBornFull of propagator/src; the interpolators
@@ -123,10 +123,28 @@ def interp_fixture(seed):
     return out
 
 
+def c1_fixture():
+    """Configuration c1 at full size (256 x 200, one shot, 64 frequencies,
+    SSF): the reference's modelling of the seeded model and its Born adjoint
+    (as coded) of that data at the same background."""
+    from wemgpu import synthetic as S
+    cfg = S.c1()
+    par = dict(cfg["par"])
+    g = R.Grid(cfg["nx"], cfg["nz"], cfg["dx"], cfg["dz"], cfg["nt"], cfg["dt"])
+    s, rho, wav = cfg["slow"], cfg["rho"], cfg["wavelet"]
+    d = R.wem_forward(par, g, wav, s, rho)
+    gs, gr = R.born_adjoint(par, g, wav, s, rho, d)
+    meta = dict(name="c1", par=par, source="reference propagator/src compiled by oracle/ref/Makefile")
+    return dict(s=s, wem=d, born_adj_s=gs, born_adj_r=gr, meta=np.frombuffer(json.dumps(meta).encode(), np.uint8))
+
+
 def main():
     if not R.available():
         raise SystemExit(f"reference checkout not found at {R.ref_root()} (set WEM_REFERENCE)")
     R.build()
+    path = os.path.join(HERE, "refc1.npz")
+    np.savez_compressed(path, **c1_fixture())
+    print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
     path = os.path.join(HERE, "refinterp.npz")
     np.savez_compressed(path, **interp_fixture(200))
     print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
