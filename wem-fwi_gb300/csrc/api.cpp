@@ -383,7 +383,10 @@ class Engine {
   }
 
   // modelling of the current background into the internal bins
-  void wem_pass() {
+  // bg_for_adjoint: the modelling also stores its down field in the
+  // adjoint's first stored field (ws_->store1), keeping its own rows of R bg
+  // in ws_->store4
+  void wem_pass(bool bg_for_adjoint = false) {
     const size_t plane = (size_t)p_.nz * geo_.nxg;
     const bool wp = warp_path();
     if (wp) pick_row_ctas();
@@ -392,9 +395,12 @@ class Engine {
     wem_rows_all_ = false;
     for_chunks(G, plane * 8, [&](const Group* gd, int ng, int rows) {
       wem_rows_all_ = ++chunks == 1 && (size_t)rows == (size_t)F_ * geo_.ns;
-      float2* A = ws_->store1.as<float2>((size_t)rows * plane);
+      const bool keep_bg = bg_for_adjoint && wp;
+      float2* A = (keep_bg ? ws_->store4 : ws_->store1).as<float2>((size_t)rows * plane);
+      ctx_.bg_store = keep_bg ? ws_->store1.as<float2>((size_t)rows * plane) : nullptr;
       if (wp) timed("k_wem", [&] { launch_pass_warp(0, ctx_, gd, ng, nullptr, nullptr, A, nullptr, nullptr, bins_, nullptr, nullptr, 0, 0); });
       else timed("k_wem", [&] { launch_wem(ctx_, gd, ng, G, A, bins_, 0); });
+      ctx_.bg_store = nullptr;
       cuda_check(cudaGetLastError(), "k_wem launch");
     }, wp);
   }
@@ -437,9 +443,7 @@ class Engine {
     // launch of the warp kernels, rows numbered alike, the modelling stores
     // bg itself and the adjoint runs only the receiver side's down sweep
     const bool split = split_gradient();
-    ctx_.wem_store_bg = split ? 1 : 0;
-    wem_pass();
-    ctx_.wem_store_bg = 0;
+    wem_pass(split);
     // residual r = WEM(m) - d_obs in time, loss = 1/2 |r|^2, r back to bins
     const size_t nd = (size_t)geo_.ns * geo_.nr * p_.nt;
     Staged obs;

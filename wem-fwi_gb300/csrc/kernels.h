@@ -26,7 +26,7 @@ struct DevCtx {
   int no_fwd_record;            // the forward-scattered (down) field is not recorded
   int last_rule;                // compat last depth row: 0 per shot (BornFull), 1 only the last (f, s)
   int one_row;                  // every group holds one row: the warp kernels use one-row CTAs
-  int wem_store_bg;             // the WEM pass stores the down field itself (R applied in its up sweep)
+  float2* bg_store;             // [rows][nz][nxg]: the WEM pass also stores its down field here, or null
   int adj_split;                // the Born adjoint's down sweep is kw_adj_down's, on the stored bg
   float dz, invN;
   const float2* tw;             // [N] exp(-2 pi i t/N)
@@ -123,7 +123,7 @@ void launch_pass_warp(int which, const DevCtx& c, const Group* g, int ng, const 
 // then needs s3: [rows][nz][nxg] filtered spectra of the stored T
 bool warp_adj_reuse(const DevCtx& c, int compat);
 // the FWI gradient's Born adjoint can run its down sweep as kw_adj_down on
-// the source field the modelling pass stored (c.wem_store_bg, c.adj_split)
+// the source field the modelling pass stored (c.bg_store, c.adj_split)
 bool warp_adj_split(const DevCtx& c);
 
 // exact gradient of the modelling (kernels_wg.cuh), two warps per row, one

@@ -531,6 +531,7 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
   const int nj = MR ? c.nref : 1;
   const size_t plane = (size_t)nz * nxg;
   float2* A = store + (size_t)(gp.row0 + (act ? warp : 0)) * plane;
+  float2* BG = c.bg_store ? c.bg_store + (size_t)(gp.row0 + (act ? warp : 0)) * plane : nullptr;
   const Ring ring{c, L, sm.ring, Src{nullptr, nullptr}, f};
   float2* wrow = reinterpret_cast<float2*>(sm.rows + (size_t)warp * 2 * L.row_bytes);
   float2 W[E], X[E];
@@ -550,14 +551,15 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
     if (!act) continue;
     const Tabs T = ring.tabs(z);
     w_record<E>(w, W, s, bin, z, bins);
-    const bool sbg = c.wem_store_bg != 0;
 #pragma unroll
     for (int j = 0; j < E; ++j) {
       bool in;
       const int x = xclamp(w, j, in);
       const float2 r = T.rc[x];
-      if (in) A[(size_t)z * nxg + x] = sbg ? W[j] : c_mul(r, W[j]);
+      if (in) A[(size_t)z * nxg + x] = c_mul(r, W[j]);
     }
+    // the down field itself for the Born adjoint of the FWI gradient
+    if (BG) w_store<E>(w, BG + (size_t)z * nxg, W);
     if (z == nz - 1) break;
     // W = P_z W
     if constexpr (MR) {
@@ -582,19 +584,7 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
   auto issue_row = [&](int d) {
     if (L.row_bytes && act && d >= 0) warp_copy(wrow + (size_t)(d & 1) * nxg, A + (size_t)d * nxg, nxg * 8, lane);
   };
-  if (act) {
-    w_load<E>(w, A + (size_t)(nz - 1) * nxg, W);
-    if (c.wem_store_bg) {
-      // the stored row is bg[nz-1]: the up field starts as R[nz-1] bg[nz-1]
-      const float2* r = rc_row(c, f, nz - 1);
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        bool in;
-        const float2 v = r[xclamp(w, j, in)];
-        W[j] = c_mul(v, W[j]);
-      }
-    }
-  }
+  if (act) w_load<E>(w, A + (size_t)(nz - 1) * nxg, W);
   ring.issue(nz - 1);
   issue_row(nz - 2);
   cp_commit();
@@ -629,23 +619,11 @@ __global__ void __launch_bounds__(R * 32, 1) kw_wem(DevCtx c, SlotLayout L, cons
       fwd_post<E, false>(w, T, 0, X, W);
     }
     const float2* a = L.row_bytes ? wrow + (size_t)((z - 1) & 1) * nxg : A + (size_t)(z - 1) * nxg;
-    if (c.wem_store_bg) {
-      // the stored row is bg[z-1]: W += R[z-1] bg[z-1]
-      const Tabs Tm = ring.tabs(z - 1);
 #pragma unroll
-      for (int j = 0; j < E; ++j) {
-        bool in;
-        const int x = xclamp(w, j, in);
-        const float2 v = a[x], r = Tm.rc[x];
-        if (in) W[j] = c_fma(W[j], r, v);
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < E; ++j) {
-        bool in;
-        const float2 v = a[xclamp(w, j, in)];
-        if (in) W[j] = c_add(W[j], v);
-      }
+    for (int j = 0; j < E; ++j) {
+      bool in;
+      const float2 v = a[xclamp(w, j, in)];
+      if (in) W[j] = c_add(W[j], v);
     }
   }
   cp_wait0();
@@ -1102,7 +1080,7 @@ __device__ __forceinline__ int launder(int v) {
   return r;
 }
 
-template <int E, bool NT, int R>
+template <int E, bool NT, int R, bool MR = false>
 __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayout L, const Group* groups,
                                                               float2* storeBG, float2* storeT, float2* storeG,
                                                               const float2* bins, float2* imgR, float2* imgS,
@@ -1138,7 +1116,16 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
   const Ring ring{c, L, sm.ring, Src{nullptr, nullptr}, f};
   const float2* xb0 = sm.sb0;
   constexpr int WB = wbuf_len<E>();
-  float2 S[E], X[E], Yd[1];
+  // Y: several references, the receiver side's sum of the references'
+  // spectra (PSPI adjoint step); one reference, unused
+  float2 S[E], X[E], Y[MR ? E : 1];
+  // a depth's tables: from the ring (one reference: every table fits), or,
+  // several references, from the ring where it fits and the global tables
+  // otherwise
+  auto tabs_at = [&](int d) {
+    if constexpr (MR) return ring.tabs(d);
+    else return ring.stabs(d);
+  };
 
   // this warp's row into its buffer (grid points)
   auto put = [&](const float2 (&v)[E]) {
@@ -1188,7 +1175,30 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
     cp_commit();
     if (act) {
       // source side: bg[z+1] = P_z bg + src; receiver side: T[z+1] = P^H_{z+1} wu
-      const Tabs T = ring.stabs(recv ? z + 1 : z);
+      const Tabs T = tabs_at(recv ? z + 1 : z);
+      if constexpr (MR) {
+        if (!recv) {
+          // one forward transform, one inverse per reference, selected into bg
+#pragma unroll
+          for (int j = 0; j < E; ++j) X[j] = S[j];
+          fwd_step_mr<E>(w, T, c.nref, X, S);
+          w_inject_src<E>(w, S, s, f, z + 1);
+          w_store<E>(w, SBG + (size_t)(z + 1) * nxg, S);
+        } else {
+          // the references' spectra summed, one inverse transform
+#pragma unroll 1
+          for (int jr = 0; jr < c.nref; ++jr) {
+            adj_pre<E, true>(w, T, jr, S, X);
+            wfft<E, false>(X, w.sb, w.tw, lane);
+            if (!adj_mid<E, true>(w, T, jr, X, Y)) continue;
+            wfft<E, true>(X, w.sb, w.tw, lane);
+          }
+          adj_post<E>(w, X, S);
+          w_store<E>(w, ST + (size_t)(z + 1) * nxg, S);
+          w_inject_rec<E>(w, S, s, bin, z + 1, bins);
+        }
+        put(S);
+      } else {
       if (!recv) {
 #pragma unroll
         for (int j = 0; j < E; ++j) X[j] = S[j];
@@ -1199,7 +1209,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
       if (!recv) {
         fwd_mid<E>(w, T, 0, X);
       } else {
-        adj_mid<E, false>(w, T, 0, X, Yd);
+        adj_mid<E, false>(w, T, 0, X, Y);
         if (reuse) {
           // filtered spectrum of T[z+1], every point (tap 0: N = nxg)
           float2* g = SG + (size_t)(z + 1) * nxg;
@@ -1222,6 +1232,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
         w_inject_rec<E>(w, S, s, bin, z + 1, bins);
       }
       put(S);
+      }  // one reference
     }
     cp_wait0();
     __syncthreads();
@@ -1252,7 +1263,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
     ring.issue(z - 2);
     cp_commit();
     if (act) {
-      const Tabs Tp = ring.stabs(z - 1);
+      const Tabs Tp = tabs_at(z - 1);
       const float2* bgp = SBG + (size_t)(z - 1) * nxg;
       const float2* tp = ST + (size_t)(z - 1) * nxg;
       if (z == nz) {
@@ -1288,9 +1299,32 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
         const bool on = recv ? (z < nz) : (k == 0 ? (z < nz && z >= 2) : (z >= 2 && (z < nz || keep_last)));
         if (!on) continue;
         const bool step = k == 0;
-        const Tabs T = (step && !recv) ? ring.stabs(z) : Tp;
+        const Tabs T = (step && !recv) ? tabs_at(z) : Tp;
         // pre
-        if (step) {
+        bool done = false;  // several references: the step ran whole here
+        if constexpr (MR) {
+          if (step) {
+            if (!recv) {
+              // bu: one forward transform, one inverse per reference,
+              // selected into bu (R bg added below)
+#pragma unroll
+              for (int j = 0; j < E; ++j) X[j] = S[j];
+              fwd_step_mr<E>(w, T, c.nref, X, S);
+            } else {
+              // q: the references' spectra summed, one inverse transform
+#pragma unroll 1
+              for (int jr = 0; jr < c.nref; ++jr) {
+                adj_pre<E, true>(w, T, jr, S, X);
+                wfft<E, false>(X, w.sb, w.tw, lane);
+                if (!adj_mid<E, true>(w, T, jr, X, Y)) continue;
+                wfft<E, true>(X, w.sb, w.tw, lane);
+              }
+            }
+            done = true;
+          }
+        }
+        if (done) {
+        } else if (step) {
           if (!recv) {
 #pragma unroll
             for (int j = 0; j < E; ++j) X[j] = S[j];
@@ -1317,7 +1351,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
             sc_pre<E>(w, T, scmode, S, X);
           }
         }
-        if (step || t1) {
+        if (!done && (step || t1)) {
           if (step || !reuse) {
             wfft<E, false>(X, w.sb, w.tw, lane);
             if (!step) {
@@ -1325,7 +1359,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
             } else if (!recv) {
               fwd_mid<E>(w, T, 0, X);
             } else {
-              adj_mid<E, false>(w, T, 0, X, Yd);
+              adj_mid<E, false>(w, T, 0, X, Y);
               if (reuse) sc_spec<E>(w, om, X, S);  // wd is spent
             }
           }
@@ -1333,12 +1367,12 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
         }
         // post: the depth's tables and rows again from a laundered depth
         const int zl = launder(z);
-        const Tabs Tq = ring.stabs(zl - 1);
+        const Tabs Tq = tabs_at(zl - 1);
         const float2* bgq = SBG + (size_t)(zl - 1) * nxg;
         const float2* tq = ST + (size_t)(zl - 1) * nxg;
         if (step) {
           if (!recv) {
-            fwd_post<E, false>(w, ring.stabs(zl), 0, X, S);
+            if constexpr (!MR) fwd_post<E, false>(w, ring.stabs(zl), 0, X, S);
 #pragma unroll
             for (int j = 0; j < E; ++j) {
               bool in;
@@ -1393,7 +1427,7 @@ __global__ void __launch_bounds__(2 * R * 32, 1) kw_born_adj2(DevCtx c, SlotLayo
 
 // Down sweep of the Born adjoint's receiver side alone, one warp per row,
 // for the FWI gradient, whose modelling pass has already stored the source
-// field bg of every depth (c.wem_store_bg): wu[0] = the injected data;
+// field bg of every depth (c.bg_store): wu[0] = the injected data;
 // T[z+1] = P^H_{z+1} wu (stored, with its filtered spectrum for the
 // scatter's spectral reuse), wu[z+1] = T[z+1] + the data injected at z + 1;
 // IR[z] = sum over the CTA's rows, in row order, of wu[z] conj(bg[z]).  The
@@ -1496,6 +1530,10 @@ __global__ void __launch_bounds__(R * 32, 2) kw_adj_down(DevCtx c, SlotLayout L,
 // rows per CTA of kw_born_adj2 (two warps per row: 16 warps at 128
 // registers; 8 rows measured faster than 6 rows at 168 registers)
 constexpr int kRowsAdj2 = 8;
+// rows per CTA of the several-reference two-warp Born adjoint: a warp's
+// rows (state, transform and the references' spectrum or sum) take up to
+// 255 registers, so 8 warps per SM
+constexpr int kRowsAdj2Mr = 4;
 // rows per CTA of the single-reference WEM kernel when its buffers fit
 // (16 warps at 128 registers)
 constexpr int kRowsWem = 16;
@@ -1506,6 +1544,7 @@ constexpr int kRowsWem = 16;
 inline int nbuf_of(int which) {
   switch (which) {
     case 8: return kRowsAdj2;
+    case 9: return 2 * kRowsAdj2Mr;
     case 3: return 2 * kRowsAdj2;
     case 7: return 2 * kRowsAdj2;
     case 4: return kRowsWem;
@@ -1517,7 +1556,7 @@ inline int nbuf_of(int which) {
 // the tables a pass reads: as WEM (0), Born forward (1) or Born adjoint (2)
 inline int tables_of(int which) {
   if (which == 8) return 3;  // the adjoint step alone: phase and split-step rows
-  return (which == 4 || which == 5 || which == 7) ? 0 : ((which == 3 || which == 6) ? 2 : which);
+  return (which == 4 || which == 5 || which == 7) ? 0 : ((which == 3 || which == 6 || which == 9) ? 2 : which);
 }
 // one-row CTAs leave the taper out of shared memory when the split-step table
 // carries it (SSF)
@@ -1585,6 +1624,13 @@ bool wem16_fits(const DevCtx& c) {
 
 // kw_born_adj2 serves this context: one reference, and its buffers, the
 // full ring and every table of a depth fit in shared memory
+// the several-reference two-warp form (pass 9): grouped CTAs, its buffers
+// in shared memory (the tables where the ring does not fit come from L2)
+template <int E>
+bool adj2mr_fits(const DevCtx& c) {
+  if (c.nref < 2 || c.one_row) return false;
+  return base_bytes<E>(c, 9) <= (size_t)max_smem_per_block();
+}
 template <int E>
 bool adj2_fits(const DevCtx& c) {
   if (c.nref != 1) return false;
@@ -1711,6 +1757,19 @@ void launch_adj_w(const DevCtx& c, const Group* g, int ng, float2* sBG, float2* 
     else go(kw_born_adj2<E, false, kRowsAdj2>);
     return;
   }
+  if (adj2mr_fits<E>(c)) {
+    // several references: the two chains of a row on two warps
+    const SlotLayout L9 = slot_layout<E>(c, 9, limit);
+    const size_t sm9 = smem_w<E>(c, 9, L9);
+    auto go = [&](auto kern) {
+      set_max_smem(kern);
+      kern<<<ng, 2 * kRowsAdj2Mr * 32, sm9, st>>>(c, L9, g, sBG, sT, nullptr, bins, ir, is, compat);
+      note_launch();
+    };
+    if (c.tap == 0) go(kw_born_adj2<E, true, kRowsAdj2Mr, true>);
+    else go(kw_born_adj2<E, false, kRowsAdj2Mr, true>);
+    return;
+  }
   const SlotLayout L = slot_layout<E>(c, 2, limit);
   const size_t sm = smem_w<E>(c, 2, L);
   auto go = [&](auto kern) {
@@ -1735,6 +1794,7 @@ bool adj_split_w(const DevCtx& c) {
 // rows per CTA the Born adjoint launcher expects
 template <int E>
 int adj_rows_w(const DevCtx& c) {
+  if (adj2mr_fits<E>(c)) return kRowsAdj2Mr;
   if (!adj2_fits<E>(c)) return kW;
   return c.one_row ? 1 : kRowsAdj2;
 }
