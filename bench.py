@@ -128,20 +128,20 @@ def workload(small=False, small_shots=8):
 # DRAM bytes (read + write) per (row, depth) of the gradient's passes, from
 # one ncu capture of the reduced case (16 shots x 21 frequencies, nz 300,
 # N 768; profiles/fwi_gradient_passes_e24_c3_small16.md; kernels of commit
-# 187d259): the traffic of a launch scales with the rows it carries, so a
+# ea1f67b): the traffic of a launch scales with the rows it carries, so a
 # full launch is this figure x rows x depths.  The Born adjoint pass of the
 # gradient is kw_adj_down + kw_born_adj2 (its up sweep), summed.
 TRAFFIC_PER_ROW_DEPTH = {
-    "k_born_adj": ((698917e3 + 1262201e3) + (1941243e3 + 78077e3)) / (336 * 300),
-    "k_wem": (692194e3 + 624966e3) / (336 * 300),
+    "k_born_adj": ((698904e3 + 1262595e3) + (1939387e3 + 77775e3)) / (336 * 300),
+    "k_wem": (735412e3 + 1244190e3) / (336 * 300),
 }
 # warp instructions per (row, depth) of the same passes (smsp__inst_executed
 # of the same capture): the pass kernels are bound by instruction issue, so
 # the line also reports the issue rate they reach against one warp
 # instruction per SM sub-partition per cycle
 INST_PER_ROW_DEPTH = {
-    "k_born_adj": (254522058 + 907077570) / (336 * 300),
-    "k_wem": 444057558 / (336 * 300),
+    "k_born_adj": (254521722 + 907278498) / (336 * 300),
+    "k_wem": 427428918 / (336 * 300),
 }
 
 
