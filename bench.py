@@ -515,7 +515,9 @@ def run_reference(args, rank, world):
     res, durs = [], []
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        r = cpu_sample(cfg, nshots=nshots) if i else first
+        # the sizing run counts as the first warm-up step; every timed step
+        # runs its own sample
+        r = first if (i == 0 and args.warmup > 0) else cpu_sample(cfg, nshots=nshots)
         if i >= args.warmup:
             res.append(r["value"])
             durs.append(time.perf_counter() - t0)
