@@ -28,14 +28,9 @@ __device__ __forceinline__ cdd csqrt(cdd a) {
   double im = sqrt(fmax(0.5 * (r - a.x), 0.0));
   return mk(re, a.y < 0 ? -im : im);
 }
-// principal power a^p for real p: |a|^p exp(i p arg a)
-__device__ __forceinline__ cdd cpow(cdd a, double p) {
-  double r = hypot(a.x, a.y), t = atan2(a.y, a.x);
-  double m = exp(p * log(r));
-  double s, c;
-  sincos(p * t, &s, &c);
-  return mk(m * c, m * s);
-}
+// The complex powers of the tables, exp(p Log a) on the principal branch,
+// are written algebraically (no FP64 logarithm, exponential or angle):
+// a^-2 = 1 / (a a) and a^(-1/2 - k) = (1 / csqrt(a)) (1 / a)^k.
 __device__ __forceinline__ float2 f2(cdd a) { return make_float2((float)a.x, (float)a.y); }
 
 // edge-extended pad along x (operator/src/Pad.h:77-96, extend = true)
@@ -228,9 +223,10 @@ __global__ void k_point_tables(int M, int nz, int nxg, int nref, int nt, double 
       if (sc) {
         const cdd su = mk(sp[i - nxg]);
         const cdd u = mul(d, csqrt(su)), w = mul(du, csqrt(s));
-        cdd v = cpow(add(u, w), -2.0);
-        cdd s1s2 = dvd(mul(du, d), v);
-        cdd r1r2 = dvd(mul(mk(2, 0), mul(su, s)), v);
+        // v = (u + w)^-2; dividing by v multiplies by (u + w)^2
+        const cdd uw = add(u, w), uw2 = mul(uw, uw);
+        cdd s1s2 = mul(mul(du, d), uw2);
+        cdd r1r2 = mul(mul(mk(2, 0), mul(su, s)), uw2);
         cdd cc = csqrt(dvd(s, su));
         va0 = mul(cc, s1s2);
         vb0 = mul(dvd(mk(1, 0), cc), s1s2);
@@ -245,8 +241,12 @@ __global__ void k_point_tables(int M, int nz, int nxg, int nref, int nt, double 
       a1[i] = f2(va1);
       b1[i] = f2(vb1);
       const cdd base = mk(s.x - eps * s.x, s.y);
-      for (int it = 0; it < nt; ++it)
-        sc[((size_t)m * nt + it) * plane + p] = f2(mul(mk(coef[it], 0), cpow(base, -0.5 - it)));
+      const cdd one = mk(1, 0), inv = dvd(one, base);
+      cdd pw = dvd(one, csqrt(base));  // base^(-1/2 - it)
+      for (int it = 0; it < nt; ++it) {
+        sc[((size_t)m * nt + it) * plane + p] = f2(mul(mk(coef[it], 0), pw));
+        pw = mul(pw, inv);
+      }
     }
   }
 }
