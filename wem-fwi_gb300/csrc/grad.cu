@@ -197,7 +197,7 @@ __global__ void k_exact_grad(DevCtx c, int nx, const float2* sp, const float2* d
 
 void launch_phase_grad_tables(const DevCtx& c, const float2* sref, float eps, float2* gam, cudaStream_t st) {
   const int nrow = c.nfreq * c.nz * c.nref;
-  const dim3 grid((c.N + 255) / 256, nrow < 65535 ? nrow : 65535);
+  const dim3 grid = table_grid((c.N + 255) / 256, nrow, 256);
   k_phase_grad<<<grid, 256, 0, st>>>(c, sref, eps, gam);
   note_launch();
 }

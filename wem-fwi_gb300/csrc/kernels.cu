@@ -6,6 +6,7 @@
 // (propagator/src/wem_prop.cpp:52-74, born_prop.cpp:75-113, 178-216); the
 // Born passes here use the linearity of the one-way operators to merge the
 // reference's seven one-way sweeps per row into two (see the pass comments).
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 
@@ -824,6 +825,16 @@ static size_t fft_bufs(const DevCtx& c, int rows, bool third) {
   return (third ? 3 : 2) * al((size_t)rows * c.N);
 }
 
+dim3 table_grid(int gx, int nrow, int threads) {
+  static const int sms = [] {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    return cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && n > 0 ? n : 152;
+  }();
+  const int want = std::max(1, 2 * sms * (2048 / threads) / std::max(gx, 1));
+  return dim3(gx, std::min(std::min(nrow, want), 65535));
+}
+
 size_t smem_wem(const DevCtx& c, int G) {
   return 8 * (al(c.N) + fft_bufs(c, G, c.nref > 1) + 2 * al((size_t)G * c.nxg));
 }
@@ -838,14 +849,14 @@ size_t smem_rows(const DevCtx& c, int G) { return 8 * (al(c.N) + fft_bufs(c, G, 
 
 void launch_phase_tables(const DevCtx& c, const float2* sref, float eps, float2* ph, cudaStream_t st) {
   const int nrow = c.nfreq * c.nz * c.nref;
-  const dim3 grid((c.N + 255) / 256, nrow < 65535 ? nrow : 65535);
+  const dim3 grid = table_grid((c.N + 255) / 256, nrow, 256);
   k_phase<<<grid, 256, 0, st>>>(c, sref, eps, ph);
   note_launch();
 }
 
 void launch_fac_tables(const DevCtx& c, const float2* q, float2* fac, cudaStream_t st) {
   const int nrow = c.nfreq * c.nz;
-  const dim3 grid((c.nxg + 127) / 128, nrow < 65535 ? nrow : 65535);
+  const dim3 grid = table_grid((c.nxg + 127) / 128, nrow, 128);
   k_fac<<<grid, 128, 0, st>>>(c, q, fac);
   note_launch();
 }

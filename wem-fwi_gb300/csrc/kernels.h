@@ -64,6 +64,10 @@ size_t smem_born_fwd(const DevCtx& c, int G);
 size_t smem_born_adj(const DevCtx& c, int G);
 size_t smem_rows(const DevCtx& c, int G);
 int max_smem_per_block();
+// grid of a table builder whose CTAs stride over nrow table rows (gx CTAs
+// across a row, `threads` per CTA): enough CTAs for two waves on every SM, so
+// each CTA walks many rows instead of the SMs scheduling one CTA per row
+dim3 table_grid(int gx, int nrow, int threads);
 // counts the library's kernel launches (wem_launch_count)
 void note_launch();
 long long launch_count();
