@@ -39,6 +39,7 @@ CASES = [
     ("coords", dict(cmap=0, prop="pspi", nref=2), ("wem", "born")),
     ("cmap_log", dict(cmap=1, prop="ssf", nref=1), ("wem", "born")),
     ("cmap_rot", dict(cmap=2, prop="pspi", nref=3), ("wem", "born")),
+    ("pspi4_t4", dict(prop="pspi", nref=4, ns=2, nx=44, tap=3, pad=2, ntaylor=4), ("wem", "born")),
 ]
 
 
