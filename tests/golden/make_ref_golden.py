@@ -40,13 +40,14 @@ CASES = [
     ("cmap_log", dict(cmap=1, prop="ssf", nref=1), ("wem", "born")),
     ("cmap_rot", dict(cmap=2, prop="pspi", nref=3), ("wem", "born")),
     ("pspi4_t4", dict(prop="pspi", nref=4, ns=2, nx=44, tap=3, pad=2, ntaylor=4), ("wem", "born")),
+    ("refl_tomo_ssf", dict(prop="ssf", nref=1, ns=2, nx=48, nz=14, tap=0, pad=0), ("refl", "tomo")),
 ]
 
 
 def make_case(kw):
     return cmap_case(**kw) if "cmap" in kw else small_case(**kw)
 # BornRefl and BornTomo spread the source over "ng" cells (ext_born_refl.cpp:18)
-EXTRA_PAR = {"ssf_tpad": dict(tpad=32), "refl_tomo": dict(ng=2)}
+EXTRA_PAR = {"ssf_tpad": dict(tpad=32), "refl_tomo": dict(ng=2), "refl_tomo_ssf": dict(ng=1)}
 
 
 def run_case(name, kw, ops, seed):

@@ -53,6 +53,11 @@ def load(name):
     kw = meta["case"]
     p0 = (cmap_case(**kw) if "cmap" in kw else small_case(**kw))[0]
     p = make_params(meta["par"], nx=p0.nx, nz=p0.nz, dx=p0.dx, dz=p0.dz, nt=p0.nt, dt=p0.dt)
+    if "refl" in meta["ops"] or "tomo" in meta["ops"]:
+        # BornRefl / BornTomo spread the source over "ng" cells
+        # (ext_born_refl.cpp:18); the library and the oracle take it in ngs,
+        # as the BornRefl / BornTomo classes of wemgpu.ops set it
+        p.ngs = int(meta["par"].get("ng", 0))
     return p, meta, {k: f[k] for k in f.files if k != "meta"}
 
 
