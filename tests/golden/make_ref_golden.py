@@ -41,6 +41,10 @@ CASES = [
     ("cmap_rot", dict(cmap=2, prop="pspi", nref=3), ("wem", "born")),
     ("pspi4_t4", dict(prop="pspi", nref=4, ns=2, nx=44, tap=3, pad=2, ntaylor=4), ("wem", "born")),
     ("refl_tomo_ssf", dict(prop="ssf", nref=1, ns=2, nx=48, nz=14, tap=0, pad=0), ("refl", "tomo")),
+    ("ssf_point_eps0", dict(prop="ssf", nref=1, ns=2, nx=40, nz=16, tap=0, pad=0, eps=0.0, ngs=0, ngr=0),
+     ("wem", "born")),
+    ("pspi3_t3_band", dict(prop="pspi", nref=3, ns=2, nx=45, nz=18, ntaylor=3, fmin=4.0, fmax=18.0),
+     ("wem", "born")),
 ]
 
 
