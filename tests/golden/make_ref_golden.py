@@ -45,13 +45,16 @@ CASES = [
      ("wem", "born")),
     ("pspi3_t3_band", dict(prop="pspi", nref=3, ns=2, nx=45, nz=18, ntaylor=3, fmin=4.0, fmax=18.0),
      ("wem", "born")),
+    ("pspi2_buried", dict(prop="pspi", nref=2, ns=2, nx=48, nz=20), ("wem", "born")),
 ]
 
 
 def make_case(kw):
     return cmap_case(**kw) if "cmap" in kw else small_case(**kw)
 # BornRefl and BornTomo spread the source over "ng" cells (ext_born_refl.cpp:18)
-EXTRA_PAR = {"ssf_tpad": dict(tpad=32), "refl_tomo": dict(ng=2), "refl_tomo_ssf": dict(ng=1)}
+EXTRA_PAR = {"ssf_tpad": dict(tpad=32), "refl_tomo": dict(ng=2), "refl_tomo_ssf": dict(ng=1),
+             # sources 3 and receivers 2 depth steps below the surface
+             "pspi2_buried": dict(osz=30.0, orz=20.0)}
 
 
 def run_case(name, kw, ops, seed):
