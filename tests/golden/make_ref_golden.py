@@ -46,6 +46,9 @@ CASES = [
     ("pspi3_t3_band", dict(prop="pspi", nref=3, ns=2, nx=45, nz=18, ntaylor=3, fmin=4.0, fmax=18.0),
      ("wem", "born")),
     ("pspi2_buried", dict(prop="pspi", nref=2, ns=2, nx=48, nz=20), ("wem", "born")),
+    # a prime trace length: the time <-> frequency step as a DFT over the bins
+    ("ssf_nt_prime", dict(prop="ssf", nref=1, ns=2, nz=16, nt=127), ("wem", "born")),
+    ("ext_pspi", dict(prop="pspi", nref=2, ns=2, nz=14, tap=3, pad=2), ("extwem", "extborn")),
 ]
 
 
