@@ -150,12 +150,36 @@ def c1_fixture():
     return dict(s=s, wem=d, born_adj_s=gs, born_adj_r=gr, meta=np.frombuffer(json.dumps(meta).encode(), np.uint8))
 
 
+def c3_fixture():
+    """Configuration c3's model and geometry (768 x 300: the 768-point warp
+    kernels of the benchmarked gradient) on its first shot and the band's 21
+    lowest frequencies (3-6 Hz): the reference's modelling, kept on every
+    8th receiver, and its Born adjoint (as coded) of its own data, slowness
+    part.  The model is not stored: the test rebuilds it from its seed and
+    checks it against the sums kept here."""
+    from wemgpu import synthetic as S
+    cfg = S.c3()
+    par = dict(cfg["par"], ns=1, fmax=6.0)
+    g = R.Grid(cfg["nx"], cfg["nz"], cfg["dx"], cfg["dz"], cfg["nt"], cfg["dt"])
+    s, rho, wav = cfg["slow"], cfg["rho"], cfg["wavelet"]
+    d = R.wem_forward(par, g, wav, s, rho)
+    gs, _ = R.born_adjoint(par, g, wav, s, rho, d)
+    meta = dict(name="c3_shot0_3to6hz", par=par, source="reference propagator/src compiled by oracle/ref/Makefile")
+    sums = np.array([np.sum(s.real, dtype=np.float64), np.sum(s.imag, dtype=np.float64),
+                     np.sum(np.abs(s), dtype=np.float64)])
+    return dict(s_sums=sums, wem_rx8=d[:, ::8, :], born_adj_s=gs,
+                meta=np.frombuffer(json.dumps(meta).encode(), np.uint8))
+
+
 def main():
     if not R.available():
         raise SystemExit(f"reference checkout not found at {R.ref_root()} (set WEM_REFERENCE)")
     R.build()
     path = os.path.join(HERE, "refc1.npz")
     np.savez_compressed(path, **c1_fixture())
+    print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
+    path = os.path.join(HERE, "refc3.npz")
+    np.savez_compressed(path, **c3_fixture())
     print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
     path = os.path.join(HERE, "refinterp.npz")
     np.savez_compressed(path, **interp_fixture(200))
