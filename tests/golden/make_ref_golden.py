@@ -171,12 +171,39 @@ def c3_fixture():
                 meta=np.frombuffer(json.dumps(meta).encode(), np.uint8))
 
 
+def c2_fixture():
+    """Configuration c2's model and geometry (1024 x 500, PSPI with four
+    references: the several-reference 1024-point warp kernels) on its first
+    shot and the band's lowest frequencies (2-3.5 Hz): the reference's
+    modelling and Born forward of c2's perturbation, kept on every 8th
+    receiver, and its Born adjoint (as coded) of its own modelled data,
+    slowness part on every 4th depth.  The model is rebuilt from its seed
+    by the test and checked against the sums kept here."""
+    from wemgpu import synthetic as S
+    cfg = S.c2()
+    par = dict(cfg["par"], ns=1, fmax=3.5)
+    g = R.Grid(cfg["nx"], cfg["nz"], cfg["dx"], cfg["dz"], cfg["nt"], cfg["dt"])
+    s, rho, wav = cfg["slow"], cfg["rho"], cfg["wavelet"]
+    d = R.wem_forward(par, g, wav, s, rho)
+    b = R.born_forward(par, g, wav, s, rho, cfg["dslow"], cfg["drho"])
+    gs, _ = R.born_adjoint(par, g, wav, s, rho, d)
+    meta = dict(name="c2_shot0_2to3.5hz", par=par,
+                source="reference propagator/src compiled by oracle/ref/Makefile")
+    sums = np.array([np.sum(s.real, dtype=np.float64), np.sum(s.imag, dtype=np.float64),
+                     np.sum(np.abs(cfg["dslow"]), dtype=np.float64)])
+    return dict(sums=sums, wem_rx8=d[:, ::8, :], born_fwd_rx8=b[:, ::8, :], born_adj_s_z4=gs[::4],
+                meta=np.frombuffer(json.dumps(meta).encode(), np.uint8))
+
+
 def main():
     if not R.available():
         raise SystemExit(f"reference checkout not found at {R.ref_root()} (set WEM_REFERENCE)")
     R.build()
     path = os.path.join(HERE, "refc1.npz")
     np.savez_compressed(path, **c1_fixture())
+    print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
+    path = os.path.join(HERE, "refc2.npz")
+    np.savez_compressed(path, **c2_fixture())
     print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
     path = os.path.join(HERE, "refc3.npz")
     np.savez_compressed(path, **c3_fixture())

@@ -373,8 +373,23 @@ def test_c3_oracle_matches_reference_run(oracle):
     assert rel_l2(a0, F["born_adj_s"]) < TOL_ORACLE, rel_l2(a0, F["born_adj_s"])
 
 
+@pytest.fixture
+def row_ctas(gpu_lib, request):
+    """1: rows of a frequency grouped in CTAs (the kernels the benchmarks
+    run); 2: one row per CTA (what a pass with no more rows than SMs gets by
+    default, as one shot has)."""
+    from wemgpu import _lib
+    _lib.call("wem_set_row_ctas", request.param)
+    yield request.param
+    _lib.call("wem_set_row_ctas", 0)
+
+
+ROWS = [pytest.param(1, id="grouped"), pytest.param(2, id="onerow")]
+
+
 @pytest.mark.gpu
-def test_gpu_c3_matches_reference_run(gpu_lib, oracle):
+@pytest.mark.parametrize("row_ctas", ROWS, indirect=True)
+def test_gpu_c3_matches_reference_run(row_ctas, oracle):
     """c3's geometry on the GPU (the 768-point warp kernels of the benchmarked
     gradient) against the reference's own outputs: the modelling, and the
     Born adjoint (as coded) of the modelled data.  The reference's fp32
@@ -394,3 +409,63 @@ def test_gpu_c3_matches_reference_run(gpu_lib, oracle):
     e_ref = rel_l2(F["born_adj_s"], ex)
     assert rel_l2(a0, F["born_adj_s"]) < max(TOL_GPU, 2 * e_ref), (rel_l2(a0, F["born_adj_s"]), e_ref)
     assert rel_l2(a0, ex) < TOL_GPU, rel_l2(a0, ex)
+
+
+def _c2():
+    """c2's first shot, 2-3.5 Hz (nine frequencies), and the reference's
+    outputs for it: modelling and Born forward on every 8th receiver, the
+    Born adjoint's slowness part on every 4th depth."""
+    from wemgpu import synthetic as S
+    cfg = S.c2()
+    f = np.load(os.path.join(HERE, "golden", "refc2.npz"))
+    F = {k: f[k] for k in f.files if k != "meta"}
+    par = json.loads(bytes(f["meta"]).decode())["par"]
+    p = make_params(par, nx=cfg["nx"], nz=cfg["nz"], dx=cfg["dx"], dz=cfg["dz"], nt=cfg["nt"], dt=cfg["dt"])
+    s = cfg["slow"]
+    sums = [np.sum(s.real, dtype=np.float64), np.sum(s.imag, dtype=np.float64),
+            np.sum(np.abs(cfg["dslow"]), dtype=np.float64)]
+    assert np.array_equal(np.array(sums), F["sums"]), "the seeded c2 model differs from the fixture's"
+    return cfg, p, F
+
+
+def test_c2_oracle_matches_reference_run(oracle):
+    """c2's geometry (1024 x 500, PSPI with four references) on one shot:
+    the oracle's modelling, Born forward and Born adjoint (of its own data,
+    1e-5 from the reference's) against the reference's."""
+    cfg, p, F = _c2()
+    s, rho, wav = cfg["slow"], cfg["rho"], cfg["wavelet"]
+    d = oracle.wem_forward(p, wav, s, rho, kind=WEM_DATA_TIME, prec=32)
+    assert rel_l2(d[:, ::8], F["wem_rx8"]) < TOL_ORACLE, rel_l2(d[:, ::8], F["wem_rx8"])
+    b = oracle.born_forward(p, wav, s, rho, cfg["dslow"], cfg["drho"], kind=WEM_DATA_TIME, prec=32)
+    assert rel_l2(b[:, ::8], F["born_fwd_rx8"]) < TOL_ORACLE, rel_l2(b[:, ::8], F["born_fwd_rx8"])
+    a0, _ = oracle.born_adjoint(p, wav, s, rho, d, kind=WEM_DATA_TIME, prec=32)
+    assert rel_l2(a0[::4], F["born_adj_s_z4"]) < TOL_ORACLE, rel_l2(a0[::4], F["born_adj_s_z4"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("row_ctas", ROWS, indirect=True)
+def test_gpu_c2_matches_reference_run(row_ctas, oracle):
+    """c2's geometry on the GPU (the several-reference 1024-point warp
+    kernels) against the reference's own outputs.  The reference's fp32 Born
+    forward is 1.8e-4 from the fp64 oracle's, so it is held as the fixtures
+    are: within twice the reference's own error of the reference run and
+    within 1e-4 of the fp64 oracle."""
+    from wemgpu.core import BornOp, WemOp
+    cfg, p, F = _c2()
+    s, rho, wav = cfg["slow"], cfg["rho"], cfg["wavelet"]
+    d = np.zeros((p.ns, p.nr, p.nt), np.float32)
+    WemOp(p, wav).forward(s, rho, d)
+    assert rel_l2(d[:, ::8], F["wem_rx8"]) < TOL_GPU, rel_l2(d[:, ::8], F["wem_rx8"])
+    op = BornOp(p, wav, s, rho)
+    b = np.zeros_like(d)
+    op.forward(cfg["dslow"], cfg["drho"], b)
+    bx = oracle.born_forward(p, wav, s, rho, cfg["dslow"], cfg["drho"], kind=WEM_DATA_TIME, prec=64)
+    e_ref = rel_l2(F["born_fwd_rx8"], bx[:, ::8])
+    assert rel_l2(b[:, ::8], F["born_fwd_rx8"]) < max(TOL_GPU, 2 * e_ref), (rel_l2(b[:, ::8], F["born_fwd_rx8"]), e_ref)
+    assert rel_l2(b, bx) < TOL_GPU, rel_l2(b, bx)
+    a0, a1 = np.zeros_like(s), np.zeros_like(s)
+    op.adjoint(a0, a1, d)
+    ax, _ = oracle.born_adjoint(p, wav, s, rho, d, kind=WEM_DATA_TIME, prec=64)
+    e_ref = rel_l2(F["born_adj_s_z4"], ax[::4])
+    assert rel_l2(a0[::4], F["born_adj_s_z4"]) < max(TOL_GPU, 2 * e_ref), (rel_l2(a0[::4], F["born_adj_s_z4"]), e_ref)
+    assert rel_l2(a0, ax) < TOL_GPU, rel_l2(a0, ax)
