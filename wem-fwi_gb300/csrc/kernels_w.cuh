@@ -361,8 +361,6 @@ __device__ __forceinline__ void sc_mid(const WRow& w, float om, float2 (&X)[E]) 
     X[j] = c_scale(X[j], k * k * s);
   }
 }
-// post, one point: i w dz (c_0 u + c_1 filtered) with the mode's conjugations;
-// x is the filtered value (ignored when ntaylor = 0)
 // (k / omega)^2 X: the filtered spectrum of a row whose transform is X / N
 // away (the inverse transform and the filter's forward one cancel when no
 // point is masked between them)
@@ -375,10 +373,15 @@ __device__ __forceinline__ void sc_spec(const WRow& w, float om, const float2 (&
     Y[j] = c_scale(X[j], k * k * s);
   }
 }
+// post, one point: i w dz (c_0 u + c_1 filtered) with the mode's conjugations;
+// x is the filtered value (ignored when ntaylor = 0).  iw = (0, +-w dz)
+// (sc_iw): the product by it is the scaled swap, two multiplies (the
+// complex product's fused terms with the zero real part give the same
+// values, up to the sign of a zero)
 __device__ __forceinline__ float2 sc_val(float2 iw, int mode, bool t1, float2 k0, float2 k1, float2 u, float2 x) {
   float2 y = mode == 0 ? c_mul(k0, u) : c_mulc(u, k0);
   if (t1) y = c_add(y, mode == 0 ? c_mul(k1, x) : (mode == 1 ? c_mulc(x, k1) : x));
-  return c_mul(iw, y);
+  return make_float2(-__fmul_rn(iw.y, y.y), __fmul_rn(iw.y, y.x));
 }
 __device__ __forceinline__ float2 sc_iw(const DevCtx& c, float om, int mode) {
   const float wdz = om * c.dz;
