@@ -128,19 +128,19 @@ def workload(small=False, small_shots=8):
 # DRAM bytes (read + write) per (row, depth) of the gradient's passes, from
 # one ncu capture of the reduced case (16 shots x 21 frequencies, nz 300,
 # N 768; profiles/fwi_gradient_passes_e24_c3_small16.md; kernels of commit
-# ea1f67b): the traffic of a launch scales with the rows it carries, so a
+# 29b9584): the traffic of a launch scales with the rows it carries, so a
 # full launch is this figure x rows x depths.  The Born adjoint pass of the
 # gradient is kw_adj_down + kw_born_adj2 (its up sweep), summed.
 TRAFFIC_PER_ROW_DEPTH = {
-    "k_born_adj": ((698904e3 + 1262595e3) + (1939387e3 + 77775e3)) / (336 * 300),
-    "k_wem": (735412e3 + 1244190e3) / (336 * 300),
+    "k_born_adj": ((699063808 + 1258508288) + (1939322112 + 74323200)) / (336 * 300),
+    "k_wem": (735724288 + 1240831488) / (336 * 300),
 }
 # warp instructions per (row, depth) of the same passes (smsp__inst_executed
 # of the same capture): the pass kernels are bound by instruction issue, so
 # the line also reports the issue rate they reach against one warp
 # instruction per SM sub-partition per cycle
 INST_PER_ROW_DEPTH = {
-    "k_born_adj": (254521722 + 907278498) / (336 * 300),
+    "k_born_adj": (254521722 + 897649314) / (336 * 300),
     "k_wem": 427428918 / (336 * 300),
 }
 
