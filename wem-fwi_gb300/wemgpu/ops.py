@@ -220,8 +220,30 @@ class BornRefl(Propagator):
         self.wave, self.par, self.domain, self.range = wave, par, model, data
         self.params = _refl_params(par, slowness.getHyper(), wave, data)
         self.cppMode = core.BornReflOp(self.params, wave.getNdArray(), slowness.getNdArray())
+        self.prec = None
+        self.pad = None
+
+    def add_prec(self, op):
+        """The background passes through op.forward first (WEM.py:101-103):
+        a coarse model and its interpolator (LanczosInterpolation2D,
+        Spline2D)."""
+        self.prec = op
+        self.big_model = op.range.clone()
+
+    def add_pad(self, op):
+        """Then through op.forward (WEM.py:104-106): BornRefl propagates on
+        the grid it is given, so a padding operator extends the slowness."""
+        self.pad = op
+        self.pad_model = op.range.clone()
 
     def set_background(self, slow):
+        # WEM.py:108-115: preconditioner, then pad, then the background
+        if self.prec is not None:
+            self.prec.forward(False, slow, self.big_model)
+            slow = self.big_model
+        if self.pad is not None:
+            self.pad.forward(False, slow, self.pad_model)
+            slow = self.pad_model
         self.cppMode.set_background(slow.getNdArray())
 
     def forward(self, add, model, data):
@@ -242,8 +264,18 @@ class BornTomo(Propagator):
         self.wave, self.par, self.domain, self.range = wave, par, model, data
         self.params = _refl_params(par, model.getHyper(), wave, data)
         self.cppMode = core.BornTomoOp(self.params, wave.getNdArray(), model.getNdArray())
+        self.pad = None
+
+    def add_pad(self, op):
+        """The reflectivity passes through op.forward before it is set
+        (WEM.py:123-131)."""
+        self.pad = op
+        self.pad_refl = op.range.clone()
 
     def setBgRefl(self, refl):
+        if self.pad is not None:
+            self.pad.forward(False, refl, self.pad_refl)
+            refl = self.pad_refl
         self.cppMode.set_refl(refl.getNdArray())
 
     def set_background(self, slow):
