@@ -436,6 +436,17 @@ int wem_ic(const void* bg, int n, int adj, const void* in, void* out, int add);
  * dz, with p->eps and p->phase_law; the adjoint takes the conjugate factor. */
 int wem_phshift(const wem_params* p, int n, float dx, float dz, float freq, float s_re,
                 float s_im, int adj, const void* in, void* out, int nrow, int add);
+/* Injection (Injection.h:19-65, Injection.cpp:8-33, 52-75; py_wem_ops.cpp:181-198):
+ * npt points (iz[i], ix[i]) of a row set data [nz][nx] (complex), each
+ * spread over ix[i] + tap + [-ng, ng] with the cos^2 window, within the
+ * row.  The model is complex [nt] (nshot = 0: every point takes
+ * model[step]) or [nshot][npt][nt] (point i takes model[shot][i][step]).
+ * Forward: data = (or += with add) the spread values; adjoint: model
+ * (+)= the gathered values, the whole model cleared first unless add, as
+ * the reference.  Depth indices outside [0, nz) are rejected (the
+ * reference would write outside the rows); host or device pointers. */
+int wem_inject(const int* iz, const int* ix, int npt, int ng, int tap, int nx, int nz, int nt, int nshot,
+               int step, int shot, int adj, void* model, void* data, int add);
 /* Reflect (Reflect.h:12-48) of the grid (slow2, rho) [nz][nx]: out = r in,
  * adjoint conj(r) in; assigned, as the reference's (no add). */
 int wem_reflect(const void* slow2, const void* rho, int nx, int nz, int adj, const void* in,

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "BornFull.h"
+#include "Injection.h"
 #include "LanczosInterpolation2D.h"
 #include "Spline2D.h"
 #include "BornRefl.h"
@@ -255,6 +256,39 @@ int ref_interp2d(int kind, int adj, int mn1, float md1, int mn2, float md2, int 
       std::memcpy(m->getVals(), model, nm);
       op->forward(m, d, false);
       std::memcpy(data, d->getVals(), nd);
+    }
+  });
+}
+
+// Injection (propagator/src/Injection.h:19-65, Injection.cpp:8-33, 52-75)
+// between a model [nt] (nshot = 0) or [nshot][npt][nt] and rows [nz][nx]:
+// forward reads model and writes data, adjoint the reverse (neither adds)
+int ref_inject(const int* iz, const int* ix, int npt, int ng, int tap, int nx, int nz, int nt, int nshot, int step,
+               int shot, int adj, float* model, float* data) {
+  return guarded([&] {
+    Injection op(std::vector<int>(iz, iz + npt), std::vector<int>(ix, ix + npt), ng, tap);
+    op.setStep(step);
+    op.setShot(shot);
+    auto d = std::make_shared<complex2DReg>(std::make_shared<hypercube>(axis(nx, 0.f, 1.f), axis(nz, 0.f, 1.f)));
+    const size_t nd = sizeof(std::complex<float>) * (size_t)nx * nz;
+    auto run = [&](auto m, size_t nm) {
+      if (adj) {
+        std::memcpy(d->getVals(), data, nd);
+        op.adjoint(m, d, false);
+        std::memcpy(model, m->getVals(), nm);
+      } else {
+        std::memcpy(m->getVals(), model, nm);
+        op.forward(m, d, false);
+        std::memcpy(data, d->getVals(), nd);
+      }
+    };
+    if (nshot == 0) {
+      run(std::make_shared<complex1DReg>(std::make_shared<hypercube>(axis(nt, 0.f, 1.f))),
+          sizeof(std::complex<float>) * (size_t)nt);
+    } else {
+      run(std::make_shared<complex3DReg>(
+              std::make_shared<hypercube>(axis(nt, 0.f, 1.f), axis(npt, 0.f, 1.f), axis(nshot, 0.f, 1.f))),
+          sizeof(std::complex<float>) * (size_t)nshot * npt * nt);
     }
   });
 }

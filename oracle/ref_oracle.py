@@ -258,3 +258,23 @@ def interp2d(kind, model_axes, data_axes, p0, p1, x, adj=False):
           ctypes.c_float(md2), dn1, ctypes.c_float(dd1), dn2, ctypes.c_float(dd2), ctypes.c_float(p0),
           ctypes.c_float(p1), _p(m), _p(d))
     return m if adj else d
+
+
+def inject(iz, ix, ng, tap, nz, nx, step, shot, x, adj=False, nt=None, nshot=0):
+    """Injection (propagator/src/Injection.cpp:8-33, 52-75): forward maps a
+    model [nt] (nshot = 0) or [nshot][npt][nt] to rows [nz][nx], adjoint the
+    reverse (nt, nshot: the model's sizes, needed for the adjoint)."""
+    izs = np.ascontiguousarray(np.asarray(iz, np.int32))
+    ixs = np.ascontiguousarray(np.asarray(ix, np.int32))
+    npt = int(izs.size)
+    if adj:
+        d = _c64(x)
+        m = np.zeros((nshot, npt, nt) if nshot else (nt,), np.complex64)
+    else:
+        m = _c64(x)
+        nt = int(m.shape[-1])
+        nshot = int(m.shape[0]) if m.ndim == 3 else 0
+        d = np.zeros((nz, nx), np.complex64)
+    _call("ref_inject", _p(izs), _p(ixs), npt, int(ng), int(tap), int(nx), int(nz), int(nt), int(nshot), int(step),
+          int(shot), int(adj), _p(m), _p(d))
+    return m if adj else d

@@ -135,6 +135,36 @@ def interp_fixture(seed):
     return out
 
 
+# point Injection (propagator/src/Injection.cpp): (name, nz, nx, npt, ng, tap,
+# nt, nshot); the points' depths and positions are seeded, some outside the
+# row so that the window's bounds check is exercised
+INJECT = [
+    ("line_ng1_tap1", 6, 50, 30, 1, 1, 24, 0),
+    ("scatter_ng3", 5, 41, 17, 3, 2, 12, 0),
+    ("shots_ng0", 4, 36, 20, 0, 0, 10, 3),
+    ("shots_ng2_tap3", 7, 45, 14, 2, 3, 9, 4),
+]
+
+
+def inject_fixture(seed):
+    rng = np.random.default_rng(seed)
+    out, cases = {}, []
+    for name, nz, nx, npt, ng, tap, nt, nshot in INJECT:
+        iz = rng.integers(0, nz, npt).astype(np.int32)
+        ix = rng.integers(-ng - tap - 2, nx + 2, npt).astype(np.int32)
+        step, shot = int(rng.integers(0, nt)), int(rng.integers(0, max(nshot, 1)))
+        m = rand_c(rng, (nshot, npt, nt) if nshot else (nt,))
+        d = rand_c(rng, (nz, nx))
+        out[name + "_iz"], out[name + "_ix"] = iz, ix
+        out[name + "_m"], out[name + "_d"] = m, d
+        out[name + "_fwd"] = R.inject(iz, ix, ng, tap, nz, nx, step, shot, m)
+        out[name + "_adj"] = R.inject(iz, ix, ng, tap, nz, nx, step, shot, d, adj=True, nt=nt, nshot=nshot)
+        cases.append(dict(name=name, nz=nz, nx=nx, ng=ng, tap=tap, nt=nt, nshot=nshot, step=step, shot=shot))
+    meta = dict(cases=cases, source="reference propagator/src/Injection.cpp compiled by oracle/ref/Makefile")
+    out["meta"] = np.frombuffer(json.dumps(meta).encode(), np.uint8)
+    return out
+
+
 def c1_fixture():
     """Configuration c1 at full size (256 x 200, one shot, 64 frequencies,
     SSF): the reference's modelling of the seeded model and its Born adjoint
@@ -207,6 +237,9 @@ def main():
     print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
     path = os.path.join(HERE, "refc3.npz")
     np.savez_compressed(path, **c3_fixture())
+    print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
+    path = os.path.join(HERE, "refinject.npz")
+    np.savez_compressed(path, **inject_fixture(300))
     print(f"{path}: {os.path.getsize(path) / 1024:.0f} KB")
     path = os.path.join(HERE, "refinterp.npz")
     np.savez_compressed(path, **interp_fixture(200))

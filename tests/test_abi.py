@@ -71,3 +71,23 @@ def test_launch_shape_knobs_validate_on_host(lib, fn, bad):
         call(fn, bad)
     assert e.value.code == 1  # WEM_EINVAL
     call(fn, 1 if fn == "wem_set_gradient_split" else 0)  # the default is always accepted
+
+
+@pytest.mark.parametrize("bad", ["depth", "step", "shot", "window"])
+def test_injection_arguments_validate_on_host(lib, bad):
+    """wem_inject rejects a point below the rows (the reference would write
+    outside them), a time sample or shot outside the model and a negative
+    window before any device work."""
+    from wemgpu._lib import WemError, call
+    iz = np.array([0, 9 if bad == "depth" else 2], np.int32)
+    ix = np.array([1, 3], np.int32)
+    nz, nx, nt, nshot = 4, 8, 5, 2
+    step = nt if bad == "step" else 1
+    shot = nshot if bad == "shot" else 0
+    ng = -1 if bad == "window" else 1
+    m = np.zeros((nshot, 2, nt), np.complex64)
+    d = np.zeros((nz, nx), np.complex64)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    with pytest.raises(WemError) as e:
+        call("wem_inject", p(iz), p(ix), 2, ng, 0, nx, nz, nt, nshot, step, shot, 0, p(m), p(d), 0)
+    assert e.value.code == 1  # WEM_EINVAL

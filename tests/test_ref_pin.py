@@ -284,6 +284,39 @@ def test_gpu_interp_matches_reference_run(gpu_lib):
         assert rel_l2(m, F[n + "_adj"]) < 1e-5, n
 
 
+# ------------------------------------------------------------ Injection
+def test_injection_oracle_matches_reference_run():
+    """The numpy restatement of Injection (oracle/injection.py) against the
+    reference's own class on the golden cases, bit for bit."""
+    from oracle import injection as J
+    f = np.load(os.path.join(HERE, "golden", "refinject.npz"))
+    for c in json.loads(bytes(f["meta"]).decode())["cases"]:
+        n = c["name"]
+        iz, ix = f[n + "_iz"].tolist(), f[n + "_ix"].tolist()
+        args = (iz, ix, c["ng"], c["tap"], c["nz"], c["nx"], c["step"], c["shot"])
+        assert np.array_equal(J.forward(*args, f[n + "_m"]), f[n + "_fwd"]), n
+        assert np.array_equal(J.adjoint(*args, f[n + "_d"], c["nt"], c["nshot"]), f[n + "_adj"]), n
+
+
+def test_live_reference_injection_matches_oracle():
+    """The reference's Injection on its own unit-test set-ups
+    (propagator/test/test_wem_ops.py:86-122) against the restatement."""
+    R = _ref()
+    from oracle import injection as J
+    rng = np.random.default_rng(9)
+    x = np.linspace(0, 100, 200).astype(int).tolist()
+    m = rand_c(rng, (100,))
+    assert np.array_equal(R.inject([0] * 200, x, 1, 1, 100, 200, 20, 0, m),
+                          J.forward([0] * 200, x, 1, 1, 100, 200, 20, 0, m))
+    d = rand_c(rng, (100, 200))
+    assert np.array_equal(R.inject([0] * 200, x, 1, 1, 100, 200, 20, 0, d, adj=True, nt=100),
+                          J.adjoint([0] * 200, x, 1, 1, 100, 200, 20, 0, d, 100))
+    x = np.linspace(0, 199, 100).astype(int).tolist()
+    m = rand_c(rng, (50, 100, 100))
+    assert np.array_equal(R.inject([0] * 100, x, 0, 0, 200, 200, 20, 20, m),
+                          J.forward([0] * 100, x, 0, 0, 200, 200, 20, 20, m))
+
+
 # ------------------------------------------------ benchmark configurations
 def _c1():
     from wemgpu import synthetic as S

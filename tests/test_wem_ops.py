@@ -208,3 +208,63 @@ def test_phshift_dot_reference_setup(gpu_lib):
     op = wem.Phshift(row, row.clone(), h, 5.0, 5, 0.002, 0)
     assert max(op.dotTest()) <= 1e-5
 
+
+def _inject_cases():
+    import json
+    import os
+    f = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "refinject.npz"))
+    return json.loads(bytes(f["meta"]).decode())["cases"], {k: f[k] for k in f.files if k != "meta"}
+
+
+def _cvec(a):
+    from wemgpu.vector import Hypercube, Vector
+    return Vector(Hypercube(ns=list(reversed(a.shape))), np.ascontiguousarray(a, np.complex64), storage="dataComplex")
+
+
+@pytest.mark.gpu
+def test_injection_matches_reference_run(gpu_lib):
+    """wem_ops.Injection against the reference's own Injection
+    (Injection.cpp:8-33, 52-75; tests/golden/refinject.npz): forward,
+    adjoint (which clears the whole model unless adding) and the add
+    forms.  The roundings are the reference's; only the order of the sums
+    may differ, so 1e-6."""
+    from wemgpu import wem_ops as wem
+    cases, F = _inject_cases()
+    for c in cases:
+        n, nz, nx = c["name"], c["nz"], c["nx"]
+        m, d = F[n + "_m"], F[n + "_d"]
+        mv, dv = _cvec(m), _cvec(np.zeros((nz, nx), np.complex64))
+        op = wem.Injection(mv, dv, F[n + "_iz"].tolist(), F[n + "_ix"].tolist(), ng=c["ng"], tap=c["tap"])
+        op.setStep(c["step"])
+        op.setShot(c["shot"])
+        dv.getNdArray()[:] = 3.0
+        op.forward(False, mv, dv)
+        assert rel_l2(dv.getNdArray(), F[n + "_fwd"]) < 1e-6, n
+        op.forward(True, mv, dv)
+        assert rel_l2(dv.getNdArray(), 2 * F[n + "_fwd"]) < 1e-6, n
+        ma = _cvec(np.full(m.shape, 5.0 + 1j, np.complex64))
+        op.adjoint(False, ma, _cvec(d))
+        assert rel_l2(ma.getNdArray(), F[n + "_adj"]) < 1e-6, n
+        op.adjoint(True, ma, _cvec(d))
+        assert rel_l2(ma.getNdArray(), 2 * F[n + "_adj"]) < 1e-6, n
+
+
+@pytest.mark.gpu
+def test_injection_reference_dot_tests(gpu_lib):
+    """The reference's two Injection dot tests (test_wem_ops.py:86-122):
+    a trace [100] onto rows [100][200] along a line of 200 points (ng 1,
+    tap 1, step 20), and shots x receivers x time [50][100][100] onto rows
+    [200][200] (ng 0, step 20, shot 20)."""
+    from wemgpu import wem_ops as wem
+    x = np.linspace(0, 200 / 2, 200).astype(int).tolist()
+    op = wem.Injection(_cvec(np.zeros(100, np.complex64)), _cvec(np.zeros((100, 200), np.complex64)),
+                       [0] * 200, x, ng=1, tap=1)
+    op.setStep(20)
+    assert max(op.dotTest()) <= 1e-5
+    x = np.linspace(0, 200 - 1, 100).astype(int).tolist()
+    op = wem.Injection(_cvec(np.zeros((50, 100, 100), np.complex64)), _cvec(np.zeros((200, 200), np.complex64)),
+                       [0] * 100, x, ng=0, tap=0)
+    op.setStep(20)
+    op.setShot(20)
+    assert max(op.dotTest()) <= 1e-5
+

@@ -2616,6 +2616,55 @@ struct ReflTables {
   }
 };
 
+// Injection.h:53-65: the cos^2 window in the reference's float arithmetic
+static std::vector<float> inject_window(int ng) {
+  std::vector<float> g(2 * ng + 1, 1.f);
+  if (ng == 0) return g;
+  const float pi = (float)(4 * std::atan(1.));
+  const int sz = 2 * ng + 1;
+  for (int i = 0; i < sz / 2; ++i) g[i] = (-std::cos(pi / ng * i) + 1) / 2;
+  for (int i = sz / 2; i < sz; ++i) g[i] = (std::cos(pi / ng * (i - sz + ng + 1)) + 1) / 2;
+  return g;
+}
+
+int wem_inject(const int* iz, const int* ix, int npt, int ng, int tap, int nx, int nz, int nt, int nshot, int step,
+               int shot, int adj, void* model, void* data, int add) {
+  return guard([&] {
+    require(model && data && model != data && npt >= 0 && (npt == 0 || (iz && ix)), "bad arguments");
+    require(nx > 0 && nz > 0 && nt > 0 && ng >= 0 && nshot >= 0, "bad sizes");
+    require(step >= 0 && step < nt, "step outside the model's time axis");
+    require(nshot == 0 || (shot >= 0 && shot < nshot), "shot outside the model's shot axis");
+    for (int i = 0; i < npt; ++i) require(iz[i] >= 0 && iz[i] < nz, "a point's depth index is outside the rows");
+    Buf gb, zb, xb;
+    const float* g = upload(gb, inject_window(ng));
+    const int* zd = upload(zb, std::vector<int>(iz, iz + npt));
+    const int* xd = upload(xb, std::vector<int>(ix, ix + npt));
+    // the 1D model [nt] gives every point model[step]; the 3D one
+    // [nshot][npt][nt] gives point i model[shot][i][step]
+    const size_t msize = (size_t)(nshot ? (size_t)nshot * npt : 1) * nt * 8, dsize = (size_t)nz * nx * 8;
+    const size_t off0 = nshot ? ((size_t)shot * npt) * nt + step : (size_t)step;
+    const size_t stride = nshot ? (size_t)nt : 0;
+    Staged sm, sd;
+    if (!adj) {
+      sm.in(model, msize);
+      sd.out(data, dsize, add != 0);
+      launch_inject(zd, xd, npt, g, ng, tap, nx, nz, 0, (float2*)sm.dev, off0, stride, (float2*)sd.dev, add, 0);
+      cuda_check(cudaGetLastError(), "inject kernel");
+      cuda_check(cudaStreamSynchronize(0), "inject");
+      sd.finish(data);
+    } else {
+      sd.in(data, dsize);
+      sm.out(model, msize, add != 0);
+      // the reference clears the whole model unless adding (Injection.cpp:22,65)
+      if (!add) cuda_check(cudaMemsetAsync(sm.dev, 0, msize, 0), "memset");
+      launch_inject(zd, xd, npt, g, ng, tap, nx, nz, 1, (float2*)sm.dev, off0, stride, (float2*)sd.dev, add, 0);
+      cuda_check(cudaGetLastError(), "inject kernel");
+      cuda_check(cudaStreamSynchronize(0), "inject");
+      sm.finish(model);
+    }
+  });
+}
+
 int wem_reflect(const void* slow2, const void* rho, int nx, int nz, int adj, const void* in, void* out) {
   return guard([&] {
     require(in && out, "NULL argument");

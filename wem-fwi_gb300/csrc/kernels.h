@@ -367,6 +367,12 @@ void launch_scale_add(float2* y, const float2* x, size_t n, cudaStream_t st);
 // out[r][k] = f[k] in[r][k] (conj(f) with conj), added with add
 void launch_diag_rows(const float2* in, const float2* f, float2* out, int n, int nrow, int conj, int add,
                       cudaStream_t st);
+// Injection (Injection.cpp:8-33, 52-75) between point values m_i =
+// model[off0 + i stride] (stride 0: one sample for every point) and a
+// [nz][nx] row set, cos^2 window g[2 ng + 1], points (iz[i], ix[i] + tap);
+// forward assigns or adds data, the adjoint adds into model
+void launch_inject(const int* iz, const int* ix, int npt, const float* g, int ng, int tap, int nx, int nz, int adj,
+                   float2* model, size_t off0, size_t stride, float2* data, int add, cudaStream_t st);
 // SplitStep at the points loc[0..nloc) of rows of nx points (srow: the
 // slowness^2 row of the depth); the other points are not touched
 void launch_splitstep(const float2* srow, const int* loc, int nloc, int nx, int nrow, double wdz, double sr,

@@ -1,6 +1,6 @@
 // Element-wise operators of the row-level API (include/wemgpu.h, wem_*
 // and wemop_* per-operator entry points), the GPU side of the reference's
-// py_wem_ops classes IC, Phshift, SplitStep and Reflect
+// py_wem_ops classes IC, Phshift, SplitStep, Reflect and Injection
 // (propagator/src/python/py_wem_ops.cpp:24-208).  Each thread owns output
 // elements, so results do not depend on the launch shape.
 #include <cuda_runtime.h>
@@ -64,7 +64,96 @@ __global__ void k_splitstep(const float2* __restrict__ srow, const int* __restri
   }
 }
 
+// Injection forward (Injection.cpp:8-19, 52-62): data[z][x] = (or +=) the sum
+// over the points i at depth z with |x - tap - ix[i]| <= ng of
+// g[x - tap - ix[i] + ng] m_i, m_i = model[off0 + i stride]; one thread per
+// data element, the points in order
+__global__ void k_inject_fwd(const int* __restrict__ iz, const int* __restrict__ ix, int npt,
+                             const float* __restrict__ g, int ng, int tap, int nx, size_t total,
+                             const float2* __restrict__ model, size_t off0, size_t stride, float2* data, int add) {
+  for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const int z = (int)(t / nx), x = (int)(t % nx);
+    float2 acc = make_float2(0.f, 0.f);
+    for (int i = 0; i < npt; ++i) {
+      const int ig = x - tap - ix[i];
+      if (iz[i] != z || ig < -ng || ig > ng) continue;
+      const float w = g[ig + ng];
+      const float2 m = model[off0 + (size_t)i * stride];
+      // the reference's roundings: the product, then the sum
+      acc = make_float2(__fadd_rn(acc.x, __fmul_rn(w, m.x)), __fadd_rn(acc.y, __fmul_rn(w, m.y)));
+    }
+    data[t] = add ? make_float2(data[t].x + acc.x, data[t].y + acc.y) : acc;
+  }
+}
+
+// the gathered value of point i (Injection.cpp:21-33, 64-75): the sum over
+// its window of g[ig + ng] data[iz[i]][ix[i] + ig + tap], inside the row
+__device__ __forceinline__ float2 inject_gather(const int* iz, const int* ix, int i, const float* g, int ng,
+                                                int tap, int nx, const float2* data) {
+  float2 acc = make_float2(0.f, 0.f);
+  for (int ig = -ng; ig <= ng; ++ig) {
+    const int off = ix[i] + ig + tap;
+    if (off < 0 || off >= nx) continue;
+    const float w = g[ig + ng];
+    const float2 d = data[(size_t)iz[i] * nx + off];
+    acc = make_float2(__fadd_rn(acc.x, __fmul_rn(w, d.x)), __fadd_rn(acc.y, __fmul_rn(w, d.y)));
+  }
+  return acc;
+}
+
+// Injection adjoint, one value per point: model[off0 + i stride] +=
+// gather(i) (the model was cleared beforehand unless adding)
+__global__ void k_inject_adj_points(const int* __restrict__ iz, const int* __restrict__ ix, int npt,
+                                    const float* __restrict__ g, int ng, int tap, int nx,
+                                    const float2* __restrict__ data, float2* model, size_t off0, size_t stride) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < npt; i += gridDim.x * blockDim.x) {
+    const float2 v = inject_gather(iz, ix, i, g, ng, tap, nx, data);
+    float2& m = model[off0 + (size_t)i * stride];
+    m = make_float2(m.x + v.x, m.y + v.y);
+  }
+}
+
+// Injection adjoint into one model sample (the 1D form): model[off0] += the
+// sum over every point of gather(i); one CTA of 256 threads, each summing
+// the points i = t (mod 256) in order, then a fixed tree
+__global__ void k_inject_adj_sum(const int* __restrict__ iz, const int* __restrict__ ix, int npt,
+                                 const float* __restrict__ g, int ng, int tap, int nx,
+                                 const float2* __restrict__ data, float2* model, size_t off0) {
+  __shared__ float2 part[256];
+  float2 acc = make_float2(0.f, 0.f);
+  for (int i = threadIdx.x; i < npt; i += 256) {
+    const float2 v = inject_gather(iz, ix, i, g, ng, tap, nx, data);
+    acc = make_float2(acc.x + v.x, acc.y + v.y);
+  }
+  part[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      part[threadIdx.x] = make_float2(part[threadIdx.x].x + part[threadIdx.x + w].x,
+                                      part[threadIdx.x].y + part[threadIdx.x + w].y);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) model[off0] = make_float2(model[off0].x + part[0].x, model[off0].y + part[0].y);
+}
+
 }  // namespace
+
+void launch_inject(const int* iz, const int* ix, int npt, const float* g, int ng, int tap, int nx, int nz, int adj,
+                   float2* model, size_t off0, size_t stride, float2* data, int add, cudaStream_t st) {
+  if (!adj) {
+    const size_t total = (size_t)nx * nz;
+    if (!total) return;
+    k_inject_fwd<<<blocks_for(total), 256, 0, st>>>(iz, ix, npt, g, ng, tap, nx, total, model, off0, stride, data,
+                                                    add);
+  } else if (stride == 0) {
+    k_inject_adj_sum<<<1, 256, 0, st>>>(iz, ix, npt, g, ng, tap, nx, data, model, off0);
+  } else {
+    if (!npt) return;
+    k_inject_adj_points<<<blocks_for((size_t)npt), 256, 0, st>>>(iz, ix, npt, g, ng, tap, nx, data, model, off0,
+                                                                 stride);
+  }
+  note_launch();
+}
 
 void launch_diag_rows(const float2* in, const float2* f, float2* out, int n, int nrow, int conj, int add,
                       cudaStream_t st) {

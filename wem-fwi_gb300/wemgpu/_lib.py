@@ -94,6 +94,7 @@ _SIGS = {
     "wem_ic": (_i, [_v, _i, _i, _v, _v, _i]),
     "wem_phshift": (_i, [_pp, _i, _f, _f, _f, _f, _f, _i, _v, _v, _i, _i]),
     "wem_reflect": (_i, [_v, _v, _i, _i, _i, _v, _v]),
+    "wem_inject": (_i, [_v, _v, _i, _i, _i, _i, _i, _i, _i, _i, _i, _i, _v, _v, _i]),
     "wem_dreflect": (_i, [_v, _v, _i, _i, _i, _v, _v, _v, _i]),
     "lanczos2d_create": (_i, [_i, _f, _i, _f, _i, _f, _i, _f, ctypes.POINTER(_f), ctypes.POINTER(_h)]),
     "spline2d_create": (_i, [_i, _f, _i, _f, _i, _f, _i, _f, _f, _f, ctypes.POINTER(_h)]),

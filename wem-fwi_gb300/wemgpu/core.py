@@ -511,6 +511,30 @@ def phshift(p: WemParams, dx, dz, freq, s, adj, x, out, add=False):
     return out
 
 
+def inject(iz, ix, ng, tap, step, shot, adj, model, data, add=False):
+    """Injection (wem_inject) between a model [nt] or [nshot][npt][nt] and
+    rows data [nz][nx], complex: forward data (+)= the spread point
+    values, adjoint model (+)= the gathered ones."""
+    izs = np.ascontiguousarray(np.asarray(iz, dtype=np.int32).ravel())
+    ixs = np.ascontiguousarray(np.asarray(ix, dtype=np.int32).ravel())
+    if izs.size != ixs.size:
+        raise ValueError("z and x lists differ in length")
+    npt = int(izs.size)
+    if len(model.shape) == 1:
+        nshot, nt = 0, int(model.shape[0])
+    elif len(model.shape) == 3:
+        if int(model.shape[1]) != npt:
+            raise ValueError(f"model has {model.shape[1]} points, the lists {npt}")
+        nshot, nt = int(model.shape[0]), int(model.shape[2])
+    else:
+        raise ValueError("model must be [nt] or [nshot][npoints][nt]")
+    nz, nx = int(data.shape[0]), int(data.shape[1])
+    _lib.call("wem_inject", izs.ctypes.data_as(ctypes.c_void_p), ixs.ctypes.data_as(ctypes.c_void_p), npt, int(ng),
+              int(tap), nx, nz, nt, nshot, int(step), int(shot), int(adj),
+              ptr(model, np.complex64, tuple(model.shape), "model", bool(adj)),
+              ptr(data, np.complex64, (nz, nx), "data", not adj), int(bool(add)))
+
+
 def reflect(slow2, rho, adj, x, out):
     """Reflect of the grid (slow2, rho): out = r x (conj(r) x)."""
     nz, nx = slow2.shape[-2], slow2.shape[-1]

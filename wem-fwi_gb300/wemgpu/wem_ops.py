@@ -228,3 +228,32 @@ class dReflect(_RowOperator):
     def adjoint(self, add, model, data):
         m = model.vecs
         core.dreflect(self.slow[0], self.slow[1], 1, _arr(m[0]), _arr(m[1]), _arr(data), add)
+
+
+class Injection(_RowOperator):
+    """Point injection and its adjoint (Injection.h:19-65,
+    Injection.cpp:8-33, 52-75; wem_ops.py:122-137): the points (z[i], x[i])
+    of the data rows [nz][nx], each spread over x[i] + tap + [-ng, ng] by
+    the cos^2 window.  The model is [nt] (every point takes its sample
+    ``step``) or [nshot][npoints][nt] (point i takes [shot][i][step]);
+    setStep / setShot choose them."""
+
+    def __init__(self, model, data, z, x, ng=0, tap=0):
+        super().__init__(model, data)
+        self.z = [int(v) for v in z]
+        self.x = [int(v) for v in x]
+        self.ng, self.tap = int(ng), int(tap)
+        self.step, self.shot = 0, 0
+
+    def setStep(self, step):
+        self.step = int(step)
+
+    def setShot(self, shot):
+        self.shot = int(shot)
+
+    def forward(self, add, model, data):
+        core.inject(self.z, self.x, self.ng, self.tap, self.step, self.shot, 0, _arr(model), _arr(data), add)
+
+    def adjoint(self, add, model, data):
+        core.inject(self.z, self.x, self.ng, self.tap, self.step, self.shot, 1, _arr(model), _arr(data), add)
+
